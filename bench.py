@@ -1,0 +1,380 @@
+"""Benchmark of the GB300 DiskDyn RK4 step: body-steps/s of the mixed-precision
+integrator on the dusty-ring workload (1.5 Msun star, 2 planets, 4,096 gravitating
+planetesimals, 1,048,576 dust grains with radiation pressure, PR and stellar-wind drag),
+with the plain-FP64 form, the error of mixed against FP64, the dust kernel's roofline, an
+end-to-end figure through the C ABI with host buffers, and a CPU baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0.  Under torchrun every rank integrates its own dust shard of the
+same size against a replica of the massive set (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RK4 body-steps/s (mixed precision, FP64-error stated)"
+UNIT = "body-steps/s"
+WORKLOAD = "dusty_ring"
+# Flops per body-body interaction (Nyland, Harris & Prins, GPU Gems 3 ch. 31) and per
+# star term (gravity reduced by beta + PR/stellar-wind drag), per tracer per stage.
+FLOP_PAIR = 20
+FLOP_STAR = 45
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n-dust", type=int, default=1048576)
+    p.add_argument("--n-plsml", type=int, default=4096)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--err-steps", type=int, default=1000)
+    p.add_argument("--err-dust", type=int, default=16384)
+    p.add_argument("--cpu-sample", type=int, default=262144)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: str):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.index, f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def smi_index(local_rank: int) -> str:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    if vis:
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if local_rank < len(ids):
+            return ids[local_rank]
+    return str(local_rank)
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys, probe_fma_peak
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    def barrier():
+        if dist:
+            dist.barrier()
+    def allmax(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    def allsum(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t)
+        return float(t.item())
+
+    sysm = synth.dusty_ring(n_dust=args.n_dust, n_plsml=args.n_plsml, seed=synth.SEED + 7919 * rank)
+    ng, nd = sysm.n_grav, sysm.n_dust
+    eng = Engine(local)
+    eng.set_size_table(**sysm.size_table)
+    phys = make_phys(**sysm.phys)
+    st0 = DeviceState.from_numpy(sysm.state, device=f"cuda:{local}")
+    st = st0.clone()
+    MIX, F64 = abi.DDX_PREC_MIXED, abi.DDX_PREC_FP64
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    stream = torch.cuda.current_stream()
+
+    def one_step(prec, ev=None):
+        if ev:
+            ev[0].record(stream)
+        eng.stage("massive_rk4", st, ng, sysm.dt, phys, prec)
+        if ev:
+            ev[1].record(stream)
+        eng.stage("small_rk4", st, ng, sysm.dt, phys, prec)
+        if ev:
+            ev[2].record(stream)
+        eng.stage("massive_final", st, ng, sysm.dt, phys, prec)
+        if ev:
+            ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        one_step(MIX)
+    torch.cuda.synchronize()
+    alive0 = int((st.N[ng:] != 0).sum().item())
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(smi_index(local)) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            one_step(MIX, evs[k])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier()
+    step_ms = [e[0].elapsed_time(e[3]) for e in evs]
+    dust_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    alive1 = int((st.N[ng:] != 0).sum().item())
+    t_total = allmax(sum(step_ms) / 1e3)
+    units = allsum((ng + 0.5 * (alive0 + alive1)) * args.steps)
+    value = units / t_total
+
+    # roofline of the dust kernel (FP32-pipe bound in the mixed path)
+    fp32_peak, fp64_peak = probe_fma_peak(local)
+    inter = 4.0 * 0.5 * (alive0 + alive1) * (ng - 1)
+    flops = FLOP_PAIR * inter + FLOP_STAR * 4.0 * 0.5 * (alive0 + alive1)
+    t_dust = statistics.mean(dust_ms) / 1e3
+    achieved = flops / t_dust / 1e12
+
+    # plain FP64 from the same initial state, and the error of mixed against it
+    st = st0.clone()
+    for _ in range(1):
+        one_step(F64)
+    st = st0.clone()
+    f64_evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.fp64_steps)]
+    torch.cuda.synchronize()
+    for k in range(args.fp64_steps):
+        flush.zero_()
+        one_step(F64, f64_evs[k])
+    torch.cuda.synchronize()
+    f64_ms = [e[0].elapsed_time(e[3]) for e in f64_evs]
+    f64_dust_ms = [e[1].elapsed_time(e[2]) for e in f64_evs]
+    ref64 = {k: getattr(st, k).clone() for k in ("x", "y", "z", "N")}
+    f64_value = allsum((ng + alive0) * args.fp64_steps) / allmax(sum(f64_ms) / 1e3)
+    st = st0.clone()
+    for _ in range(args.fp64_steps):
+        one_step(MIX)
+    torch.cuda.synchronize()
+    def rel_err(a, b):
+        live = (a["N"] != 0) & (b.N != 0)
+        d = torch.sqrt((a["x"] - b.x) ** 2 + (a["y"] - b.y) ** 2 + (a["z"] - b.z) ** 2)
+        r = torch.sqrt(a["x"] ** 2 + a["y"] ** 2 + a["z"] ** 2)
+        return (d / r)[live].double().cpu().numpy()
+    e_short = rel_err(ref64, st)
+
+    # long-horizon error: err_steps steps of a smaller shard, mixed vs FP64
+    err_long = None
+    if args.err_steps > 0 and rank == 0:
+        small = synth.dusty_ring(n_dust=args.err_dust, n_plsml=args.n_plsml, seed=synth.SEED + 17)
+        sa = DeviceState.from_numpy(small.state)
+        sb = DeviceState.from_numpy(small.state)
+        eng.evolve(sa, small.n_grav, small.dt, args.err_steps, phys, F64)
+        eng.evolve(sb, small.n_grav, small.dt, args.err_steps, phys, MIX)
+        torch.cuda.synchronize()
+        ea = rel_err({k: getattr(sa, k) for k in ("x", "y", "z", "N")}, sb)
+        dm = torch.sqrt((sa.x[:small.n_grav] - sb.x[:small.n_grav]) ** 2 + (sa.y[:small.n_grav] - sb.y[:small.n_grav]) ** 2
+                        + (sa.z[:small.n_grav] - sb.z[:small.n_grav]) ** 2)
+        rm = torch.sqrt(sa.x[:small.n_grav] ** 2 + sa.y[:small.n_grav] ** 2 + sa.z[:small.n_grav] ** 2)
+        err_long = {"steps": args.err_steps, "n_dust": args.err_dust, "n_grav": small.n_grav,
+                    "dust_rel_pos_err_median": float(np.median(ea)),
+                    "dust_rel_pos_err_p90": float(np.quantile(ea, 0.9)),
+                    "dust_rel_pos_err_p99": float(np.quantile(ea, 0.99)),
+                    "dust_rel_pos_err_max": float(ea.max()),
+                    "massive_rel_pos_err_max": float((dm[1:] / rm[1:]).max().item())}
+
+    # end to end through the C ABI with host buffers: per step, H2D of the state from
+    # pinned memory, the step, D2H of the updated state
+    host = {k: getattr(st0, k).cpu().pin_memory() for k in ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id")}
+    out = {k: torch.empty_like(host[k]).pin_memory() for k in ("x", "y", "z", "vx", "vy", "vz", "N")}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = sum(t.numel() * t.element_size() for t in out.values())
+    st = st0.clone()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = []
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for f, t in host.items():
+            getattr(st, f).copy_(t, non_blocking=True)
+        eng.step(st, ng, sysm.dt, phys, MIX)
+        for f, t in out.items():
+            t.copy_(getattr(st, f), non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+    e2e_value = allsum((ng + alive0) * args.steps) / allmax(sum(e2e_ms) / 1e3)
+
+    peaks = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 state + f32 perturbations (mixed)",
+        "data": "synthetic (seeded Philox), dusty-ring configuration",
+        "config": {"workload": WORKLOAD, "n_grav": ng, "n_dust_per_gpu": nd, "n_planetesimals": args.n_plsml,
+                   "dt_yr": sysm.dt, "precision": "mixed", "physics": "radiation+PR+stellar-wind drag",
+                   "l2": "flushed between timed steps (256 MiB write)"},
+        "wall_s_timed_region": wall,
+        "fp64": {"value": f64_value, "unit": UNIT, "ms_per_step": statistics.mean(f64_ms),
+                 "steps": args.fp64_steps, "dust_kernel_ms": statistics.mean(f64_dust_ms)},
+        "mixed_over_fp64": value / f64_value,
+        "error_vs_fp64": {"steps": args.fp64_steps, "dust_rel_pos_err_median": float(np.median(e_short)),
+                          "dust_rel_pos_err_max": float(e_short.max())},
+        "error_vs_fp64_long": err_long,
+        "roofline": {"kernel": "dust_rk4_kernel<mixed>", "bound": "fp32_pipe", "achieved": achieved,
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "peak_source": "ddx_probe_fma_peak (FMA chains, measured in this run); "
+                                    "MEASURED_PEAKS.json has no FP32/FP64 pipe figure",
+                     "flops_per_launch": flops, "dust_kernel_ms": t_dust * 1e3,
+                     "fp64_peak_tflops": fp64_peak, "traffic": None,
+                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(sysm, args.cpu_sample)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(sysm, n_sample):
+    """The FP64 CPU oracle (OpenMP, every host core) on one step of a sample of the same
+    workload: all massive bodies and the first n_sample grains."""
+    import oracle.cpu as oc
+    ng = sysm.n_grav
+    n_sample = min(n_sample, sysm.n_dust)
+    sub = {k: v[:ng + n_sample].copy() for k, v in sysm.state.items()}
+    t0 = time.perf_counter()
+    oc.step(sub, ng, sysm.dt, sysm.size_table, sysm.phys, 1)
+    t = time.perf_counter() - t0
+    return {"value": (ng + n_sample) / t, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"1 FP64 step of {ng} massive bodies + {n_sample} grains of the same workload"}
+
+
+def run_reference(args, world, rank, local):
+    """Reference arm: the reference's hot path on the host cores -- it has no CPU
+    implementation of its own, so the oracle port (FP64, OpenMP over all cores) -- on the
+    same workload, each step a bounded sample of it.  The reference's own CUDA kernels
+    (compiled unmodified for sm_103a) are timed beside it on one full-size step."""
+    if rank != 0:
+        return
+    import oracle.cpu as oc
+    from diskdyn_gb300 import synth
+    sysm = synth.dusty_ring(n_dust=args.n_dust, n_plsml=args.n_plsml)
+    ng = sysm.n_grav
+    n_sample = min(65536, sysm.n_dust)
+    sub = {k: v[:ng + n_sample].copy() for k, v in sysm.state.items()}
+    for _ in range(args.warmup):
+        oc.step(sub, ng, sysm.dt, sysm.size_table, sysm.phys, 1)
+    t0 = time.perf_counter()
+    cur = sub
+    for _ in range(args.steps):
+        cur = oc.step(cur, ng, sysm.dt, sysm.size_table, sysm.phys, 1)
+    t = time.perf_counter() - t0
+    value = (ng + n_sample) * args.steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox), dusty-ring configuration",
+            "config": {"workload": WORKLOAD, "n_grav": ng, "n_dust_per_gpu": args.n_dust,
+                       "n_planetesimals": args.n_plsml, "dt_yr": sysm.dt, "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"each step: {ng} massive bodies + {n_sample} grains of the workload"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    try:
+        import oracle.refk as rk
+        if rk.available():
+            _, ms = rk.step(sysm.state, ng, sysm.dt, sysm.size_table, sysm.phys, 1, return_ms=True)
+            line["reference_cuda_gb300"] = {
+                "value": (ng + sysm.n_dust) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+                "what": "the reference's own kernels compiled unmodified for sm_103a, one full step, CUDA events"}
+    except Exception as e:  # the GPU leg is informative only
+        line["reference_cuda_gb300"] = {"unavailable": str(e)[:200]}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, local)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

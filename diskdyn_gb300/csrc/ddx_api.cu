@@ -1,0 +1,355 @@
+// C ABI of the DiskDyn GB300 path: context, tables and the stream-ordered launch
+// sequences behind ddx_step / ddx_evolve / ddx_image / ddx_sed.
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include "ddx_internal.cuh"
+#include "ddx_flux.cuh"
+
+using namespace ddx;
+
+struct ddx_ctx {
+    int device = 0;
+    // size-bin table
+    int n_grid = 0;
+    SizeBin* bins = nullptr;
+    double* size_d = nullptr;
+    // massive-set scratch
+    MassiveScratch ms{};
+    // optics
+    bool optics_set = false;
+    OpticsDev od{};
+    OpticsDev* od_dev = nullptr;
+    double *w = nullptr, *in = nullptr, *Qabs = nullptr, *Qsca = nullptr, *Qp = nullptr,
+           *Td = nullptr, *lQp = nullptr, *lTd = nullptr, *w5 = nullptr;
+    ViewConst* vc = nullptr;
+    double* sed_partial = nullptr;
+    int sed_partial_cap = 0;
+    unsigned long long* counters = nullptr;   // [0]: tracers that took the exact pixel path
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? DDX_OK : DDX_ERR_CUDA; }
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void**)p, sizeof(T) * n);
+}
+
+void free_massive(MassiveScratch& ms) {
+    cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.A); cudaFree(ms.R);
+    ms = MassiveScratch{};
+}
+
+int ensure_massive(ddx_ctx* c, int n_grav) {
+    if (c->ms.cap >= n_grav && c->ms.P) return DDX_OK;
+    free_massive(c->ms);
+    int cap = 64;
+    while (cap < n_grav) cap *= 2;
+    MassiveScratch ms{};
+    ms.cap = cap;
+    if (dalloc(&ms.P, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.Phi, (size_t)4 * cap) != cudaSuccess ||
+        dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess ||
+        dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess) {
+        free_massive(ms);
+        cudaGetLastError();
+        return DDX_ERR_NOMEM;
+    }
+    c->ms = ms;
+    return DDX_OK;
+}
+
+bool state_ok(const ddx_state* s) {
+    return s && s->x && s->y && s->z && s->vx && s->vy && s->vz && s->m && s->N && s->id;
+}
+
+int make_step_args(const ddx_phys* p, int n_grav, int n_dust, double dt, int mode, StepArgs& a) {
+    if (!p || n_grav < 1 || n_dust < 0) return DDX_ERR_ARG;
+    if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
+    a.n_grav = n_grav;
+    a.n_dust = n_dust;
+    a.dt = dt;
+    a.dt2 = dt * 0.5;          // src/grid.cu:711,716 pass dt*0.5
+    a.dt6 = dt / 6.0;          // src/grid.cu:750 passes dt/6.0
+    a.SWQ = p->SWQ;
+    a.FLQ = p->FLQ;
+    a.Wz = p->Wz;
+    a.Bstar = p->Bstar;
+    a.Rstar = p->Rstar;
+    a.vswAU = p->vsw_AUyr;
+    a.Rmin = p->Rmin;
+    a.mode = mode;
+    return DDX_OK;
+}
+
+// Star-only systems: the reference never runs the massive stages when n_grav <= 1
+// (src/grid.cu:698, 747), so its stage arrays keep the zeros written at set-up and the
+// star never moves.  DDX_MODE_REFERENCE reproduces that; DDX_MODE_FIXED advances the star
+// ballistically through the regular passes.
+__global__ void star_only_reference_kernel(ddx_state s, MassiveScratch ms) {
+    if (threadIdx.x < 4) {
+        const double m = s.m[0];
+        ms.P[threadIdx.x * ms.cap] = make_body(0.0, 0.0, 0.0, m);
+        ms.Phi[threadIdx.x * ms.cap] = make_float4(0.f, 0.f, 0.f, (float)m);
+        ms.Plo[threadIdx.x * ms.cap] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+int enqueue_step(ddx_ctx* c, const ddx_state& s, const StepArgs& a, int precision, cudaStream_t st) {
+    if (a.n_grav == 1 && a.mode == DDX_MODE_REFERENCE) {
+        star_only_reference_kernel<<<1, 32, 0, st>>>(s, c->ms);
+        if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
+        return cuda_status(launch_dust(s, a, c->ms, c->bins, precision, st));
+    }
+    if (launch_massive_prepare(s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
+    if (launch_massive_pass1(s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
+    if (launch_massive_pass2(s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
+    return cuda_status(launch_dust(s, a, c->ms, c->bins, precision, st));
+}
+
+void free_optics(ddx_ctx* c) {
+    cudaFree(c->w); cudaFree(c->in); cudaFree(c->Qabs); cudaFree(c->Qsca); cudaFree(c->Qp);
+    cudaFree(c->Td); cudaFree(c->lQp); cudaFree(c->lTd); cudaFree(c->w5);
+    c->w = c->in = c->Qabs = c->Qsca = c->Qp = c->Td = c->lQp = c->lTd = c->w5 = nullptr;
+    c->optics_set = false;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ddx_abi_version(void) { return DDX_ABI_VERSION; }
+
+const char* ddx_status_string(int status) {
+    switch (status) {
+        case DDX_OK: return "ok";
+        case DDX_ERR_ARG: return "invalid argument";
+        case DDX_ERR_CUDA: return "CUDA runtime error";
+        case DDX_ERR_NOMEM: return "device allocation failed";
+        case DDX_ERR_STATE: return "required table not set";
+        case DDX_ERR_RANGE: return "size beyond limit";
+        case DDX_ERR_TIMEOUT: return "device-side wait timed out";
+        case DDX_ERR_NONFINITE: return "non-finite value";
+        default: return "unknown status";
+    }
+}
+
+int ddx_create(ddx_ctx** out, int device) {
+    if (!out) return DDX_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return DDX_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return DDX_ERR_CUDA;
+    ddx_ctx* c = new ddx_ctx();
+    c->device = device;
+    if (dalloc(&c->vc, 1) != cudaSuccess || dalloc(&c->od_dev, 1) != cudaSuccess ||
+        dalloc(&c->counters, 4) != cudaSuccess) {
+        cudaFree(c->vc); cudaFree(c->od_dev); cudaFree(c->counters);
+        delete c;
+        return DDX_ERR_NOMEM;
+    }
+    cudaMemset(c->counters, 0, 4 * sizeof(unsigned long long));
+    *out = c;
+    return DDX_OK;
+}
+
+int ddx_destroy(ddx_ctx* c) {
+    if (!c) return DDX_ERR_ARG;
+    cudaSetDevice(c->device);
+    free_massive(c->ms);
+    free_optics(c);
+    cudaFree(c->bins); cudaFree(c->size_d); cudaFree(c->vc); cudaFree(c->od_dev);
+    cudaFree(c->sed_partial); cudaFree(c->counters);
+    delete c;
+    return DDX_OK;
+}
+
+int ddx_set_size_table(ddx_ctx* c, int n_grid, const double* size, const float* beta,
+                       const float* betasw, const float* q) {
+    if (!c || n_grid < 0 || (n_grid > 0 && (!size || !beta || !betasw || !q))) return DDX_ERR_ARG;
+    if (n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
+    cudaSetDevice(c->device);
+    std::vector<SizeBin> h(n_grid > 0 ? n_grid : 1);
+    for (int k = 0; k < n_grid; ++k) h[k] = SizeBin{beta[k], betasw[k], q[k], 0.f};
+    cudaFree(c->bins); cudaFree(c->size_d);
+    c->bins = nullptr; c->size_d = nullptr;
+    if (dalloc(&c->bins, h.size()) != cudaSuccess || dalloc(&c->size_d, h.size()) != cudaSuccess)
+        return DDX_ERR_NOMEM;
+    if (cudaMemcpy(c->bins, h.data(), sizeof(SizeBin) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return DDX_ERR_CUDA;
+    if (n_grid > 0 && cudaMemcpy(c->size_d, size, sizeof(double) * n_grid, cudaMemcpyHostToDevice) != cudaSuccess)
+        return DDX_ERR_CUDA;
+    c->n_grid = n_grid;
+    if (c->optics_set) c->od.size = c->size_d;
+    return DDX_OK;
+}
+
+int ddx_set_optics(ddx_ctx* c, int n_grid, int n_wav, int n_theta, const double* w,
+                   const double* in, const double* Qabs, const double* Qsca,
+                   const double* Qpfunc, const double* Td, double Rmin, double Rmax) {
+    if (!c || n_grid < 1 || n_wav < 1 || n_theta < 2 || !w || !in || !Qabs || !Qsca || !Qpfunc || !Td)
+        return DDX_ERR_ARG;
+    if (n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
+    if (!(Rmin > 0.0) || !(Rmax > Rmin)) return DDX_ERR_ARG;
+    if (c->n_grid != n_grid) return DDX_ERR_STATE;   // the size table gives the grain sizes
+    cudaSetDevice(c->device);
+    free_optics(c);
+    const size_t nq = (size_t)n_grid * n_theta * n_wav, nw = (size_t)n_grid * n_wav,
+                 nt = (size_t)n_grid * DDX_NR;
+    if (dalloc(&c->w, n_wav) || dalloc(&c->in, n_wav) || dalloc(&c->Qabs, nw) || dalloc(&c->Qsca, nw) ||
+        dalloc(&c->Qp, nq) || dalloc(&c->Td, nt) || dalloc(&c->lQp, nq) || dalloc(&c->lTd, nt) ||
+        dalloc(&c->w5, n_wav)) {
+        free_optics(c);
+        cudaGetLastError();
+        return DDX_ERR_NOMEM;
+    }
+    cudaError_t e = cudaSuccess;
+    e = e ? e : cudaMemcpy(c->w, w, sizeof(double) * n_wav, cudaMemcpyHostToDevice);
+    e = e ? e : cudaMemcpy(c->in, in, sizeof(double) * n_wav, cudaMemcpyHostToDevice);
+    e = e ? e : cudaMemcpy(c->Qabs, Qabs, sizeof(double) * nw, cudaMemcpyHostToDevice);
+    e = e ? e : cudaMemcpy(c->Qsca, Qsca, sizeof(double) * nw, cudaMemcpyHostToDevice);
+    e = e ? e : cudaMemcpy(c->Qp, Qpfunc, sizeof(double) * nq, cudaMemcpyHostToDevice);
+    e = e ? e : cudaMemcpy(c->Td, Td, sizeof(double) * nt, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { free_optics(c); return DDX_ERR_CUDA; }
+    OpticsDev& o = c->od;
+    o.w = c->w; o.in = c->in; o.Qabs = c->Qabs; o.Qsca = c->Qsca; o.Qp = c->Qp; o.Td = c->Td;
+    o.size = c->size_d; o.lQp = c->lQp; o.lTd = c->lTd; o.w5 = c->w5;
+    o.Rmin = Rmin; o.Rmax = Rmax; o.fR = 0.0;
+    o.n_grid = n_grid; o.n_wav = n_wav; o.n_theta = n_theta;
+    if (cudaMemcpy(c->od_dev, &o, sizeof(OpticsDev), cudaMemcpyHostToDevice) != cudaSuccess) return DDX_ERR_CUDA;
+    if (launch_optics_prepare(o, c->od_dev, 0) != cudaSuccess) return DDX_ERR_CUDA;
+    if (cudaMemcpy(&o, c->od_dev, sizeof(OpticsDev), cudaMemcpyDeviceToHost) != cudaSuccess) return DDX_ERR_CUDA;
+    c->optics_set = true;
+    return DDX_OK;
+}
+
+int ddx_step(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
+             const ddx_phys* phys, int precision, int mode, void* stream) {
+    return ddx_evolve(c, s, n_grav, n_dust, dt, 1, phys, precision, mode, stream);
+}
+
+int ddx_evolve(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,
+               const ddx_phys* phys, int precision, int mode, void* stream) {
+    if (!c || !state_ok(s) || n_steps < 0) return DDX_ERR_ARG;
+    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (!c->bins) return DDX_ERR_STATE;
+    StepArgs a;
+    int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
+    if (r) return r;
+    cudaSetDevice(c->device);
+    if ((r = ensure_massive(c, n_grav))) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int k = 0; k < n_steps; ++k)
+        if ((r = enqueue_step(c, *s, a, precision, st))) return r;
+    return DDX_OK;
+}
+
+namespace {
+int prepare_call(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
+                 const ddx_phys* phys, int precision, int mode, StepArgs& a) {
+    if (!c || !state_ok(s)) return DDX_ERR_ARG;
+    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (!c->bins) return DDX_ERR_STATE;
+    int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
+    if (r) return r;
+    cudaSetDevice(c->device);
+    return ensure_massive(c, n_grav);
+}
+}  // namespace
+
+int ddx_massive_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
+                    const ddx_phys* phys, int precision, int mode, void* stream) {
+    StepArgs a;
+    int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
+    if (r) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (a.n_grav == 1 && a.mode == DDX_MODE_REFERENCE) {
+        star_only_reference_kernel<<<1, 32, 0, st>>>(*s, c->ms);
+        return cuda_status(cudaGetLastError());
+    }
+    if (launch_massive_prepare(*s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
+    return cuda_status(launch_massive_pass1(*s, a, c->ms, precision, st));
+}
+
+int ddx_small_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
+                  const ddx_phys* phys, int precision, int mode, void* stream) {
+    StepArgs a;
+    int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
+    if (r) return r;
+    return cuda_status(launch_dust(*s, a, c->ms, c->bins, precision, (cudaStream_t)stream));
+}
+
+int ddx_massive_final(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
+                      const ddx_phys* phys, int precision, int mode, void* stream) {
+    StepArgs a;
+    int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
+    if (r) return r;
+    if (a.n_grav == 1 && a.mode == DDX_MODE_REFERENCE) return DDX_OK;
+    return cuda_status(launch_massive_pass2(*s, a, c->ms, precision, (cudaStream_t)stream));
+}
+
+int ddx_image(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_view* view,
+              const int* wj, int n_img, double* Fd, int precision, void* stream) {
+    if (!c || !state_ok(s) || !view || !wj || !Fd || n_grav < 0 || n_dust < 0) return DDX_ERR_ARG;
+    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (n_img < 1 || view->xsize < 1 || view->ysize < 1 || !(view->fov > 0.0) || !(view->dist > 0.0))
+        return DDX_ERR_ARG;
+    if (n_img > kMaxImages) return DDX_ERR_RANGE;
+    if (!c->optics_set) return DDX_ERR_STATE;
+    ImageList il;
+    il.n = n_img;
+    for (int k = 0; k < n_img; ++k) {
+        if (wj[k] < 0 || wj[k] >= c->od.n_wav) return DDX_ERR_ARG;
+        il.wj[k] = wj[k];
+    }
+    cudaSetDevice(c->device);
+    return cuda_status(launch_image(*s, n_grav, n_dust, *view, c->od, il, c->vc, Fd, c->counters,
+                                    (cudaStream_t)stream));
+}
+
+int ddx_sed(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_view* view,
+            double* Fsed, int precision, int mode, void* stream) {
+    if (!c || !state_ok(s) || !view || !Fsed || n_grav < 0 || n_dust < 0) return DDX_ERR_ARG;
+    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
+    if (!(view->dist > 0.0)) return DDX_ERR_ARG;
+    if (!c->optics_set) return DDX_ERR_STATE;
+    cudaSetDevice(c->device);
+    const int nb = sed_blocks(n_dust);
+    const int need = nb * c->od.n_wav;
+    if (need > c->sed_partial_cap) {
+        cudaFree(c->sed_partial);
+        c->sed_partial = nullptr;
+        c->sed_partial_cap = 0;
+        if (dalloc(&c->sed_partial, need) != cudaSuccess) return DDX_ERR_NOMEM;
+        c->sed_partial_cap = need;
+    }
+    return cuda_status(launch_sed(*s, n_grav, n_dust, *view, c->od, c->vc, c->sed_partial, mode,
+                                  Fsed, (cudaStream_t)stream));
+}
+
+int ddx_debug_pixels(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_view* view,
+                     int* pix, int* exact) {
+    if (!c || !state_ok(s) || !view || !pix || !exact || n_grav < 0 || n_dust < 0) return DDX_ERR_ARG;
+    if (view->xsize < 1 || view->ysize < 1 || !(view->fov > 0.0)) return DDX_ERR_ARG;
+    cudaSetDevice(c->device);
+    const int n_theta = c->optics_set ? c->od.n_theta : 2;
+    return cuda_status(launch_pixels(*s, n_grav, n_dust, *view, n_theta, c->vc, pix, exact, 0));
+}
+
+// Number of tracers that took the exact (reference-sequence) pixel path since the
+// context was created; a diagnostic for the guard band of ddx_image.
+unsigned long long ddx_debug_exact_pixel_count(ddx_ctx* c) {
+    if (!c) return 0;
+    unsigned long long h = 0;
+    cudaMemcpy(&h, c->counters, sizeof(h), cudaMemcpyDeviceToHost);
+    return h;
+}
+
+}  // extern "C"

@@ -1,0 +1,461 @@
+// RK4 step of the DiskDyn system on sm_103a.
+//
+// Reference behaviour (src/gpu_functions.cu:71-943, launch sequence src/grid.cu:693-752):
+//   massive set : k1x = x; k2x = x + v dt/2; k2r = v + k1v dt/2; k3x = x + k2r dt/2;
+//                 k3r = v + k2v dt/2; k4x = x + k3r dt; k4r = v + k3v dt;
+//                 kNv = sum_j m_j (x_j - x_i)/r^3 at stage N;  x += dt/6 (v + 2k2r + 2k3r + k4r);
+//                 v += dt/6 (k1v + 2k2v + 2k3v + k4v).
+//   dust        : the same four stages per tracer, with the star term (gravity reduced by
+//                 beta + beta_sw, PR + stellar-wind drag, optional Lorentz force) and the
+//                 gravity of massive bodies 1..n_grav-1 taken at their stage positions.
+//
+// Because k2x depends only on x, v and k3x only on k1v, k4x only on k2v, the four massive
+// force evaluations need two dependent passes: pass 1 evaluates A1 (at P1) and A2 (at P2),
+// pass 2 evaluates A3 (at P3) and A4 (at P4).  The reference issues 4*(num+1)+4 launches
+// per step with CAS atomics; here it is prepare + pass1 + pass2 + dust, deterministic, with
+// no atomics.
+#include "ddx_internal.cuh"
+
+namespace ddx {
+
+// ---------------------------------------------------------------------------------------
+// Massive set
+// ---------------------------------------------------------------------------------------
+
+// P1 = x, P2 = x + v dt/2 (src/gpu_functions.cu:90-99, 219-230).
+__global__ void massive_prepare_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int prec) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_grav) return;
+    const double x = s.x[i], y = s.y[i], z = s.z[i], m = s.m[i];
+    const double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+    const double x2 = x + vx * a.dt2, y2 = y + vy * a.dt2, z2 = z + vz * a.dt2;
+    ms.P[0 * ms.cap + i] = make_body(x, y, z, m);
+    ms.P[1 * ms.cap + i] = make_body(x2, y2, z2, m);
+    if (prec == DDX_PREC_MIXED) {
+        float4 h, l;
+        split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
+        h.w = (float)m; l.w = 0.f;
+        ms.Phi[0 * ms.cap + i] = h; ms.Plo[0 * ms.cap + i] = l;
+        split_hilo(x2, h.x, l.x); split_hilo(y2, h.y, l.y); split_hilo(z2, h.z, l.z);
+        ms.Phi[1 * ms.cap + i] = h; ms.Plo[1 * ms.cap + i] = l;
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void kahan_add(float& S, float& C, float v) {
+    const float y = v - C;
+    const float t = S + y;
+    C = (t - S) - y;
+    S = t;
+}
+
+// Acceleration of body i from body j (FP64): m_j (x_j - x_i)/r^3; zero for coincident
+// bodies, like the reference's f != 0 test (src/gpu_functions.cu:156-172).
+__device__ __forceinline__ void pair64(const Body pi, const Body pj, double& ax,
+                                       double& ay, double& az) {
+    const double dX = pj.x - pi.x, dY = pj.y - pi.y, dZ = pj.z - pi.z;
+    const double RR = dX * dX + dY * dY + dZ * dZ;
+    if (RR > 0.0) {
+        const double ri = rsqrt(RR);
+        const double f = pj.m * (ri * ri * ri);
+        ax = fma(f, dX, ax); ay = fma(f, dY, ay); az = fma(f, dZ, az);
+    }
+}
+
+// Same in FP32 on hi/lo split positions: the difference (hi_j - hi_i) + (lo_j - lo_i)
+// keeps FP32 relative precision in the separation even when |x| >> |x_j - x_i|.
+__device__ __forceinline__ void pair32(const float4 hi, const float4 li, const float4 hj,
+                                       const float4 lj, float& fx, float& fy, float& fz) {
+    const float dX = (hj.x - hi.x) + (lj.x - li.x);
+    const float dY = (hj.y - hi.y) + (lj.y - li.y);
+    const float dZ = (hj.z - hi.z) + (lj.z - li.z);
+    const float RR = fmaf(dX, dX, fmaf(dY, dY, dZ * dZ));
+    if (RR > 0.f) {
+        const float ri = rsqrtf(RR);
+        const float f = hj.w * (ri * (ri * ri));
+        fx = fmaf(f, dX, fx); fy = fmaf(f, dY, fy); fz = fmaf(f, dZ, fz);
+    }
+}
+
+// One warp per target body i, lanes stride over the sources, fixed-order butterfly
+// reduction (deterministic).  Evaluates the accelerations at two stages sa, sb at once.
+// In the mixed path every pair that involves the star (index 0) stays FP64; the other
+// pairs run in FP32 with a per-lane Kahan sum.
+template <int PREC>
+__device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms, int ng, int i,
+                                                         int sa, int sb, double a_out[6]) {
+    const int lane = threadIdx.x & 31;
+    double ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+    const Body pa = ms.P[sa * ms.cap + i];
+    const Body pb = ms.P[sb * ms.cap + i];
+    if (PREC == DDX_PREC_FP64) {
+        for (int j = lane; j < ng; j += 32) {
+            if (j == i) continue;
+            pair64(pa, ms.P[sa * ms.cap + j], ax, ay, az);
+            pair64(pb, ms.P[sb * ms.cap + j], bx, by, bz);
+        }
+    } else {
+        float Sa[3] = {0.f, 0.f, 0.f}, Ca[3] = {0.f, 0.f, 0.f};
+        float Sb[3] = {0.f, 0.f, 0.f}, Cb[3] = {0.f, 0.f, 0.f};
+        const float4 ha = ms.Phi[sa * ms.cap + i], la = ms.Plo[sa * ms.cap + i];
+        const float4 hb = ms.Phi[sb * ms.cap + i], lb = ms.Plo[sb * ms.cap + i];
+        for (int j = lane; j < ng; j += 32) {
+            if (j == i) continue;
+            if (i == 0 || j == 0) {
+                pair64(pa, ms.P[sa * ms.cap + j], ax, ay, az);
+                pair64(pb, ms.P[sb * ms.cap + j], bx, by, bz);
+            } else {
+                float fx = 0.f, fy = 0.f, fz = 0.f;
+                pair32(ha, la, ms.Phi[sa * ms.cap + j], ms.Plo[sa * ms.cap + j], fx, fy, fz);
+                kahan_add(Sa[0], Ca[0], fx); kahan_add(Sa[1], Ca[1], fy); kahan_add(Sa[2], Ca[2], fz);
+                fx = fy = fz = 0.f;
+                pair32(hb, lb, ms.Phi[sb * ms.cap + j], ms.Plo[sb * ms.cap + j], fx, fy, fz);
+                kahan_add(Sb[0], Cb[0], fx); kahan_add(Sb[1], Cb[1], fy); kahan_add(Sb[2], Cb[2], fz);
+            }
+        }
+        ax += (double)Sa[0] - (double)Ca[0]; ay += (double)Sa[1] - (double)Ca[1];
+        az += (double)Sa[2] - (double)Ca[2];
+        bx += (double)Sb[0] - (double)Cb[0]; by += (double)Sb[1] - (double)Cb[1];
+        bz += (double)Sb[2] - (double)Cb[2];
+    }
+    a_out[0] = warp_sum(ax); a_out[1] = warp_sum(ay); a_out[2] = warp_sum(az);
+    a_out[3] = warp_sum(bx); a_out[4] = warp_sum(by); a_out[5] = warp_sum(bz);
+}
+
+__device__ __forceinline__ void store_stage_pos(MassiveScratch& ms, int stage, int i, double x,
+                                                double y, double z, double m, int prec) {
+    ms.P[stage * ms.cap + i] = make_body(x, y, z, m);
+    if (prec == DDX_PREC_MIXED) {
+        float4 h, l;
+        split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
+        h.w = (float)m; l.w = 0.f;
+        ms.Phi[stage * ms.cap + i] = h; ms.Plo[stage * ms.cap + i] = l;
+    }
+}
+
+// Pass 1: A1 at P1, A2 at P2; then R2, P3, R3, P4 for the target
+// (src/gpu_functions.cu:219-230, 350-362, 482-493).
+template <int PREC>
+__global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.n_grav) return;  // warp-uniform
+    double acc[6];
+    massive_two_stage_accel<PREC>(ms, a.n_grav, i, 0, 1, acc);
+    if ((threadIdx.x & 31) != 0) return;
+    const int c = ms.cap;
+    double* A = ms.A;
+    double* R = ms.R;
+    A[(0 * 3 + 0) * c + i] = acc[0]; A[(0 * 3 + 1) * c + i] = acc[1]; A[(0 * 3 + 2) * c + i] = acc[2];
+    A[(1 * 3 + 0) * c + i] = acc[3]; A[(1 * 3 + 1) * c + i] = acc[4]; A[(1 * 3 + 2) * c + i] = acc[5];
+    const double x = s.x[i], y = s.y[i], z = s.z[i], m = s.m[i];
+    const double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+    const double k2rx = vx + acc[0] * a.dt2, k2ry = vy + acc[1] * a.dt2, k2rz = vz + acc[2] * a.dt2;
+    const double k3x = x + k2rx * a.dt2, k3y = y + k2ry * a.dt2, k3z = z + k2rz * a.dt2;
+    const double k3rx = vx + acc[3] * a.dt2, k3ry = vy + acc[4] * a.dt2, k3rz = vz + acc[5] * a.dt2;
+    const double k4x = x + k3rx * a.dt, k4y = y + k3ry * a.dt, k4z = z + k3rz * a.dt;
+    R[(0 * 3 + 0) * c + i] = k2rx; R[(0 * 3 + 1) * c + i] = k2ry; R[(0 * 3 + 2) * c + i] = k2rz;
+    R[(1 * 3 + 0) * c + i] = k3rx; R[(1 * 3 + 1) * c + i] = k3ry; R[(1 * 3 + 2) * c + i] = k3rz;
+    store_stage_pos(ms, 2, i, k3x, k3y, k3z, m, PREC);
+    store_stage_pos(ms, 3, i, k4x, k4y, k4z, m, PREC);
+}
+
+// Pass 2: A3 at P3, A4 at P4; R4; final combination (src/gpu_functions.cu:613-625).
+// Reads only stage records of other bodies, so updating x, v of the target is safe.
+template <int PREC>
+__global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.n_grav) return;
+    double acc[6];
+    massive_two_stage_accel<PREC>(ms, a.n_grav, i, 2, 3, acc);
+    if ((threadIdx.x & 31) != 0) return;
+    const int c = ms.cap;
+    double* A = ms.A;
+    const double* R = ms.R;
+    A[(2 * 3 + 0) * c + i] = acc[0]; A[(2 * 3 + 1) * c + i] = acc[1]; A[(2 * 3 + 2) * c + i] = acc[2];
+    A[(3 * 3 + 0) * c + i] = acc[3]; A[(3 * 3 + 1) * c + i] = acc[4]; A[(3 * 3 + 2) * c + i] = acc[5];
+    const double vx = s.vx[i], vy = s.vy[i], vz = s.vz[i];
+    const double k4rx = vx + acc[0] * a.dt, k4ry = vy + acc[1] * a.dt, k4rz = vz + acc[2] * a.dt;
+    const double dt = a.dt6;
+    s.x[i] += dt * (vx + 2.0 * R[(0 * 3 + 0) * c + i] + 2.0 * R[(1 * 3 + 0) * c + i] + k4rx);
+    s.y[i] += dt * (vy + 2.0 * R[(0 * 3 + 1) * c + i] + 2.0 * R[(1 * 3 + 1) * c + i] + k4ry);
+    s.z[i] += dt * (vz + 2.0 * R[(0 * 3 + 2) * c + i] + 2.0 * R[(1 * 3 + 2) * c + i] + k4rz);
+    s.vx[i] += dt * (A[(0 * 3 + 0) * c + i] + 2.0 * A[(1 * 3 + 0) * c + i] + 2.0 * acc[0] + acc[3]);
+    s.vy[i] += dt * (A[(0 * 3 + 1) * c + i] + 2.0 * A[(1 * 3 + 1) * c + i] + 2.0 * acc[1] + acc[4]);
+    s.vz[i] += dt * (A[(0 * 3 + 2) * c + i] + 2.0 * A[(1 * 3 + 2) * c + i] + 2.0 * acc[2] + acc[5]);
+}
+
+// ---------------------------------------------------------------------------------------
+// Dust tracers
+// ---------------------------------------------------------------------------------------
+
+// Variants of the dust kernel.
+enum DustVariant {
+    kDustFP64Exact = 0,  // reference arithmetic expression for expression: m/RR/sqrt(RR)
+    kDustFP64 = 1,       // FP64 with rsqrt
+    kDustMixed = 2,      // FP32 hi/lo perturbations, Kahan over spans of kSpan sources
+};
+
+constexpr int kDustThreads = 256;
+constexpr int kDustTile = 1024;    // sources per shared-memory tile (32 KiB)
+constexpr int kSpan = 8;           // plain FP32 partial sums over this many sources
+constexpr float kFarAway = 1.0e18f;  // padding source position, AU (mass 0)
+
+// Star term of one stage (src/gpu_functions.cu:680-718): gravity reduced by beta+beta_sw,
+// PR + stellar-wind drag, optional Lorentz force.  Returns false when the tracer is
+// inside the sublimation radius.  Written operation for operation like the reference so
+// that the FP64 results agree bit for bit on the same GPU.
+__device__ __forceinline__ bool star_term(double dx, double dy, double dz, double rx, double ry,
+                                          double rz, double m0, float bet, float betsw, float qe,
+                                          double m, const StepArgs& a, double& kx, double& ky,
+                                          double& kz) {
+    const double RR = dx * dx + dy * dy + dz * dz;
+    const double RR3 = RR * sqrt(RR);
+    if (RR <= a.Rmin * a.Rmin) return false;
+    const double Fg = (1.0 - bet - betsw) * m0 / RR3;
+    double Fbase1;
+    if (a.SWQ == 1) Fbase1 = m0 / RR * (bet / kLightAU + betsw / a.vswAU);
+    else            Fbase1 = bet * m0 / kLightAU / RR;
+    const double Fbase2 = (dx * rx + dy * ry + dz * rz) / RR;
+    const double Fdrx = Fbase1 * (Fbase2 * dx + rx);
+    const double Fdry = Fbase1 * (Fbase2 * dy + ry);
+    const double Fdrz = Fbase1 * (Fbase2 * dz + rz);
+    double Flx, Fly;
+    if (a.FLQ == 1) {
+        const double Bz = a.Bstar * a.Rstar * a.Rstar * a.Rstar / RR3;
+        Flx = qe * (ry - a.Wz * dx) * Bz / m;
+        Fly = -qe * (rx + a.Wz * dy) * Bz / m;
+    } else {
+        Flx = 0; Fly = 0;
+    }
+    kx = -Fg * dx - Fdrx + Flx;
+    ky = -Fg * dy - Fdry + Fly;
+    kz = -Fg * dz - Fdrz;
+    return true;
+}
+
+// Gravity of massive bodies 1..n_grav-1 at stage `st` on every tracer of the block.
+// Sources are staged through shared memory tile by tile; every thread of the block takes
+// part in the loads and barriers whether or not its tracer is still alive.
+// Returns false (for the calling thread) on an exact coincidence with a body.
+template <int VAR>
+__device__ __forceinline__ bool dust_perturb(const MassiveScratch& ms, int ng, int st, bool alive,
+                                             double xt, double yt, double zt, double& kx,
+                                             double& ky, double& kz, unsigned char* smem) {
+    const int nsrc = ng - 1;
+    bool ok = true;
+    if (VAR == kDustMixed) {
+        float4* shi = reinterpret_cast<float4*>(smem);
+        float4* slo = shi + kDustTile;
+        float xh, xl, yh, yl, zh, zl;
+        split_hilo(xt, xh, xl); split_hilo(yt, yh, yl); split_hilo(zt, zh, zl);
+        float Sx = 0.f, Sy = 0.f, Sz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
+        for (int base = 0; base < nsrc; base += kDustTile) {
+            const int cnt = min(kDustTile, nsrc - base);
+            const int padded = (cnt + kSpan - 1) / kSpan * kSpan;
+            __syncthreads();
+            for (int k = threadIdx.x; k < padded; k += blockDim.x) {
+                if (k < cnt) {
+                    shi[k] = ms.Phi[st * ms.cap + 1 + base + k];
+                    slo[k] = ms.Plo[st * ms.cap + 1 + base + k];
+                } else {
+                    shi[k] = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
+                    slo[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+            __syncthreads();
+            if (alive) {
+                for (int k = 0; k < padded; k += kSpan) {
+                    float px = 0.f, py = 0.f, pz = 0.f;
+#pragma unroll
+                    for (int u = 0; u < kSpan; ++u) {
+                        const float4 h = shi[k + u];
+                        const float4 l = slo[k + u];
+                        const float dX = (xh - h.x) + (xl - l.x);
+                        const float dY = (yh - h.y) + (yl - l.y);
+                        const float dZ = (zh - h.z) + (zl - l.z);
+                        const float RR = fmaf(dX, dX, fmaf(dY, dY, dZ * dZ));
+                        const float ri = rsqrtf(RR);
+                        const float f = h.w * (ri * (ri * ri));
+                        px = fmaf(-f, dX, px); py = fmaf(-f, dY, py); pz = fmaf(-f, dZ, pz);
+                    }
+                    kahan_add(Sx, Cx, px); kahan_add(Sy, Cy, py); kahan_add(Sz, Cz, pz);
+                }
+            }
+        }
+        const double px = (double)Sx - (double)Cx, py = (double)Sy - (double)Cy,
+                     pz = (double)Sz - (double)Cz;
+        // An exact coincidence makes RR = 0, rsqrtf = inf and the sum NaN.
+        if (alive && !(isfinite(px) && isfinite(py) && isfinite(pz))) ok = false;
+        kx += px; ky += py; kz += pz;
+    } else {
+        Body* sP = reinterpret_cast<Body*>(smem);
+        for (int base = 0; base < nsrc; base += kDustTile) {
+            const int cnt = min(kDustTile, nsrc - base);
+            __syncthreads();
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+                sP[k] = ms.P[st * ms.cap + 1 + base + k];
+            __syncthreads();
+            if (alive && ok) {
+                if (VAR == kDustFP64Exact) {
+                    // src/gpu_functions.cu:722-735, in order, with its early exit.
+                    for (int k = 0; k < cnt; ++k) {
+                        const Body p = sP[k];
+                        const double dx = xt - p.x, dy = yt - p.y, dz = zt - p.z;
+                        const double RR = dx * dx + dy * dy + dz * dz;
+                        if (RR == 0) { ok = false; break; }
+                        const double f = p.m / RR / sqrt(RR);
+                        kx += -f * dx; ky += -f * dy; kz += -f * dz;
+                    }
+                } else {
+#pragma unroll 4
+                    for (int k = 0; k < cnt; ++k) {
+                        const Body p = sP[k];
+                        const double dx = xt - p.x, dy = yt - p.y, dz = zt - p.z;
+                        const double RR = dx * dx + dy * dy + dz * dz;
+                        const double ri = rsqrt(RR);
+                        const double f = p.m * (ri * ri * ri);
+                        kx = fma(-f, dx, kx); ky = fma(-f, dy, ky); kz = fma(-f, dz, kz);
+                    }
+                }
+            }
+        }
+        if (VAR == kDustFP64 && alive && !(isfinite(kx) && isfinite(ky) && isfinite(kz))) ok = false;
+    }
+    return ok;
+}
+
+// Full RK4 of one dust tracer per thread (src/gpu_functions.cu:627-943).
+template <int VAR>
+__global__ void __launch_bounds__(kDustThreads)
+dust_rk4_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ng = a.n_grav;
+    const int t = ng + i;
+    bool alive = false;
+    double x = 0, y = 0, z = 0, vx = 0, vy = 0, vz = 0, m = 1.0;
+    float bet = 0.f, betsw = 0.f, qe = 0.f;
+    if (i < a.n_dust) {
+        alive = (s.N[t] != 0.0);
+        if (alive) {
+            x = s.x[t]; y = s.y[t]; z = s.z[t];
+            vx = s.vx[t]; vy = s.vy[t]; vz = s.vz[t];
+            m = s.m[t];
+            const int id = s.id[t];
+            if (id >= 0) {
+                const SizeBin b = bins[id];
+                bet = b.beta; betsw = b.betasw; qe = b.q;
+            }
+        }
+    }
+    const double dt = a.dt, dt2 = a.dt / 2.0, dt6 = a.dt / 6.0;
+    double k1vx = 0, k1vy = 0, k1vz = 0, k2vx = 0, k2vy = 0, k2vz = 0;
+    double k3vx = 0, k3vy = 0, k3vz = 0, k4vx = 0, k4vy = 0, k4vz = 0;
+    double k2rx = 0, k2ry = 0, k2rz = 0, k3rx = 0, k3ry = 0, k3rz = 0;
+    double k4rx = 0, k4ry = 0, k4rz = 0;
+    int removed = 0;  // 1: sublimated (stage kept in removed_stage), 2: coincidence
+    int removed_stage = -1;
+
+#pragma unroll 1
+    for (int st = 0; st < 4; ++st) {
+        double xt, yt, zt, rx, ry, rz;
+        if (st == 0)      { xt = x; yt = y; zt = z; rx = vx; ry = vy; rz = vz; }
+        else if (st == 1) {
+            k2rx = vx + k1vx * dt2; k2ry = vy + k1vy * dt2; k2rz = vz + k1vz * dt2;
+            xt = x + vx * dt2; yt = y + vy * dt2; zt = z + vz * dt2;
+            rx = k2rx; ry = k2ry; rz = k2rz;
+        } else if (st == 2) {
+            k3rx = vx + k2vx * dt2; k3ry = vy + k2vy * dt2; k3rz = vz + k2vz * dt2;
+            xt = x + k2rx * dt2; yt = y + k2ry * dt2; zt = z + k2rz * dt2;
+            rx = k3rx; ry = k3ry; rz = k3rz;
+        } else {
+            k4rx = vx + k3vx * dt; k4ry = vy + k3vy * dt; k4rz = vz + k3vz * dt;
+            xt = x + k3rx * dt; yt = y + k3ry * dt; zt = z + k3rz * dt;
+            rx = k4rx; ry = k4ry; rz = k4rz;
+        }
+        double kx = 0, ky = 0, kz = 0;
+        if (alive) {
+            const Body ps = ms.P[st * ms.cap + 0];
+            if (!star_term(xt - ps.x, yt - ps.y, zt - ps.z, rx, ry, rz, ps.m, bet, betsw, qe, m,
+                           a, kx, ky, kz)) {
+                alive = false; removed = 1; removed_stage = st;
+            }
+        }
+        if (!dust_perturb<VAR>(ms, ng, st, alive, xt, yt, zt, kx, ky, kz, smem)) {
+            alive = false; removed = 2; removed_stage = st;
+        }
+        if (st == 0)      { k1vx = kx; k1vy = ky; k1vz = kz; }
+        else if (st == 1) { k2vx = kx; k2vy = ky; k2vz = kz; }
+        else if (st == 2) { k3vx = kx; k3vy = ky; k3vz = kz; }
+        else              { k4vx = kx; k4vy = ky; k4vz = kz; }
+    }
+    if (i >= a.n_dust) return;
+    if (removed) {
+        // src/gpu_functions.cu:878 zeroes N[i] (i is the dust-relative index) on a stage-4
+        // sublimation and leaves the grain alive; DDX_MODE_REFERENCE reproduces it.
+        if (removed == 1 && removed_stage == 3 && a.mode == DDX_MODE_REFERENCE) s.N[i] = 0;
+        else s.N[t] = 0;
+        return;
+    }
+    if (!alive) return;
+    x += dt6 * (vx + 2.0 * (k2rx + k3rx) + k4rx);
+    y += dt6 * (vy + 2.0 * (k2ry + k3ry) + k4ry);
+    z += dt6 * (vz + 2.0 * (k2rz + k3rz) + k4rz);
+    vx += dt6 * (k1vx + 2.0 * (k2vx + k3vx) + k4vx);
+    vy += dt6 * (k1vy + 2.0 * (k2vy + k3vy) + k4vy);
+    vz += dt6 * (k1vz + 2.0 * (k2vz + k3vz) + k4vz);
+    s.x[t] = x; s.y[t] = y; s.z[t] = z;
+    s.vx[t] = vx; s.vy[t] = vy; s.vz[t] = vz;
+}
+
+// ---------------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------------
+
+cudaError_t launch_massive_prepare(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
+                                   int precision, cudaStream_t st) {
+    const int threads = 128;
+    const int blocks = (a.n_grav + threads - 1) / threads;
+    massive_prepare_kernel<<<blocks, threads, 0, st>>>(s, a, ms, precision);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
+                                 int precision, cudaStream_t st) {
+    const int threads = 128;  // 4 targets per block
+    const int blocks = (a.n_grav * 32 + threads - 1) / threads;
+    if (precision == DDX_PREC_MIXED) massive_pass1_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
+    else massive_pass1_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
+                                 int precision, cudaStream_t st) {
+    const int threads = 128;
+    const int blocks = (a.n_grav * 32 + threads - 1) / threads;
+    if (precision == DDX_PREC_MIXED) massive_pass2_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
+    else massive_pass2_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
+                        const SizeBin* bins, int precision, cudaStream_t st) {
+    if (a.n_dust <= 0) return cudaSuccess;
+    const int blocks = (a.n_dust + kDustThreads - 1) / kDustThreads;
+    const size_t smem = (size_t)kDustTile * 32;
+    if (precision == DDX_PREC_MIXED) {
+        dust_rk4_kernel<kDustMixed><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
+    } else if (a.mode == DDX_MODE_REFERENCE) {
+        dust_rk4_kernel<kDustFP64Exact><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
+    } else {
+        dust_rk4_kernel<kDustFP64><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ddx

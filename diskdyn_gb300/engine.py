@@ -1,0 +1,200 @@
+"""Python host interface of the GB300 DiskDyn path, over the C ABI.
+
+`Engine` mirrors the reference's `class Grid` where the hot path is concerned
+(src/ddyn.cuh:213-275): it owns the device-side tables (size bins, optics) and runs the
+step (`massive_RK4 + small_RK4 + massive_final`, src/grid.cu:387-389), the images
+(`null_flux + calc_flux`, src/grid.cu:411-421) and the SED (src/grid.cu:396-406) through
+libddx.so.  The particle state stays in caller-owned torch CUDA tensors in the
+reference's layout: one array per field, massive bodies first, star at index 0.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import abi
+
+STATE_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id")
+
+
+@dataclass
+class DeviceState:
+    """SoA particle state on the GPU (float64 fields, int32 id), n_grav + n_dust long."""
+    x: torch.Tensor
+    y: torch.Tensor
+    z: torch.Tensor
+    vx: torch.Tensor
+    vy: torch.Tensor
+    vz: torch.Tensor
+    m: torch.Tensor
+    N: torch.Tensor
+    id: torch.Tensor
+    _abi: abi.State = field(default=None, repr=False)
+
+    def __post_init__(self):
+        n = self.x.numel()
+        for name in STATE_FIELDS:
+            t = getattr(self, name)
+            want = torch.int32 if name == "id" else torch.float64
+            if t.dtype != want or not t.is_cuda or not t.is_contiguous() or t.numel() != n:
+                raise ValueError(f"state field {name}: need contiguous CUDA {want} of length {n}")
+        self._abi = abi.State(*[getattr(self, f).data_ptr() for f in STATE_FIELDS])
+
+    @property
+    def n_all(self) -> int:
+        return self.x.numel()
+
+    @classmethod
+    def from_numpy(cls, arrays: dict, device="cuda:0", pin: bool = False) -> "DeviceState":
+        ts = {}
+        for f in STATE_FIELDS:
+            a = np.ascontiguousarray(arrays[f], dtype=np.int32 if f == "id" else np.float64)
+            ts[f] = torch.from_numpy(a).to(device)
+        return cls(**ts)
+
+    def copy_from_(self, arrays: dict, non_blocking: bool = False) -> None:
+        for f in STATE_FIELDS:
+            src = arrays[f]
+            if isinstance(src, np.ndarray):
+                src = torch.from_numpy(np.ascontiguousarray(src))
+            getattr(self, f).copy_(src, non_blocking=non_blocking)
+
+    def to_numpy(self) -> dict:
+        return {f: getattr(self, f).cpu().numpy() for f in STATE_FIELDS}
+
+    def clone(self) -> "DeviceState":
+        return DeviceState(**{f: getattr(self, f).clone() for f in STATE_FIELDS})
+
+
+def make_phys(radQ=0, SWQ=0, FLQ=0, Wz=0.0, Bstar=0.0, Rstar=0.0, rho=0.0, vsw_AUyr=1.0,
+              Rmin=0.0) -> abi.Phys:
+    return abi.Phys(int(radQ), int(SWQ), int(FLQ), float(Wz), float(Bstar), float(Rstar),
+                    float(rho), float(vsw_AUyr), float(Rmin))
+
+
+def make_view(dist, fov, PA, inc, longitude, xsize, ysize) -> abi.View:
+    return abi.View(float(dist), float(fov), float(PA), float(inc), float(longitude),
+                    int(xsize), int(ysize))
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream)
+
+
+def _host(a, dtype):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+def probe_fma_peak(device: int = 0) -> tuple[float, float]:
+    """Measured FP32 and FP64 FMA throughput (TFLOP/s) of the device."""
+    lib = abi.load()
+    a, b = C.c_double(), C.c_double()
+    abi.check(lib.ddx_probe_fma_peak(device, C.byref(a), C.byref(b)), "ddx_probe_fma_peak")
+    return a.value, b.value
+
+
+class Engine:
+    """One libddx context on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = abi.load()
+        self.device = device
+        h = C.c_void_p()
+        abi.check(self.lib.ddx_create(C.byref(h), device), "ddx_create")
+        self.ctx = h
+        self.n_grid = 0
+        self.n_wav = 0
+
+    def close(self) -> None:
+        if self.ctx:
+            abi.check(self.lib.ddx_destroy(self.ctx), "ddx_destroy")
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- tables -------------------------------------------------------------------------
+    def set_size_table(self, size, beta, betasw, q) -> None:
+        s, ps = _host(size, np.float64)
+        b, pb = _host(beta, np.float32)
+        bs, pbs = _host(betasw, np.float32)
+        qq, pq = _host(q, np.float32)
+        abi.check(self.lib.ddx_set_size_table(self.ctx, len(s), ps, pb, pbs, pq), "ddx_set_size_table")
+        self.n_grid = len(s)
+
+    def set_optics(self, w, influx, Qabs, Qsca, Qpfunc, Td, Rmin, Rmax) -> None:
+        n_wav = len(w)
+        n_grid = Qabs.shape[0]
+        n_theta = Qpfunc.shape[1]
+        arrs = [_host(a, np.float64) for a in (w, influx, Qabs, Qsca, Qpfunc, Td)]
+        abi.check(self.lib.ddx_set_optics(self.ctx, n_grid, n_wav, n_theta,
+                                          *[p for _, p in arrs], float(Rmin), float(Rmax)),
+                  "ddx_set_optics")
+        self.n_wav = n_wav
+
+    # -- dynamics -----------------------------------------------------------------------
+    def step(self, st: DeviceState, n_grav: int, dt: float, phys: abi.Phys,
+             precision: int = abi.DDX_PREC_FP64, mode: int = abi.DDX_MODE_FIXED,
+             stream=None) -> None:
+        self.evolve(st, n_grav, dt, 1, phys, precision, mode, stream)
+
+    def evolve(self, st: DeviceState, n_grav: int, dt: float, n_steps: int, phys: abi.Phys,
+               precision: int = abi.DDX_PREC_FP64, mode: int = abi.DDX_MODE_FIXED,
+               stream=None) -> None:
+        n_dust = st.n_all - n_grav
+        abi.check(self.lib.ddx_evolve(self.ctx, C.byref(st._abi), n_grav, n_dust, float(dt),
+                                      int(n_steps), C.byref(phys), precision, mode,
+                                      C.c_void_p(_stream_handle(stream))), "ddx_evolve")
+
+    def stage(self, which: str, st: DeviceState, n_grav: int, dt: float, phys: abi.Phys,
+              precision: int = abi.DDX_PREC_FP64, mode: int = abi.DDX_MODE_FIXED, stream=None) -> None:
+        """One of the reference's three step calls: 'massive_rk4', 'small_rk4' or
+        'massive_final' (src/grid.cu:387-389)."""
+        fn = getattr(self.lib, "ddx_" + which)
+        abi.check(fn(self.ctx, C.byref(st._abi), n_grav, st.n_all - n_grav, float(dt), C.byref(phys),
+                     precision, mode, C.c_void_p(_stream_handle(stream))), "ddx_" + which)
+
+    # -- flux ---------------------------------------------------------------------------
+    def image(self, st: DeviceState, n_grav: int, view: abi.View, wj, out: torch.Tensor | None = None,
+              precision: int = abi.DDX_PREC_FP64, stream=None) -> torch.Tensor:
+        wj_a, pwj = _host(wj, np.int32)
+        n_img = len(wj_a)
+        npix = view.xsize * view.ysize
+        if out is None:
+            out = torch.empty((n_img, view.xsize, view.ysize), dtype=torch.float64, device=st.x.device)
+        assert out.is_contiguous() and out.numel() == n_img * npix and out.dtype == torch.float64
+        abi.check(self.lib.ddx_image(self.ctx, C.byref(st._abi), n_grav, st.n_all - n_grav,
+                                     C.byref(view), pwj, n_img, C.c_void_p(out.data_ptr()),
+                                     precision, C.c_void_p(_stream_handle(stream))), "ddx_image")
+        return out
+
+    def sed(self, st: DeviceState, n_grav: int, view: abi.View, out: torch.Tensor | None = None,
+            precision: int = abi.DDX_PREC_FP64, mode: int = abi.DDX_MODE_FIXED,
+            stream=None) -> torch.Tensor:
+        if out is None:
+            out = torch.empty(self.n_wav, dtype=torch.float64, device=st.x.device)
+        abi.check(self.lib.ddx_sed(self.ctx, C.byref(st._abi), n_grav, st.n_all - n_grav,
+                                   C.byref(view), C.c_void_p(out.data_ptr()), precision, mode,
+                                   C.c_void_p(_stream_handle(stream))), "ddx_sed")
+        return out
+
+    def pixels(self, st: DeviceState, n_grav: int, view: abi.View):
+        """Per-tracer pixel index ysize*x + y (-1 outside / no optics) and whether the
+        exact reference sequence decided it."""
+        n_dust = st.n_all - n_grav
+        pix = torch.empty(max(n_dust, 1), dtype=torch.int32, device=st.x.device)
+        ex = torch.empty(max(n_dust, 1), dtype=torch.int32, device=st.x.device)
+        abi.check(self.lib.ddx_debug_pixels(self.ctx, C.byref(st._abi), n_grav, n_dust,
+                                            C.byref(view), C.c_void_p(pix.data_ptr()),
+                                            C.c_void_p(ex.data_ptr())), "ddx_debug_pixels")
+        torch.cuda.synchronize()
+        return pix[:n_dust], ex[:n_dust]

@@ -1,0 +1,178 @@
+/*
+ * diskdyn_gb300.h -- C ABI of the GB300 (sm_103a) DiskDyn dynamical and imaging path.
+ *
+ * The library replaces the per-step kernel launches and the flux kernels that the
+ * reference's `class Grid` issues.  Every entry point takes plain device pointers and
+ * sizes, is stream-ordered on a caller-supplied CUDA stream (passed as `void*`; NULL is
+ * the legacy default stream, which is what the reference uses), and returns an int status
+ * (DDX_OK == 0) instead of calling exit().  A context is not re-entrant: calls that share
+ * one context must not overlap in host threads.
+ *
+ * State layout is the reference's: one SoA array per field, n_all = n_grav + n_dust
+ * entries, massive bodies first with the star at index 0, then the dust tracers
+ * (src/grid.cu:104-189 of the reference).  Units are AU, yr and mass*4*pi^2 in Msun,
+ * so an acceleration is m/r^2 (src/ddyn.cuh:17-38, src/read_in.cu:76).
+ */
+#ifndef DISKDYN_GB300_H
+#define DISKDYN_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DDX_ABI_VERSION 1
+
+/* Status codes.  The reference exits the process instead (src/error.cu:75-91,
+ * src/ddyn.cuh:400-408). */
+#define DDX_OK              0
+#define DDX_ERR_ARG         1   /* null pointer, negative count, unknown enum value */
+#define DDX_ERR_CUDA        2   /* a CUDA runtime call or kernel launch failed */
+#define DDX_ERR_NOMEM       3   /* device allocation failed */
+#define DDX_ERR_STATE       4   /* a table needed by the call was never set */
+#define DDX_ERR_RANGE       5   /* a size is beyond a documented limit */
+#define DDX_ERR_TIMEOUT     6   /* a bounded device-side wait gave up */
+#define DDX_ERR_NONFINITE   7   /* NaN/Inf found where a finite value is required */
+
+/* Arithmetic of the force stage. */
+#define DDX_PREC_FP64   0   /* every operation in FP64, like the reference */
+#define DDX_PREC_MIXED  1   /* FP64 state, Kepler term and stage combination; FP32
+                               body-body perturbations with compensated sums */
+
+/* Behaviour switch for the reference's known defects. */
+#define DDX_MODE_FIXED      0   /* defects corrected (default) */
+#define DDX_MODE_REFERENCE  1   /* defects reproduced where they are deterministic */
+
+/* Maximum number of size bins; the reference keeps them in __constant__ arrays of
+ * this length (src/ddyn.cuh:33 `nsize`, src/ddyn.cu:29-32). */
+#define DDX_MAX_SIZE_BINS 2700
+/* Radial grid of the dust-temperature table (src/ddyn.cuh:32 `nR`). */
+#define DDX_NR 100
+
+/* Device pointers to the particle state.  Replaces the state half of
+ * `struct coord` (src/ddyn.cuh:44-58); the 32 RK4 scratch arrays of that struct are
+ * not part of the interface, the context owns its own scratch. */
+typedef struct {
+    double *x, *y, *z;      /* AU */
+    double *vx, *vy, *vz;   /* AU/yr */
+    double *m;              /* mass * 4 pi^2, Msun */
+    double *N;              /* grains per tracer; 0 marks a removed tracer */
+    int    *id;             /* size-bin index, -1 = no optical data */
+} ddx_state;
+
+/* Physics switches and stellar constants, in the units the reference passes to
+ * RK4calc_dust (src/grid.cu:737, src/read_in.cu:591-603). */
+typedef struct {
+    int    radQ, SWQ, FLQ;  /* radiation pressure / stellar-wind drag / Lorentz force */
+    double Wz;              /* stellar rotation rate, 1/yr */
+    double Bstar;           /* surface field, Msun/yr^2/A */
+    double Rstar;           /* AU */
+    double rho;             /* bulk density, kg/m^3 (unused by the force; kept for parity) */
+    double vsw_AUyr;        /* stellar-wind speed, AU/yr */
+    double Rmin;            /* sublimation radius, AU */
+} ddx_phys;
+
+/* Observer geometry, in the units the reference passes to calc_flux_driver
+ * (src/grid.cu:51-52, src/read_in.cu:608-624). */
+typedef struct {
+    double dist;            /* distance, m */
+    double fov;             /* field of view, AU */
+    double PA, inc, longitude;  /* radians */
+    int    xsize, ysize;    /* pixels */
+} ddx_view;
+
+typedef struct ddx_ctx ddx_ctx;
+
+/* Create a context on `device` (cudaSetDevice is called on it).  Replaces the buffer
+ * ownership of Grid::allocgpu (src/init.cu:543-602); scratch grows on demand. */
+int ddx_create(ddx_ctx **out, int device);
+int ddx_destroy(ddx_ctx *ctx);
+
+/* Per-size-bin table: grain size [m], beta, beta_sw, charge q.  Host pointers, n_grid
+ * entries, n_grid <= DDX_MAX_SIZE_BINS.  Replaces the __constant__ fill of
+ * Grid::sync_dust_to_gpu (src/init.cu:649-660). */
+int ddx_set_size_table(ddx_ctx *ctx, int n_grid, const double *size, const float *beta,
+                       const float *betasw, const float *q);
+
+/* Optical tables, host pointers, copied to the device.  Layouts as in the reference
+ * (src/read_in.cu:450-498, src/grid.cu:793-825):
+ *   w[n_wav] (m), in[n_wav] (stellar flux at the observer), Qabs/Qsca[n_grid][n_wav],
+ *   Qpfunc[n_grid][n_theta][n_wav], Td[n_grid][DDX_NR] (K) on the log-R grid
+ *   [Rmin, Rmax] (AU).  Replaces the table half of Grid::sync_dust_to_gpu
+ *   (src/init.cu:642-647). */
+int ddx_set_optics(ddx_ctx *ctx, int n_grid, int n_wav, int n_theta, const double *w,
+                   const double *in, const double *Qabs, const double *Qsca,
+                   const double *Qpfunc, const double *Td, double Rmin, double Rmax);
+
+/* One fixed-dt RK4 step of the whole system: massive all-pairs gravity, then every
+ * dust tracer under stellar gravity reduced by beta, PR and stellar-wind drag, the
+ * optional Lorentz force and the gravity of every massive body, then the massive
+ * combination.  Equivalent to the reference's
+ *     massive_RK4(dt); small_RK4(dt); massive_final(dt);   (src/grid.cu:387-389)
+ * The size table must be set.  `precision` is DDX_PREC_*, `mode` is DDX_MODE_*. */
+int ddx_step(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
+             const ddx_phys *phys, int precision, int mode, void *stream);
+
+/* The same step split at the reference's three call sites, for a caller that keeps
+ * them apart (src/grid.cu:387-389):
+ *   ddx_massive_rk4   <- Grid::massive_RK4  : stage positions P1..P4 of the massive set
+ *                                             (accelerations A1, A2 evaluated);
+ *   ddx_small_rk4     <- Grid::small_RK4    : full RK4 of every dust tracer against them;
+ *   ddx_massive_final <- Grid::massive_final: A3, A4 and the RK4 combination of the
+ *                                             massive set.
+ * They must be called in this order, on one stream, with the same state, sizes, dt,
+ * physics, precision and mode; the stage positions live in the context in between. */
+int ddx_massive_rk4(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
+                    const ddx_phys *phys, int precision, int mode, void *stream);
+int ddx_small_rk4(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
+                  const ddx_phys *phys, int precision, int mode, void *stream);
+int ddx_massive_final(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
+                      const ddx_phys *phys, int precision, int mode, void *stream);
+
+/* n_steps calls of ddx_step with the same dt, with the launches of all steps enqueued
+ * back to back (no host synchronisation in between). */
+int ddx_evolve(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
+               int n_steps, const ddx_phys *phys, int precision, int mode, void *stream);
+
+/* Images at the table wavelengths wj[0..n_img-1]: scattered + thermal flux of every
+ * dust tracer with id >= 0, projected through `view` and summed into
+ * Fd[img][xsize*ysize] (device pointer), pixel (x, y) at Fd[img*npix + ysize*x + y]
+ * (x-major, like the reference).  Fd is overwritten.  Pixel indices are bit-identical
+ * to the reference's calc_flux_driver on the same GPU.  Replaces
+ *     null_flux(); calc_flux(wj);   per image wavelength (src/grid.cu:411-421). */
+int ddx_image(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
+              const ddx_view *view, const int *wj, int n_img, double *Fd, int precision,
+              void *stream);
+
+/* SED: total flux of all dust tracers at every table wavelength, Fsed[n_wav] (device
+ * pointer), overwritten.  Replaces the per-wavelength loop
+ *     null_flux_part(); calc_flux_sed(j); copy_sed(j);   (src/grid.cu:396-406)
+ * mode DDX_MODE_REFERENCE keeps the reference's rotation by the spherical radius
+ * (src/gpu_functions.cu:1106-1107); DDX_MODE_FIXED rotates by the cylindrical one. */
+int ddx_sed(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
+            const ddx_view *view, double *Fsed, int precision, int mode, void *stream);
+
+/* Diagnostics (no reference counterpart).  ddx_debug_pixels writes, for every dust
+ * tracer, the pixel index ysize*x + y that ddx_image uses (or -1 for a tracer without
+ * optical data or outside the image) to pix[n_dust], and 1/0 to exact[n_dust] when the
+ * reference's own expression sequence decided it (tracers within the guard band of a
+ * pixel edge).  Both device pointers.  ddx_debug_exact_pixel_count returns how many
+ * tracers took that exact path in ddx_image calls on this context. */
+int ddx_debug_pixels(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
+                     const ddx_view *view, int *pix, int *exact);
+unsigned long long ddx_debug_exact_pixel_count(ddx_ctx *ctx);
+
+/* Throughput probe (no reference counterpart): chains of independent FMAs on every SM of
+ * `device`, timed with CUDA events.  Writes the measured FP32 and FP64 FMA rates in
+ * TFLOP/s (2 flops per FMA); used as the compute-pipe roofline denominators. */
+int ddx_probe_fma_peak(int device, double *fp32_tflops, double *fp64_tflops);
+
+/* Error string for a status code. */
+const char *ddx_status_string(int status);
+
+/* ABI version of the loaded library (DDX_ABI_VERSION). */
+int ddx_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DISKDYN_GB300_H */

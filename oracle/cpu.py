@@ -1,0 +1,157 @@
+"""ORACLE -- test infrastructure.  ctypes binding of liboracle.so (ddx_oracle.c)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .build_oracle import LIB, build
+
+FIELDS = ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id")
+
+
+class OState(C.Structure):
+    _fields_ = [(f, C.c_void_p) for f in FIELDS]
+
+
+class OPhys(C.Structure):
+    _fields_ = [("radQ", C.c_int), ("SWQ", C.c_int), ("FLQ", C.c_int), ("Wz", C.c_double),
+                ("Bstar", C.c_double), ("Rstar", C.c_double), ("rho", C.c_double),
+                ("vsw_AUyr", C.c_double), ("Rmin", C.c_double)]
+
+
+class OView(C.Structure):
+    _fields_ = [("dist", C.c_double), ("fov", C.c_double), ("PA", C.c_double),
+                ("inc", C.c_double), ("longitude", C.c_double), ("xsize", C.c_int),
+                ("ysize", C.c_int)]
+
+
+class OOptics(C.Structure):
+    _fields_ = [("w", C.c_void_p), ("in_", C.c_void_p), ("Qabs", C.c_void_p), ("Qsca", C.c_void_p),
+                ("Qpfunc", C.c_void_p), ("Td", C.c_void_p), ("size", C.c_void_p),
+                ("Rmin", C.c_double), ("Rmax", C.c_double), ("n_grid", C.c_int),
+                ("n_wav", C.c_int), ("n_theta", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build()))
+        _lib.ora_step.argtypes = [OState, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.POINTER(OPhys), C.c_int, C.c_void_p]
+        _lib.ora_dust.argtypes = [OState, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(OPhys), C.c_int]
+        _lib.ora_image.argtypes = [OState, C.c_int, C.c_int, C.POINTER(OOptics), C.POINTER(OView),
+                                   C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.ora_sed.argtypes = [OState, C.c_int, C.c_int, C.POINTER(OOptics), C.POINTER(OView),
+                                 C.c_void_p, C.c_int]
+        _lib.ora_dust_temp.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]
+        for f in ("ora_step", "ora_dust", "ora_image", "ora_sed", "ora_dust_temp"):
+            getattr(_lib, f).restype = C.c_int
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def host_state(arrays: dict) -> tuple[dict, OState]:
+    """Contiguous copies of a state dict and the struct pointing at them."""
+    st = {f: np.array(arrays[f], dtype=np.int32 if f == "id" else np.float64, copy=True) for f in FIELDS}
+    return st, OState(*[_ptr(st[f]) for f in FIELDS])
+
+
+def phys(d: dict) -> OPhys:
+    return OPhys(int(d["radQ"]), int(d["SWQ"]), int(d["FLQ"]), float(d["Wz"]), float(d["Bstar"]),
+                 float(d["Rstar"]), float(d["rho"]), float(d["vsw_AUyr"]), float(d["Rmin"]))
+
+
+def view(d: dict) -> OView:
+    return OView(float(d["dist"]), float(d["fov"]), float(d["PA"]), float(d["inc"]),
+                 float(d["longitude"]), int(d["xsize"]), int(d["ysize"]))
+
+
+def step(arrays: dict, n_grav: int, dt: float, size_table: dict, phys_d: dict, n_steps: int = 1,
+         ref_mode: bool = False, return_kpos: bool = False):
+    """n_steps reference steps on a copy of `arrays`; returns the new state dict
+    (and the massive stage positions of the last step, shape (4, 3, n_grav))."""
+    st, os_ = host_state(arrays)
+    n_dust = len(st["x"]) - n_grav
+    b = np.ascontiguousarray(size_table["beta"], np.float32)
+    bs = np.ascontiguousarray(size_table["betasw"], np.float32)
+    q = np.ascontiguousarray(size_table["q"], np.float32)
+    kpos = np.zeros((4, 3, n_grav))
+    ph = phys(phys_d)
+    for _ in range(n_steps):
+        r = lib().ora_step(os_, n_grav, n_dust, float(dt), _ptr(b), _ptr(bs), _ptr(q), C.byref(ph),
+                           int(ref_mode), _ptr(kpos))
+        if r:
+            raise RuntimeError("ora_step failed")
+    return (st, kpos) if return_kpos else st
+
+
+def dust(arrays: dict, n_grav: int, dt: float, kpos, size_table: dict, phys_d: dict,
+         i0: int = 0, i1: int | None = None, ref_mode: bool = False) -> dict:
+    """Dust half of a step with given massive stage positions (4, 3, n_grav)."""
+    st, os_ = host_state(arrays)
+    n_dust = len(st["x"]) - n_grav
+    i1 = n_dust if i1 is None else i1
+    kp = np.ascontiguousarray(kpos, np.float64)
+    b = np.ascontiguousarray(size_table["beta"], np.float32)
+    bs = np.ascontiguousarray(size_table["betasw"], np.float32)
+    q = np.ascontiguousarray(size_table["q"], np.float32)
+    ph = phys(phys_d)
+    if lib().ora_dust(os_, n_grav, n_dust, i0, i1, float(dt), _ptr(kp), _ptr(b), _ptr(bs), _ptr(q),
+                      C.byref(ph), int(ref_mode)):
+        raise RuntimeError("ora_dust failed")
+    return st
+
+
+def _optics(o: dict, size):
+    keep = {k: np.ascontiguousarray(o[k], np.float64) for k in ("w", "in", "Qabs", "Qsca", "Qpfunc", "Td")}
+    keep["size"] = np.ascontiguousarray(size, np.float64)
+    oo = OOptics(_ptr(keep["w"]), _ptr(keep["in"]), _ptr(keep["Qabs"]), _ptr(keep["Qsca"]),
+                 _ptr(keep["Qpfunc"]), _ptr(keep["Td"]), _ptr(keep["size"]), float(o["Rmin"]),
+                 float(o["Rmax"]), keep["Qabs"].shape[0], len(keep["w"]), keep["Qpfunc"].shape[1])
+    return keep, oo
+
+
+def image(arrays: dict, n_grav: int, optics: dict, size, view_d: dict, wj):
+    """Images (n_img, xsize, ysize) and per-tracer pixel index (-1 = none)."""
+    st, os_ = host_state(arrays)
+    n_dust = len(st["x"]) - n_grav
+    keep, oo = _optics(optics, size)
+    v = view(view_d)
+    wj_a = np.ascontiguousarray(wj, np.int32)
+    Fd = np.zeros((len(wj_a), v.xsize, v.ysize))
+    pix = np.zeros(max(n_dust, 1), np.int32)
+    lib().ora_image(os_, n_grav, n_dust, C.byref(oo), C.byref(v), _ptr(wj_a), len(wj_a), _ptr(Fd), _ptr(pix))
+    return Fd, pix[:n_dust]
+
+
+def sed(arrays: dict, n_grav: int, optics: dict, size, view_d: dict, ref_mode: bool = False):
+    st, os_ = host_state(arrays)
+    n_dust = len(st["x"]) - n_grav
+    keep, oo = _optics(optics, size)
+    v = view(view_d)
+    out = np.zeros(oo.n_wav)
+    lib().ora_sed(os_, n_grav, n_dust, C.byref(oo), C.byref(v), _ptr(out), int(ref_mode))
+    return out
+
+
+def dust_temp(w, influx, Qabs, dist, Rmax_AU):
+    """calculate_dust_temp (src/grid.cu:754-834): returns Td (n_grid, 100), Rmin, Rmax [AU]."""
+    w = np.ascontiguousarray(w, np.float64)
+    influx = np.ascontiguousarray(influx, np.float64)
+    Qabs = np.ascontiguousarray(Qabs, np.float64)
+    n_grid, n_wav = Qabs.shape
+    Td = np.zeros((n_grid, 100))
+    rmin = C.c_double(0.0)
+    rmax = C.c_double(float(Rmax_AU))
+    lib().ora_dust_temp(n_grid, n_wav, _ptr(w), _ptr(influx), _ptr(Qabs), float(dist), C.byref(rmin),
+                        C.byref(rmax), _ptr(Td))
+    return Td, rmin.value, rmax.value

@@ -1,0 +1,456 @@
+/*
+ * ORACLE -- test infrastructure, not product code.
+ *
+ * A plain-C FP64 restatement of the reference DiskDyn hot path, written to check the
+ * CUDA kernels of diskdyn_gb300 and to serve as the timed CPU baseline.  Nothing in the
+ * product links or calls this file; only the tests, the smoke check and the CPU-baseline
+ * leg of bench.py do.
+ *
+ * Each function states the reference lines it follows (paths within the DiskDyn project).
+ * Arithmetic is kept in the reference's order, expression by expression; the only
+ * intended differences are the summation order of the massive-set accelerations (the
+ * reference adds them with CAS atomics in a hardware-dependent order) and libm instead of
+ * the CUDA math library.  Build with -ffp-contract=off so x86 and Arm hosts agree.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORA_AU      1.49598e11
+#define ORA_LIGHTAU 63239.6717367
+#define ORA_CSPEED  299792458.0
+#define ORA_KBOLTZ  1.3806503E-23
+#define ORA_HPLANK  6.626068E-34
+#define ORA_PI      3.14159265358979323846
+#define ORA_NR      100
+#define ORA_TSUB    2000.0
+
+typedef struct {
+    double *x, *y, *z, *vx, *vy, *vz, *m, *N;
+    int *id;
+} ora_state;
+
+typedef struct {
+    int radQ, SWQ, FLQ;
+    double Wz, Bstar, Rstar, rho, vsw_AUyr, Rmin;
+} ora_phys;
+
+typedef struct {
+    double dist, fov, PA, inc, longitude;
+    int xsize, ysize;
+} ora_view;
+
+/* ------------------------------------------------------------------------------------
+ * Massive set: src/grid.cu:693-752 with src/gpu_functions.cu:71-625.
+ * Stage accelerations: a_i = sum_{j != i} m_j (x_j - x_i) / (RR sqrt(RR)), pairs with
+ * RR == 0 contribute nothing (src/gpu_functions.cu:156-178).  The reference forms
+ * kv = dX / f then multiplies by m_j (:164, :190); the same two roundings are used here.
+ * ------------------------------------------------------------------------------------ */
+static void massive_accel(int ng, const double *kx, const double *ky, const double *kz,
+                          const double *m, double *ax, double *ay, double *az) {
+    int i;
+#pragma omp parallel for schedule(static) if (ng > 256)
+    for (i = 0; i < ng; ++i) {
+        double KX = 0.0, KY = 0.0, KZ = 0.0;
+        for (int j = 0; j < ng; ++j) {
+            if (j == i) continue;
+            double dX = kx[j] - kx[i];
+            double dY = ky[j] - ky[i];
+            double dZ = kz[j] - kz[i];
+            double RR = dX * dX + dY * dY + dZ * dZ;
+            double f = RR * sqrt(RR);
+            if (f != 0) {
+                KX += (dX / f) * m[j];
+                KY += (dY / f) * m[j];
+                KZ += (dZ / f) * m[j];
+            }
+        }
+        ax[i] = KX; ay[i] = KY; az[i] = KZ;
+    }
+}
+
+/* Stage positions of the massive set, 4 x 3 x ng doubles written to kpos as
+ * [stage][xyz][i], and the final update of x, v.  With ng <= 1 the reference skips the
+ * massive stages entirely (src/grid.cu:698, 747): the stage arrays keep their set-up
+ * zeros and the star does not move; ref_single = 1 reproduces that. */
+static void massive_rk4(int ng, ora_state s, double dt, double *kpos, int ref_single) {
+    size_t n = (size_t)ng;
+    if (ng <= 1) {
+        if (ref_single) {
+            memset(kpos, 0, sizeof(double) * 12 * n);
+        } else {
+            for (int st = 0; st < 4; ++st) {
+                double c = st == 0 ? 0.0 : (st == 3 ? dt : dt * 0.5);
+                kpos[(st * 3 + 0) * n] = s.x[0] + s.vx[0] * c;
+                kpos[(st * 3 + 1) * n] = s.y[0] + s.vy[0] * c;
+                kpos[(st * 3 + 2) * n] = s.z[0] + s.vz[0] * c;
+            }
+        }
+        return;
+    }
+    double *k1x = kpos + 0 * n, *k1y = kpos + 1 * n, *k1z = kpos + 2 * n;
+    double *k2x = kpos + 3 * n, *k2y = kpos + 4 * n, *k2z = kpos + 5 * n;
+    double *k3x = kpos + 6 * n, *k3y = kpos + 7 * n, *k3z = kpos + 8 * n;
+    double *k4x = kpos + 9 * n, *k4y = kpos + 10 * n, *k4z = kpos + 11 * n;
+    double *buf = (double *)malloc(sizeof(double) * 21 * n);
+    double *k1vx = buf, *k1vy = buf + n, *k1vz = buf + 2 * n;
+    double *k2vx = buf + 3 * n, *k2vy = buf + 4 * n, *k2vz = buf + 5 * n;
+    double *k3vx = buf + 6 * n, *k3vy = buf + 7 * n, *k3vz = buf + 8 * n;
+    double *k4vx = buf + 9 * n, *k4vy = buf + 10 * n, *k4vz = buf + 11 * n;
+    double *k2rx = buf + 12 * n, *k2ry = buf + 13 * n, *k2rz = buf + 14 * n;
+    double *k3rx = buf + 15 * n, *k3ry = buf + 16 * n, *k3rz = buf + 17 * n;
+    double *k4rx = buf + 18 * n, *k4ry = buf + 19 * n, *k4rz = buf + 20 * n;
+    double h = dt * 0.5;       /* src/grid.cu:711,716 */
+    for (int i = 0; i < ng; ++i) { k1x[i] = s.x[i]; k1y[i] = s.y[i]; k1z[i] = s.z[i]; }
+    massive_accel(ng, k1x, k1y, k1z, s.m, k1vx, k1vy, k1vz);
+    for (int i = 0; i < ng; ++i) {             /* RK4calc_massive3 */
+        k2x[i] = s.x[i] + s.vx[i] * h; k2y[i] = s.y[i] + s.vy[i] * h; k2z[i] = s.z[i] + s.vz[i] * h;
+        k2rx[i] = s.vx[i] + k1vx[i] * h; k2ry[i] = s.vy[i] + k1vy[i] * h; k2rz[i] = s.vz[i] + k1vz[i] * h;
+    }
+    massive_accel(ng, k2x, k2y, k2z, s.m, k2vx, k2vy, k2vz);
+    for (int i = 0; i < ng; ++i) {             /* RK4calc_massive5 */
+        k3x[i] = s.x[i] + k2rx[i] * h; k3y[i] = s.y[i] + k2ry[i] * h; k3z[i] = s.z[i] + k2rz[i] * h;
+        k3rx[i] = s.vx[i] + k2vx[i] * h; k3ry[i] = s.vy[i] + k2vy[i] * h; k3rz[i] = s.vz[i] + k2vz[i] * h;
+    }
+    massive_accel(ng, k3x, k3y, k3z, s.m, k3vx, k3vy, k3vz);
+    for (int i = 0; i < ng; ++i) {             /* RK4calc_massive7 */
+        k4x[i] = s.x[i] + k3rx[i] * dt; k4y[i] = s.y[i] + k3ry[i] * dt; k4z[i] = s.z[i] + k3rz[i] * dt;
+        k4rx[i] = s.vx[i] + k3vx[i] * dt; k4ry[i] = s.vy[i] + k3vy[i] * dt; k4rz[i] = s.vz[i] + k3vz[i] * dt;
+    }
+    massive_accel(ng, k4x, k4y, k4z, s.m, k4vx, k4vy, k4vz);
+    /* The massive final update happens after the dust step in the reference
+     * (src/grid.cu:387-389); it only reads these arrays, so doing it here, after the stage
+     * positions are saved, gives the same result. */
+    double d6 = dt / 6.0;      /* src/grid.cu:750 */
+    for (int i = 0; i < ng; ++i) {             /* RK4calc_massive_final */
+        s.x[i] += d6 * (s.vx[i] + 2.0 * k2rx[i] + 2.0 * k3rx[i] + k4rx[i]);
+        s.y[i] += d6 * (s.vy[i] + 2.0 * k2ry[i] + 2.0 * k3ry[i] + k4ry[i]);
+        s.z[i] += d6 * (s.vz[i] + 2.0 * k2rz[i] + 2.0 * k3rz[i] + k4rz[i]);
+        s.vx[i] += d6 * (k1vx[i] + 2.0 * k2vx[i] + 2.0 * k3vx[i] + k4vx[i]);
+        s.vy[i] += d6 * (k1vy[i] + 2.0 * k2vy[i] + 2.0 * k3vy[i] + k4vy[i]);
+        s.vz[i] += d6 * (k1vz[i] + 2.0 * k2vz[i] + 2.0 * k3vz[i] + k4vz[i]);
+    }
+    free(buf);
+}
+
+/* ------------------------------------------------------------------------------------
+ * Dust: src/gpu_functions.cu:627-943, one tracer, in order.
+ * Returns 0 = updated, 1 = removed (N set to 0 at the index the reference uses).
+ * ------------------------------------------------------------------------------------ */
+static int star_stage(double dx, double dy, double dz, double rx, double ry, double rz,
+                      double m0, float bet, float betsw, float qe, double m,
+                      const ora_phys *p, double *kx, double *ky, double *kz) {
+    double RR = dx * dx + dy * dy + dz * dz;
+    double RR3 = RR * sqrt(RR);
+    if (RR <= p->Rmin * p->Rmin) return 0;
+    double Fg = (1.0 - bet - betsw) * m0 / RR3;
+    double Fbase1;
+    if (p->SWQ == 1) Fbase1 = m0 / RR * (bet / ORA_LIGHTAU + betsw / p->vsw_AUyr);
+    else             Fbase1 = bet * m0 / ORA_LIGHTAU / RR;
+    double Fbase2 = (dx * rx + dy * ry + dz * rz) / RR;
+    double Fdrx = Fbase1 * (Fbase2 * dx + rx);
+    double Fdry = Fbase1 * (Fbase2 * dy + ry);
+    double Fdrz = Fbase1 * (Fbase2 * dz + rz);
+    double Flx, Fly;
+    if (p->FLQ == 1) {
+        double Bz = p->Bstar * p->Rstar * p->Rstar * p->Rstar / RR3;
+        Flx = qe * (ry - p->Wz * dx) * Bz / m;
+        Fly = -qe * (rx + p->Wz * dy) * Bz / m;
+    } else {
+        Flx = 0; Fly = 0;
+    }
+    *kx = -Fg * dx - Fdrx + Flx;
+    *ky = -Fg * dy - Fdry + Fly;
+    *kz = -Fg * dz - Fdrz;
+    return 1;
+}
+
+static int bodies_stage(int ng, const double *kx_, const double *ky_, const double *kz_,
+                        const double *mm, double xt, double yt, double zt,
+                        double *kx, double *ky, double *kz) {
+    for (int j = 1; j < ng; ++j) {
+        double dx = xt - kx_[j];
+        double dy = yt - ky_[j];
+        double dz = zt - kz_[j];
+        double RR = dx * dx + dy * dy + dz * dz;
+        if (RR == 0) return 0;
+        double f = mm[j] / RR / sqrt(RR);
+        *kx += -f * dx;
+        *ky += -f * dy;
+        *kz += -f * dz;
+    }
+    return 1;
+}
+
+static void dust_one(int ng, int i, ora_state s, const double *kpos, size_t n, double dt,
+                     const float *beta, const float *betasw, const float *q,
+                     const ora_phys *p, int ref_mode) {
+    const double *k1x = kpos + 0 * n, *k1y = kpos + 1 * n, *k1z = kpos + 2 * n;
+    const double *k2x = kpos + 3 * n, *k2y = kpos + 4 * n, *k2z = kpos + 5 * n;
+    const double *k3x = kpos + 6 * n, *k3y = kpos + 7 * n, *k3z = kpos + 8 * n;
+    const double *k4x = kpos + 9 * n, *k4y = kpos + 10 * n, *k4z = kpos + 11 * n;
+    int t = ng + i;
+    if (s.N[t] == 0) return;
+    int id = s.id[t];
+    double dt2 = dt / 2.0, dt6 = dt / 6.0;
+    double x = s.x[t], y = s.y[t], z = s.z[t], vx = s.vx[t], vy = s.vy[t], vz = s.vz[t];
+    float bet = 0.f, betsw = 0.f, qe = 0.f;
+    /* The reference reads q[id] even for id < 0 (src/gpu_functions.cu:665), an
+     * out-of-bounds read used only with the Lorentz force; 0 is used instead. */
+    if (id >= 0) { bet = beta[id]; betsw = betasw[id]; qe = q[id]; }
+    double m = s.m[t], m0 = s.m[0];
+    double k1vx, k1vy, k1vz, k2vx, k2vy, k2vz, k3vx, k3vy, k3vz, k4vx, k4vy, k4vz;
+    double k2rx, k2ry, k2rz, k3rx, k3ry, k3rz, k4rx, k4ry, k4rz, xt, yt, zt;
+
+    /* K1 */
+    if (!star_stage(x - k1x[0], y - k1y[0], z - k1z[0], vx, vy, vz, m0, bet, betsw, qe, m, p,
+                    &k1vx, &k1vy, &k1vz)) { s.N[t] = 0; return; }
+    if (!bodies_stage(ng, k1x, k1y, k1z, s.m, x, y, z, &k1vx, &k1vy, &k1vz)) { s.N[t] = 0; return; }
+    /* K2 */
+    k2rx = vx + k1vx * dt2; k2ry = vy + k1vy * dt2; k2rz = vz + k1vz * dt2;
+    xt = x + vx * dt2; yt = y + vy * dt2; zt = z + vz * dt2;
+    if (!star_stage(xt - k2x[0], yt - k2y[0], zt - k2z[0], k2rx, k2ry, k2rz, m0, bet, betsw, qe, m,
+                    p, &k2vx, &k2vy, &k2vz)) { s.N[t] = 0; return; }
+    if (!bodies_stage(ng, k2x, k2y, k2z, s.m, xt, yt, zt, &k2vx, &k2vy, &k2vz)) { s.N[t] = 0; return; }
+    /* K3 */
+    k3rx = vx + k2vx * dt2; k3ry = vy + k2vy * dt2; k3rz = vz + k2vz * dt2;
+    xt = x + k2rx * dt2; yt = y + k2ry * dt2; zt = z + k2rz * dt2;
+    if (!star_stage(xt - k3x[0], yt - k3y[0], zt - k3z[0], k3rx, k3ry, k3rz, m0, bet, betsw, qe, m,
+                    p, &k3vx, &k3vy, &k3vz)) { s.N[t] = 0; return; }
+    if (!bodies_stage(ng, k3x, k3y, k3z, s.m, xt, yt, zt, &k3vx, &k3vy, &k3vz)) { s.N[t] = 0; return; }
+    /* K4 */
+    k4rx = vx + k3vx * dt; k4ry = vy + k3vy * dt; k4rz = vz + k3vz * dt;
+    xt = x + k3rx * dt; yt = y + k3ry * dt; zt = z + k3rz * dt;
+    if (!star_stage(xt - k4x[0], yt - k4y[0], zt - k4z[0], k4rx, k4ry, k4rz, m0, bet, betsw, qe, m,
+                    p, &k4vx, &k4vy, &k4vz)) {
+        /* src/gpu_functions.cu:878 zeroes N[i] -- the dust-relative index used as an
+         * absolute one -- and leaves this grain's state as it was. */
+        if (ref_mode) s.N[i] = 0; else s.N[t] = 0;
+        return;
+    }
+    if (!bodies_stage(ng, k4x, k4y, k4z, s.m, xt, yt, zt, &k4vx, &k4vy, &k4vz)) { s.N[t] = 0; return; }
+    /* Evolve (src/gpu_functions.cu:927-941) */
+    x += dt6 * (vx + 2.0 * (k2rx + k3rx) + k4rx);
+    y += dt6 * (vy + 2.0 * (k2ry + k3ry) + k4ry);
+    z += dt6 * (vz + 2.0 * (k2rz + k3rz) + k4rz);
+    vx += dt6 * (k1vx + 2.0 * (k2vx + k3vx) + k4vx);
+    vy += dt6 * (k1vy + 2.0 * (k2vy + k3vy) + k4vy);
+    vz += dt6 * (k1vz + 2.0 * (k2vz + k3vz) + k4vz);
+    s.x[t] = x; s.y[t] = y; s.z[t] = z;
+    s.vx[t] = vx; s.vy[t] = vy; s.vz[t] = vz;
+}
+
+/* One step: massive_RK4(dt); small_RK4(dt); massive_final(dt) (src/grid.cu:387-389).
+ * kpos_out (optional, 12*n_grav doubles) receives the massive stage positions.
+ * nthreads <= 0 leaves the OpenMP default. */
+int ora_step(ora_state s, int n_grav, int n_dust, double dt, const float *beta,
+             const float *betasw, const float *q, const ora_phys *p, int ref_mode,
+             double *kpos_out) {
+    if (n_grav < 1 || n_dust < 0) return 1;
+    size_t n = (size_t)n_grav;
+    double *kpos = kpos_out ? kpos_out : (double *)malloc(sizeof(double) * 12 * n);
+    massive_rk4(n_grav, s, dt, kpos, ref_mode);
+    int i;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (i = 0; i < n_dust; ++i) dust_one(n_grav, i, s, kpos, n, dt, beta, betasw, q, p, ref_mode);
+    if (!kpos_out) free(kpos);
+    return 0;
+}
+
+/* The dust half only, with the massive stage positions given (12*n_grav doubles laid out
+ * [stage][xyz][body]); used to time or check the dust kernel in isolation. */
+int ora_dust(ora_state s, int n_grav, int n_dust, int i0, int i1, double dt, const double *kpos,
+             const float *beta, const float *betasw, const float *q, const ora_phys *p,
+             int ref_mode) {
+    if (n_grav < 1 || i0 < 0 || i1 > n_dust) return 1;
+    int i;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (i = i0; i < i1; ++i) dust_one(n_grav, i, s, kpos, (size_t)n_grav, dt, beta, betasw, q, p, ref_mode);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Image and SED: src/gpu_functions.cu:983-1156.
+ * ------------------------------------------------------------------------------------ */
+typedef struct {
+    const double *w, *in, *Qabs, *Qsca, *Qpfunc, *Td, *size;
+    double Rmin, Rmax;
+    int n_grid, n_wav, n_theta;
+} ora_optics;
+
+static double temp_of(double R, int id, const ora_optics *o) {
+    double f = log(o->Rmax / o->Rmin) / ((double)ORA_NR - 1.0);
+    const double *Td = o->Td;
+    if (R <= o->Rmin) return Td[id * ORA_NR];
+    if (R >= o->Rmax) return Td[id * ORA_NR + ORA_NR - 1];
+    int Rid = (int)(log(R / o->Rmin) / f) + 1;
+    double Rin = o->Rmin * exp((Rid - 1) * f);
+    double Rout = o->Rmin * exp(Rid * f);
+    return exp(log(Td[id * ORA_NR + Rid - 1]) +
+               log(Td[id * ORA_NR + Rid] / Td[id * ORA_NR + Rid - 1]) * log(R / Rin) / log(Rout / Rin));
+}
+
+static double flux_of(double n, int id, int wj, double R, double T, double cossc,
+                      const ora_optics *o, double dist) {
+    int nwav = o->n_wav, ntheta = o->n_theta;
+    double wvl = o->w[wj];
+    double I = (2 * ORA_HPLANK * ORA_CSPEED * ORA_CSPEED) /
+               (pow(wvl, 5) * (exp(ORA_HPLANK * ORA_CSPEED / (wvl * ORA_KBOLTZ * T)) - 1.0)) * ORA_PI;
+    int cosinm = (int)floor(0.5 * (cossc + 1.0) * (ntheta - 1));
+    int cosinp = cosinm + 1;
+    double cosm = (double)(cosinm)*2.0 / (ntheta - 1) - 1.0;
+    double cosp = (double)(cosinp)*2.0 / (ntheta - 1) - 1.0;
+    const double *Q = o->Qpfunc;
+    double P = exp(log(Q[nwav * (ntheta * id + cosinm) + wj]) +
+                   (log(Q[nwav * (ntheta * id + cosinp) + wj]) - log(Q[nwav * (ntheta * id + cosinm) + wj])) *
+                       (cossc - cosm) / (cosp - cosm));
+    double s = o->size[id];
+    double Fscat = o->in[wj] * ORA_PI * s * s * o->Qsca[nwav * id + wj] * P / R / R / ORA_AU / ORA_AU;
+    double Fther = I * s * s * o->Qabs[nwav * id + wj] / dist / dist;
+    return n * (Fther + Fscat) * 1e26 * wvl * wvl / ORA_CSPEED;
+}
+
+/* Pixel of one tracer (src/gpu_functions.cu:1001-1047); returns 0 when outside the image.
+ * Also returns R and the scattering-angle cosine. */
+static int pixel_of(double x, double y, double z, const ora_view *v, int ntheta, int *xim,
+                    int *yim, double *Rout, double *cossc_out, int sed_ref_radius) {
+    double rot = v->longitude, incl = v->inc, PA = v->PA, dist = v->dist;
+    double phi = atan2(y, x);
+    double R = sqrt(x * x + y * y + z * z);
+    double Rd = sqrt(x * x + y * y);
+    double rr = sed_ref_radius ? R : Rd;
+    x = rr * cos(phi + rot);
+    y = rr * sin(phi + rot);
+    double ly = -dist * sin(incl) - y;
+    double lz = dist * cos(incl) - z;
+    double cossc = (x * x + (-y) * ly + (-z) * lz) / R / sqrt(x * x + ly * ly + lz * lz);
+    if (cossc < -1) cossc = -1.0;
+    if (cossc >= 1.0 - 2.0 / ntheta) cossc = 1.0 - 2.0 / ntheta;
+    *Rout = R;
+    *cossc_out = cossc;
+    if (!xim) return 1;
+    y = sqrt(y * y + z * z) * cos(atan2(z, y) - incl);
+    phi = atan2(y, x);
+    Rd = sqrt(x * x + y * y);
+    x = Rd * cos(phi + PA);
+    y = Rd * sin(phi + PA);
+    double psca;
+    if (v->xsize >= v->ysize) psca = v->fov / v->xsize;
+    else                      psca = v->fov / v->ysize;
+    x = x + 0.5 * psca * v->xsize;
+    y = y + 0.5 * psca * v->ysize;
+    *xim = (int)floor(x / psca);
+    *yim = (int)floor(y / psca);
+    if (*xim < 0 || *xim > v->xsize - 1 || *yim < 0 || *yim > v->ysize - 1) return 0;
+    return 1;
+}
+
+/* Images at wj[0..n_img-1]; Fd[img][xsize*ysize] x-major, overwritten.  pix_out
+ * (optional, n_dust ints) receives ysize*xim + yim of each tracer, or -1. */
+int ora_image(ora_state s, int n_grav, int n_dust, const ora_optics *o, const ora_view *v,
+              const int *wj, int n_img, double *Fd, int *pix_out) {
+    size_t npix = (size_t)v->xsize * v->ysize;
+    memset(Fd, 0, sizeof(double) * npix * n_img);
+    for (int i = 0; i < n_dust; ++i) {
+        int t = n_grav + i;
+        if (pix_out) pix_out[i] = -1;
+        int id = s.id[t];
+        if (id < 0) continue;
+        int xim, yim;
+        double R, cossc;
+        if (!pixel_of(s.x[t], s.y[t], s.z[t], v, o->n_theta, &xim, &yim, &R, &cossc, 0)) continue;
+        if (pix_out) pix_out[i] = v->ysize * xim + yim;
+        if (!(R > o->Rmin)) continue;
+        double T = temp_of(R, id, o);
+        for (int k = 0; k < n_img; ++k)
+            Fd[k * npix + (size_t)v->ysize * xim + yim] += flux_of(s.N[t], id, wj[k], R, T, cossc, o, v->dist);
+    }
+    return 0;
+}
+
+/* SED at every table wavelength: Fsed[j] = sum over tracers (src/gpu_functions.cu:1083-1156
+ * and :961-981).  ref_mode = 1 rotates by the spherical radius like the reference. */
+int ora_sed(ora_state s, int n_grav, int n_dust, const ora_optics *o, const ora_view *v,
+            double *Fsed, int ref_mode) {
+    int nw = o->n_wav;
+    for (int j = 0; j < nw; ++j) Fsed[j] = 0.0;
+    int j;
+#pragma omp parallel for schedule(static)
+    for (j = 0; j < nw; ++j) {
+        double acc = 0.0;
+        for (int i = 0; i < n_dust; ++i) {
+            int t = n_grav + i;
+            int id = s.id[t];
+            if (id < 0) continue;
+            double R, cossc;
+            pixel_of(s.x[t], s.y[t], s.z[t], v, o->n_theta, NULL, NULL, &R, &cossc, ref_mode);
+            if (!(R > o->Rmin)) continue;
+            double T = temp_of(R, id, o);
+            acc += flux_of(s.N[t], id, j, R, T, cossc, o, v->dist);
+        }
+        Fsed[j] = acc;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Dust-temperature table: Grid::calculate_dust_temp, src/grid.cu:754-834, and the Planck
+ * function intens, src/functions.cu:390-397.  Rmax_AU is the largest configured radius
+ * (before the reference's factor 2); on return Td[n_grid][100] holds T on the log grid
+ * and *Rmin_AU, *Rmax_AU the grid limits in AU.  dist in m.
+ * ------------------------------------------------------------------------------------ */
+static double intens(double temp, double wvl) {
+    return (2 * ORA_HPLANK * ORA_CSPEED * ORA_CSPEED) /
+           (pow(wvl, 5) * (exp(ORA_HPLANK * ORA_CSPEED / (wvl * ORA_KBOLTZ * temp)) - 1));
+}
+
+int ora_dust_temp(int n_grid, int n_wav, const double *w, const double *in, const double *Qabs,
+                  double dist, double *Rmin_AU, double *Rmax_AU, double *Td) {
+    double Rmax = *Rmax_AU * 2 * ORA_AU;
+    double Rmin = Rmax;
+    for (int k = 0; k < n_grid; ++k) {
+        double star = 0.0, gflux = 0.0;
+        for (int i = 1; i < n_wav; i++)
+            star += 0.5 * (w[i] - w[i - 1]) * (Qabs[k * n_wav + i - 1] * in[i - 1] + Qabs[k * n_wav + i] * in[i]) / ORA_PI;
+        star *= pow(dist, 2.0);
+        for (int i = 1; i < n_wav; i++)
+            gflux += 0.5 * (w[i] - w[i - 1]) * (Qabs[k * n_wav + i - 1] * intens(ORA_TSUB, w[i - 1]) + Qabs[k * n_wav + i] * intens(ORA_TSUB, w[i]));
+        double Rtmp = 0.5 * sqrt(star / gflux);
+        if (Rtmp < Rmin) Rmin = Rtmp;
+    }
+    int nT = (int)floor((2 * ORA_TSUB - 3) * 0.5) + 1;
+    int k;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (k = 0; k < n_grid; ++k) {
+        double *Ra = (double *)malloc(sizeof(double) * nT), *Ta = (double *)malloc(sizeof(double) * nT);
+        double star = 0.0;
+        for (int i = 1; i < n_wav; i++)
+            star += 0.5 * (w[i] - w[i - 1]) * (Qabs[k * n_wav + i - 1] * in[i - 1] + Qabs[k * n_wav + i] * in[i]) / ORA_PI;
+        star *= pow(dist, 2.0);
+        int j = 0;
+        for (double T = 2 * ORA_TSUB; T >= 3.0; T -= 2.0) {
+            double gflux = 0.0;
+            for (int i = 1; i < n_wav; i++)
+                gflux += 0.5 * (w[i] - w[i - 1]) * (Qabs[k * n_wav + i - 1] * intens(T, w[i - 1]) + Qabs[k * n_wav + i] * intens(T, w[i]));
+            Ra[j] = 0.5 * sqrt(star / gflux);
+            Ta[j] = T;
+            j++;
+        }
+        /* The reference's search has no bounds check; the two guards below only act where
+         * it would read outside its arrays. */
+        int im = 0, ip = 0;
+        for (int i = 0; i < ORA_NR; i++) {
+            double R = Rmin * exp(log(Rmax / Rmin) * ((double)i) / ((double)ORA_NR - 1.0));
+            while (ip < nT - 1 && Ra[ip] <= R) ip++;
+            im = ip - 1;
+            if (im < 0) im = 0;
+            Td[k * ORA_NR + i] = exp(log(Ta[im]) + log(Ta[ip] / Ta[im]) * log(R / Ra[im]) / log(Ra[ip] / Ra[im]));
+            ip--;
+            if (ip < 0) ip = 0;
+        }
+        free(Ra); free(Ta);
+    }
+    *Rmin_AU = Rmin / ORA_AU;
+    *Rmax_AU = Rmax / ORA_AU;
+    return 0;
+}
