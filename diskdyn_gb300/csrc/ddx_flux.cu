@@ -27,6 +27,7 @@ __global__ void view_setup_kernel(ViewConst* vc, ddx_view v, int n_theta) {
     c.rot = v.longitude;
     c.incl = v.inc;
     c.PA = v.PA;
+    c.fov = v.fov;
     c.xsize = v.xsize;
     c.ysize = v.ysize;
     c.ntheta = n_theta;
@@ -40,23 +41,39 @@ __global__ void view_setup_kernel(ViewConst* vc, ddx_view v, int n_theta) {
     *vc = c;
 }
 
-// Reference pixel sequence (src/gpu_functions.cu:1001-1008, 1027-1044), kept out of
-// line so the common path does not carry its registers.
+// Reference geometry sequence (src/gpu_functions.cu:1001-1044), kept out of line so the
+// common path does not carry its registers.  It reproduces the reference's whole
+// expression graph up to the pixel floor -- including R, the scattering-angle cosine and
+// the products they share with the pixel chain (x*x of the rotated position, z*z) --
+// because the compiler's FMA contraction of a product depends on how many expressions
+// use it.  Returns the pixel and the clamped scattering-angle cosine.
 __device__ __noinline__ void exact_pixel(double x, double y, double z, const ViewConst& v,
-                                         int& xim, int& yim) {
+                                         int& xim, int& yim, double& cossc_out) {
+    const double rot = v.rot, incl = v.incl, PA = v.PA, dist = v.dist, FOV = v.fov;
+    const int xsize = v.xsize, ysize = v.ysize, ntheta = v.ntheta;
     double phi = atan2(y, x);
+    double R = sqrt(x * x + y * y + z * z);
     double Rd = sqrt(x * x + y * y);
-    x = Rd * cos(phi + v.rot);
-    y = Rd * sin(phi + v.rot);
-    y = sqrt(y * y + z * z) * cos(atan2(z, y) - v.incl);
+    x = Rd * cos(phi + rot);
+    y = Rd * sin(phi + rot);
+    double ly = -dist * sin(incl) - y;
+    double lz = dist * cos(incl) - z;
+    double cossc = (x * x + (-y) * ly + (-z) * lz) / R / sqrt(x * x + ly * ly + lz * lz);
+    if (cossc < -1) cossc = -1.0;
+    if (cossc >= 1.0 - 2.0 / ntheta) cossc = 1.0 - 2.0 / ntheta;
+    y = sqrt(y * y + z * z) * cos(atan2(z, y) - incl);
     phi = atan2(y, x);
     Rd = sqrt(x * x + y * y);
-    x = Rd * cos(phi + v.PA);
-    y = Rd * sin(phi + v.PA);
-    x = x + 0.5 * v.psca * v.xsize;
-    y = y + 0.5 * v.psca * v.ysize;
-    xim = floor(x / v.psca);
-    yim = floor(y / v.psca);
+    x = Rd * cos(phi + PA);
+    y = Rd * sin(phi + PA);
+    double psca;
+    if (xsize >= ysize) psca = FOV / xsize;
+    else                psca = FOV / ysize;
+    x = x + 0.5 * psca * xsize;
+    y = y + 0.5 * psca * ysize;
+    xim = floor(x / psca);
+    yim = floor(y / psca);
+    cossc_out = cossc;
 }
 
 // Width of the band around a pixel edge inside which the fast projection is not trusted.
@@ -166,9 +183,11 @@ image_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ 
     double u, w;
     fast_pixel_coord(x, y, z, v, u, w);
     int xim, yim;
+    double cossc;
     const double g = guard_width(R, fmax(fabs(u), fabs(w)), v);
-    if (near_edge(u, g) || near_edge(w, g)) {
-        exact_pixel(x, y, z, v, xim, yim);
+    const bool exact = near_edge(u, g) || near_edge(w, g);
+    if (exact) {
+        exact_pixel(x, y, z, v, xim, yim, cossc);
         atomicAdd(nexact, 1ull);
     } else {
         xim = (int)floor(u);
@@ -177,9 +196,11 @@ image_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ 
     if (xim < 0 || xim > v.xsize - 1 || yim < 0 || yim > v.ysize - 1) return;
     if (!(R > o.Rmin)) return;
 
-    const double x1 = x * v.cr - y * v.sr;
-    const double y1 = x * v.sr + y * v.cr;
-    const double cossc = scatter_cos(x1, y1, z, R, v);
+    if (!exact) {
+        const double x1 = x * v.cr - y * v.sr;
+        const double y1 = x * v.sr + y * v.cr;
+        cossc = scatter_cos(x1, y1, z, R, v);
+    }
     int cosinm; double wt;
     phase_bracket(cossc, v.ntheta, cosinm, wt);
     const double T = dust_temperature(R, id, o);
@@ -211,7 +232,8 @@ __global__ void pixel_kernel(ddx_state s, int n_grav, int n_dust, const ViewCons
     int xim, yim;
     const double g = guard_width(R, fmax(fabs(u), fabs(w)), v);
     if (near_edge(u, g) || near_edge(w, g)) {
-        exact_pixel(x, y, z, v, xim, yim);
+        double cossc;
+        exact_pixel(x, y, z, v, xim, yim, cossc);
         exact[i] = 1;
     } else {
         xim = (int)floor(u);

@@ -8,7 +8,7 @@ constexpr int kMaxImages = 64;   // image wavelengths per ddx_image call
 
 // Constants of one observer geometry (device resident, written by view_setup_kernel).
 struct ViewConst {
-    double dist, rot, incl, PA, psca;
+    double dist, rot, incl, PA, psca, fov;
     double cr, sr, ci, si, cp, sp;   // cos/sin of rot, incl, PA
     double ly0, lz0;                 // -dist sin(incl), dist cos(incl)
     int xsize, ysize, ntheta;

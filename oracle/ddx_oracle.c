@@ -79,11 +79,19 @@ static void massive_rk4(int ng, ora_state s, double dt, double *kpos, int ref_si
         if (ref_single) {
             memset(kpos, 0, sizeof(double) * 12 * n);
         } else {
+            /* A lone star feels no force: its stage positions are ballistic and the RK4
+             * combination moves it by v dt. */
             for (int st = 0; st < 4; ++st) {
                 double c = st == 0 ? 0.0 : (st == 3 ? dt : dt * 0.5);
                 kpos[(st * 3 + 0) * n] = s.x[0] + s.vx[0] * c;
                 kpos[(st * 3 + 1) * n] = s.y[0] + s.vy[0] * c;
                 kpos[(st * 3 + 2) * n] = s.z[0] + s.vz[0] * c;
+            }
+            if (ng == 1) {
+                double d6 = dt / 6.0;
+                s.x[0] += d6 * (s.vx[0] + 2.0 * s.vx[0] + 2.0 * s.vx[0] + s.vx[0]);
+                s.y[0] += d6 * (s.vy[0] + 2.0 * s.vy[0] + 2.0 * s.vy[0] + s.vy[0]);
+                s.z[0] += d6 * (s.vz[0] + 2.0 * s.vz[0] + 2.0 * s.vz[0] + s.vz[0]);
             }
         }
         return;
