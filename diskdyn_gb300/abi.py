@@ -65,6 +65,9 @@ SIGNATURES = [
                                 C.POINTER(Phys), C.c_int, C.c_int, C.c_void_p]),
     ("ddx_massive_final", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double,
                                     C.POINTER(Phys), C.c_int, C.c_int, C.c_void_p]),
+    ("ddx_step_noalloc", C.c_int, [C.c_int, C.POINTER(State), C.c_int, C.c_int, C.c_double,
+                                   C.POINTER(Phys), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_int, C.c_int, C.c_void_p]),
     ("ddx_evolve", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double, C.c_int,
                              C.POINTER(Phys), C.c_int, C.c_int, C.c_void_p]),
     ("ddx_image", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.POINTER(View),

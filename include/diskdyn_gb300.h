@@ -133,6 +133,26 @@ int ddx_massive_final(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, 
 int ddx_evolve(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
                int n_steps, const ddx_phys *phys, int precision, int mode, void *stream);
 
+/* ddx_step without any device allocation.  No counterpart in the reference.
+ *
+ * Some callers cannot call cudaMalloc, for example a host inside a framework whose pool
+ * allocator owns all device memory, or a loop that must keep a fixed device footprint.
+ * This entry point needs no context.  Its scratch is one file-scope __device__ array of
+ * fixed size (about 3.4 MiB), which every GPU that loads the library holds until the
+ * process exits.  It takes at most DDX_NOALLOC_MAX_GRAV massive bodies and
+ * DDX_MAX_SIZE_BINS size bins and answers DDX_ERR_RANGE beyond that.  beta, betasw and q
+ * are device pointers with n_grid entries; everything else is as for ddx_step.
+ *
+ * The first call on a device resolves the array's device address (cudaGetSymbolAddress
+ * with that device current).  Make that first call before any stream capture.  All
+ * calls share the one array, so calls that overlap on the GPU (different streams,
+ * different host threads) race; serialise them.  Each call writes every scratch word it
+ * reads, so nothing carries over from the previous call. */
+#define DDX_NOALLOC_MAX_GRAV 8192
+int ddx_step_noalloc(int device, const ddx_state *s, int n_grav, int n_dust, double dt,
+                     const ddx_phys *phys, int n_grid, const float *beta, const float *betasw,
+                     const float *q, int precision, int mode, void *stream);
+
 /* Images at the table wavelengths wj[0..n_img-1]: scattered + thermal flux of every
  * dust tracer with id >= 0, projected through `view` and summed into
  * Fd[img][xsize*ysize] (device pointer), pixel (x, y) at Fd[img*npix + ysize*x + y]

@@ -1,0 +1,66 @@
+"""ddx_step_noalloc: the RK4 step for callers that cannot allocate device memory.
+
+Those callers -- a host inside a framework whose pool allocator owns the device memory,
+or a loop that must keep a fixed device footprint -- get a step whose scratch is a fixed
+file-scope device array instead of cudaMalloc'd context buffers.  The test calls it
+through the C ABI twice in a row (the second call reuses the array the first one left
+behind) and checks every result against ddx_step on the same input, bit for bit, since
+both run the same kernels.  It passes alone in a fresh process and after the other
+tests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from diskdyn_gb300 import abi, synth
+from diskdyn_gb300.engine import DeviceState, make_phys
+
+pytestmark = pytest.mark.gpu
+
+
+def noalloc_step(lib, st, sysm, tab, prec, mode):
+    phys = make_phys(**sysm.phys)
+    r = lib.ddx_step_noalloc(0, C.byref(st._abi), sysm.n_grav, st.n_all - sysm.n_grav, C.c_double(sysm.dt),
+                             C.byref(phys), len(tab["beta"]), C.c_void_p(tab["beta"].data_ptr()),
+                             C.c_void_p(tab["betasw"].data_ptr()), C.c_void_p(tab["q"].data_ptr()),
+                             prec, mode, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    abi.check(r, "ddx_step_noalloc")
+
+
+@pytest.mark.parametrize("prec", [abi.DDX_PREC_FP64, abi.DDX_PREC_MIXED])
+@pytest.mark.parametrize("mode", [abi.DDX_MODE_FIXED, abi.DDX_MODE_REFERENCE])
+def test_noalloc_step_matches_ddx_step_twice(built_lib, prec, mode):
+    from diskdyn_gb300.engine import Engine
+    lib = abi.load()
+    eng = Engine(0)
+    sysm = synth.dusty_ring(n_dust=4096, n_plsml=300, seed=21, n_steps=2)
+    eng.set_size_table(**sysm.size_table)
+    tab = {k: torch.tensor(np.asarray(sysm.size_table[k], np.float32), device="cuda")
+           for k in ("beta", "betasw", "q")}
+    a = DeviceState.from_numpy(sysm.state)
+    b = DeviceState.from_numpy(sysm.state)
+    for _ in range(2):
+        eng.step(a, sysm.n_grav, sysm.dt, make_phys(**sysm.phys), prec, mode)
+        noalloc_step(lib, b, sysm, tab, prec, mode)
+        torch.cuda.synchronize()
+        for f in ("x", "y", "z", "vx", "vy", "vz", "N"):
+            assert torch.equal(getattr(a, f), getattr(b, f)), f
+    eng.close()
+
+
+def test_noalloc_rejects_sizes_beyond_its_limit(built_lib):
+    lib = abi.load()
+    sysm = synth.solar_like(n_dust=8)
+    st = DeviceState.from_numpy(sysm.state)
+    phys = make_phys(**sysm.phys)
+    tab = torch.zeros(4, dtype=torch.float32, device="cuda")
+    p = C.c_void_p(tab.data_ptr())
+    too_many = abi.load().ddx_step_noalloc(0, C.byref(st._abi), 8193, 0, C.c_double(0.1), C.byref(phys),
+                                            4, p, p, p, 0, 0, None)
+    assert too_many == 5
+    assert lib.ddx_step_noalloc(0, C.byref(st._abi), sysm.n_grav, 8, C.c_double(0.1), C.byref(phys),
+                                2701, p, p, p, 0, 0, None) == 5
+    assert lib.ddx_step_noalloc(0, C.byref(st._abi), 0, 8, C.c_double(0.1), C.byref(phys),
+                                4, p, p, p, 0, 0, None) == 1
