@@ -77,6 +77,8 @@ SIGNATURES = [
     ("ddx_debug_pixels", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.POINTER(View),
                                    C.c_void_p, C.c_void_p]),
     ("ddx_debug_exact_pixel_count", C.c_ulonglong, [C.c_void_p]),
+    ("ddx_sync_status", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("ddx_debug_lose_tile_copy", C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong]),
     ("ddx_probe_fma_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
 

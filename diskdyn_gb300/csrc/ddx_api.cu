@@ -26,7 +26,20 @@ struct ddx_ctx {
     double* sed_partial = nullptr;
     int sed_partial_cap = 0;
     unsigned long long* counters = nullptr;   // [0]: tracers that took the exact pixel path
+    int* status = nullptr;                      // kStatus* bits set by kernels (device)
+    int inject_lose_tile = -1;                  // one-shot test hook for the next mixed dust launch
+    unsigned long long inject_wait_ns = 0;
 };
+
+namespace {
+void take_injection(ddx_ctx* c, StepArgs& a) {
+    if (c->inject_lose_tile >= 0) {
+        a.lose_tile = c->inject_lose_tile;
+        a.wait_ns = c->inject_wait_ns;
+        c->inject_lose_tile = -1;
+    }
+}
+}  // namespace
 
 namespace {
 
@@ -40,8 +53,8 @@ cudaError_t dalloc(T** p, size_t n) {
 }
 
 void free_massive(MassiveScratch& ms) {
-    cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.A); cudaFree(ms.R);
-    ms = MassiveScratch{};
+    cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.PP); cudaFree(ms.A); cudaFree(ms.R);
+    ms = MassiveScratch{};   // the status word belongs to the context, not to the scratch
 }
 
 int ensure_massive(ddx_ctx* c, int n_grav) {
@@ -51,9 +64,12 @@ int ensure_massive(ddx_ctx* c, int n_grav) {
     while (cap < n_grav) cap *= 2;
     MassiveScratch ms{};
     ms.cap = cap;
+    ms.pcap = pair_count(cap) + kPairSpan;
+    ms.status = c->status;
     if (dalloc(&ms.P, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.Phi, (size_t)4 * cap) != cudaSuccess ||
-        dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess ||
-        dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess) {
+        dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.PP, (size_t)4 * ms.pcap) != cudaSuccess ||
+        dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess || dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess) {
+        ms.status = nullptr;
         free_massive(ms);
         cudaGetLastError();
         return DDX_ERR_NOMEM;
@@ -82,6 +98,8 @@ int make_step_args(const ddx_phys* p, int n_grav, int n_dust, double dt, int mod
     a.vswAU = p->vsw_AUyr;
     a.Rmin = p->Rmin;
     a.mode = mode;
+    a.lose_tile = -1;
+    a.wait_ns = kDefaultWaitNs;
     return DDX_OK;
 }
 
@@ -98,7 +116,8 @@ __global__ void star_only_reference_kernel(ddx_state s, MassiveScratch ms) {
     }
 }
 
-int enqueue_step(ddx_ctx* c, const ddx_state& s, const StepArgs& a, int precision, cudaStream_t st) {
+int enqueue_step(ddx_ctx* c, const ddx_state& s, StepArgs a, int precision, cudaStream_t st) {
+    take_injection(c, a);
     if (a.n_grav == 1 && a.mode == DDX_MODE_REFERENCE) {
         star_only_reference_kernel<<<1, 32, 0, st>>>(s, c->ms);
         if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
@@ -149,12 +168,13 @@ int ddx_create(ddx_ctx** out, int device) {
     ddx_ctx* c = new ddx_ctx();
     c->device = device;
     if (dalloc(&c->vc, 1) != cudaSuccess || dalloc(&c->od_dev, 1) != cudaSuccess ||
-        dalloc(&c->counters, 4) != cudaSuccess) {
-        cudaFree(c->vc); cudaFree(c->od_dev); cudaFree(c->counters);
+        dalloc(&c->counters, 4) != cudaSuccess || dalloc(&c->status, 1) != cudaSuccess) {
+        cudaFree(c->vc); cudaFree(c->od_dev); cudaFree(c->counters); cudaFree(c->status);
         delete c;
         return DDX_ERR_NOMEM;
     }
     cudaMemset(c->counters, 0, 4 * sizeof(unsigned long long));
+    cudaMemset(c->status, 0, sizeof(int));
     *out = c;
     return DDX_OK;
 }
@@ -165,7 +185,7 @@ int ddx_destroy(ddx_ctx* c) {
     free_massive(c->ms);
     free_optics(c);
     cudaFree(c->bins); cudaFree(c->size_d); cudaFree(c->vc); cudaFree(c->od_dev);
-    cudaFree(c->sed_partial); cudaFree(c->counters);
+    cudaFree(c->sed_partial); cudaFree(c->counters); cudaFree(c->status);
     delete c;
     return DDX_OK;
 }
@@ -282,7 +302,15 @@ int ddx_small_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double
     StepArgs a;
     int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
     if (r) return r;
+    take_injection(c, a);
     return cuda_status(launch_dust(*s, a, c->ms, c->bins, precision, (cudaStream_t)stream));
+}
+
+int ddx_debug_lose_tile_copy(ddx_ctx* c, int tile, unsigned long long wait_ns) {
+    if (!c || tile < 0 || wait_ns == 0) return DDX_ERR_ARG;
+    c->inject_lose_tile = tile;
+    c->inject_wait_ns = wait_ns;
+    return DDX_OK;
 }
 
 int ddx_massive_final(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
@@ -341,6 +369,16 @@ int ddx_debug_pixels(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, con
     cudaSetDevice(c->device);
     const int n_theta = c->optics_set ? c->od.n_theta : 2;
     return cuda_status(launch_pixels(*s, n_grav, n_dust, *view, n_theta, c->vc, pix, exact, 0));
+}
+
+int ddx_sync_status(ddx_ctx* c, void* stream) {
+    if (!c) return DDX_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return DDX_ERR_CUDA;
+    int h = 0;
+    if (cudaMemcpy(&h, c->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DDX_ERR_CUDA;
+    if (h != 0 && cudaMemset(c->status, 0, sizeof(int)) != cudaSuccess) return DDX_ERR_CUDA;
+    return (h & kStatusTimeout) ? DDX_ERR_TIMEOUT : DDX_OK;
 }
 
 // Number of tracers that took the exact (reference-sequence) pixel path since the

@@ -1,0 +1,287 @@
+// Mixed-precision RK4 of the dust tracers on sm_103a (src/gpu_functions.cu:627-943).
+//
+// FP64: tracer state, stage positions and velocities, the star term (reduced gravity,
+// PR + stellar-wind drag, Lorentz force) and the RK4 combination.  FP32: the gravity of
+// the perturbing bodies, on hi/lo split positions so the separation keeps FP32 relative
+// precision at any distance from the star, with plain sums over spans of 16 sources and a
+// Kahan sum across spans.
+//
+// Blackwell mapping:
+//  - perturbers arrive as 64-byte pair records (two bodies per record, one quantity of
+//    both bodies per 8-byte slot), and every FP32 operation of the pair force runs as one
+//    f32x2 instruction (add/sub/mul/fma.rn.f32x2) on both bodies, halving the issue
+//    slots of the FP32 work, which is what bounds this kernel;
+//  - the pair records of all four stages stream through two shared-memory tiles filled
+//    by TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx), so tile k+1 lands while
+//    tile k is consumed; every thread of the block reads the same record (broadcast);
+//  - each mbarrier wait is bounded by the global timer; a block that gives up sets the
+//    context's status word, waits (bounded) for its own copies, leaves its tracers
+//    untouched and exits.
+#include "ddx_internal.cuh"
+
+namespace ddx {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTilePairs = 512;                 // pair records per tile (32 KiB)
+
+typedef unsigned long long f2;   // two FP32 lanes of one f32x2 instruction
+
+__device__ __forceinline__ f2 f2_dup(float a) {
+    f2 r; asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a)); return r;
+}
+__device__ __forceinline__ void f2_split(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_join(float lo, float hi) {
+    f2 r; asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi)); return r;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c)); return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r; asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r;
+}
+__device__ __forceinline__ void kahan2(f2& S, f2& C, f2 v) {
+    const f2 y = sub2(v, C);
+    const f2 t = add2(S, y);
+    C = sub2(sub2(t, S), y);
+    S = t;
+}
+// Compensated sum of both lanes of (S, C), in FP64.
+__device__ __forceinline__ double f2_total(f2 S, f2 C) {
+    float s0, s1, c0, c1;
+    f2_split(S, s0, s1);
+    f2_split(C, c0, c1);
+    return ((double)s0 - (double)c0) + ((double)s1 - (double)c1);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t; asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t)); return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t mb, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(mb), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mb, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mb), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, unsigned bytes, uint32_t mb) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(mb) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t mb, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(mb), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Wait for phase `parity` of the mbarrier to complete, for at most limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, unsigned parity, unsigned long long limit_ns) {
+    if (mbar_try(mb, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try(mb, parity))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads, 2)
+dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) unsigned long long mbar[2];
+    BodyPair* const tiles = reinterpret_cast<BodyPair*>(smem);
+    const int tid = threadIdx.x;
+    const int i = blockIdx.x * kThreads + tid;
+    const int ng = a.n_grav;
+    const int t = ng + i;
+
+    bool alive = false;
+    double x = 0, y = 0, z = 0, vx = 0, vy = 0, vz = 0, m = 1.0;
+    float bet = 0.f, betsw = 0.f, qe = 0.f;
+    if (i < a.n_dust) {
+        alive = (s.N[t] != 0.0);
+        if (alive) {
+            x = s.x[t]; y = s.y[t]; z = s.z[t];
+            vx = s.vx[t]; vy = s.vy[t]; vz = s.vz[t];
+            m = s.m[t];
+            const int id = s.id[t];
+            if (id >= 0) {
+                const SizeBin b = bins[id];
+                bet = b.beta; betsw = b.betasw; qe = b.q;
+            }
+        }
+    }
+
+    const int npairs = pair_count(ng);
+    const int ntiles = (npairs + kTilePairs - 1) / kTilePairs;
+    const int G = 4 * ntiles;                       // tiles over all four stages
+    const uint32_t mb[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
+    if (tid == 0) {
+        mbar_init(mb[0], 1);
+        mbar_init(mb[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    // Thread 0 streams tile g of the sequence (stage-major) into buffer g & 1.  The test
+    // hook a.lose_tile leaves one tile's copy unissued, so the waits on it run out.
+    // in_flight: tiles issued and not yet consumed (thread 0 only; at most two).
+    int in_flight[2] = {-1, -1};
+    auto issue = [&](int g) {
+        if (g == a.lose_tile) return;
+        const int stg = g / ntiles, first = (g - stg * ntiles) * kTilePairs;
+        const unsigned bytes = (unsigned)(min(kTilePairs, npairs - first) * sizeof(BodyPair));
+        mbar_expect_tx(mb[g & 1], bytes);
+        bulk_load(smem_u32(tiles + (g & 1) * kTilePairs), ms.PP + (size_t)stg * ms.pcap + first, bytes,
+                  mb[g & 1]);
+        in_flight[g & 1] = g;
+    };
+    if (tid == 0 && G > 0) issue(0);
+
+    const double dt = a.dt, dt2 = a.dt / 2.0, dt6 = a.dt / 6.0;
+    double k1vx = 0, k1vy = 0, k1vz = 0, k2vx = 0, k2vy = 0, k2vz = 0;
+    double k3vx = 0, k3vy = 0, k3vz = 0, k4vx = 0, k4vy = 0, k4vz = 0;
+    double k2rx = 0, k2ry = 0, k2rz = 0, k3rx = 0, k3ry = 0, k3rz = 0;
+    double k4rx = 0, k4ry = 0, k4rz = 0;
+    int removed = 0, removed_stage = -1;
+    int lost = 0;
+    int g = 0;
+
+#pragma unroll 1
+    for (int st = 0; st < 4; ++st) {
+        double xt, yt, zt, rx, ry, rz;
+        if (st == 0)      { xt = x; yt = y; zt = z; rx = vx; ry = vy; rz = vz; }
+        else if (st == 1) {
+            k2rx = vx + k1vx * dt2; k2ry = vy + k1vy * dt2; k2rz = vz + k1vz * dt2;
+            xt = x + vx * dt2; yt = y + vy * dt2; zt = z + vz * dt2;
+            rx = k2rx; ry = k2ry; rz = k2rz;
+        } else if (st == 2) {
+            k3rx = vx + k2vx * dt2; k3ry = vy + k2vy * dt2; k3rz = vz + k2vz * dt2;
+            xt = x + k2rx * dt2; yt = y + k2ry * dt2; zt = z + k2rz * dt2;
+            rx = k3rx; ry = k3ry; rz = k3rz;
+        } else {
+            k4rx = vx + k3vx * dt; k4ry = vy + k3vy * dt; k4rz = vz + k3vz * dt;
+            xt = x + k3rx * dt; yt = y + k3ry * dt; zt = z + k3rz * dt;
+            rx = k4rx; ry = k4ry; rz = k4rz;
+        }
+        double kx = 0, ky = 0, kz = 0;
+        if (alive) {
+            const Body ps = ms.P[st * ms.cap + 0];
+            if (!star_term(xt - ps.x, yt - ps.y, zt - ps.z, rx, ry, rz, ps.m, bet, betsw, qe, m, a,
+                           kx, ky, kz)) {
+                alive = false; removed = 1; removed_stage = st;
+            }
+        }
+        float xh, xl, yh, yl, zh, zl;
+        split_hilo(xt, xh, xl); split_hilo(yt, yh, yl); split_hilo(zt, zh, zl);
+        const f2 XH = f2_dup(xh), XL = f2_dup(xl), YH = f2_dup(yh), YL = f2_dup(yl);
+        const f2 ZH = f2_dup(zh), ZL = f2_dup(zl);
+        f2 Sx = 0, Sy = 0, Sz = 0, Cx = 0, Cy = 0, Cz = 0;
+        for (int tt = 0; tt < ntiles; ++tt, ++g) {
+            lost = __syncthreads_or(lost);      // also: every thread is done with tile g-1
+            if (lost) break;
+            if (tid == 0 && g + 1 < G) issue(g + 1);
+            if (!mbar_wait(mb[g & 1], (g >> 1) & 1, a.wait_ns)) { lost = 1; continue; }
+            if (tid == 0) in_flight[g & 1] = -1;
+            if (!alive) continue;
+            const BodyPair* T = tiles + (g & 1) * kTilePairs;
+            const int cnt = min(kTilePairs, npairs - tt * kTilePairs);   // a multiple of kPairSpan
+            for (int k = 0; k < cnt; k += kPairSpan) {
+                f2 px = 0, py = 0, pz = 0;
+#pragma unroll
+                for (int u = 0; u < kPairSpan; ++u) {
+                    const BodyPair* r = T + k + u;
+                    const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);  // hx, hy
+                    const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);  // hz, m
+                    const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r->lx);  // lx, ly
+                    const f2 lz = *reinterpret_cast<const f2*>(r->lz);
+                    const f2 dX = add2(sub2(q0.x, XH), sub2(q2.x, XL));
+                    const f2 dY = add2(sub2(q0.y, YH), sub2(q2.y, YL));
+                    const f2 dZ = add2(sub2(q1.x, ZH), sub2(lz, ZL));
+                    const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+                    float r0, r1;
+                    f2_split(RR, r0, r1);
+                    const f2 ri = f2_join(rsqrt_approx(r0), rsqrt_approx(r1));
+                    const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
+                    px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+                }
+                kahan2(Sx, Cx, px); kahan2(Sy, Cy, py); kahan2(Sz, Cz, pz);
+            }
+        }
+        if (ntiles > 0) lost = __syncthreads_or(lost);   // block-uniform before branching on it
+        if (lost) break;
+        if (alive) {
+            const double px = f2_total(Sx, Cx), py = f2_total(Sy, Cy), pz = f2_total(Sz, Cz);
+            // An exact coincidence makes RR = 0, the rsqrt infinite and the sum NaN.
+            if (!(isfinite(px) && isfinite(py) && isfinite(pz))) {
+                alive = false; removed = 2; removed_stage = st;
+            }
+            kx += px; ky += py; kz += pz;
+        }
+        if (st == 0)      { k1vx = kx; k1vy = ky; k1vz = kz; }
+        else if (st == 1) { k2vx = kx; k2vy = ky; k2vz = kz; }
+        else if (st == 2) { k3vx = kx; k3vy = ky; k3vz = kz; }
+        else              { k4vx = kx; k4vy = ky; k4vz = kz; }
+    }
+    lost = __syncthreads_or(lost);
+    if (lost) {
+        if (tid == 0) {
+            atomicOr(ms.status, kStatusTimeout);
+            // let this block's copies that are still in flight land before it exits
+            for (int b = 0; b < 2; ++b)
+                if (in_flight[b] >= 0) mbar_wait(mb[b], (in_flight[b] >> 1) & 1, a.wait_ns);
+        }
+        return;
+    }
+    if (i >= a.n_dust) return;
+    if (removed) {
+        if (removed == 1 && removed_stage == 3 && a.mode == DDX_MODE_REFERENCE) s.N[i] = 0;
+        else s.N[t] = 0;
+        return;
+    }
+    if (!alive) return;
+    x += dt6 * (vx + 2.0 * (k2rx + k3rx) + k4rx);
+    y += dt6 * (vy + 2.0 * (k2ry + k3ry) + k4ry);
+    z += dt6 * (vz + 2.0 * (k2rz + k3rz) + k4rz);
+    vx += dt6 * (k1vx + 2.0 * (k2vx + k3vx) + k4vx);
+    vy += dt6 * (k1vy + 2.0 * (k2vy + k3vy) + k4vy);
+    vz += dt6 * (k1vz + 2.0 * (k2vz + k3vz) + k4vz);
+    s.x[t] = x; s.y[t] = y; s.z[t] = z;
+    s.vx[t] = vx; s.vy[t] = vy; s.vz[t] = vz;
+}
+
+}  // namespace
+
+cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
+                              const SizeBin* bins, cudaStream_t st) {
+    if (a.n_dust <= 0) return cudaSuccess;
+    const size_t smem = 2 * (size_t)kTilePairs * sizeof(BodyPair);
+    static bool attr_set[128] = {};   // the attribute is set once per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(dust_rk4_mixed_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    const int blocks = (a.n_dust + kThreads - 1) / kThreads;
+    dust_rk4_mixed_kernel<<<blocks, kThreads, smem, st>>>(s, a, ms, bins);
+    return cudaGetLastError();
+}
+
+}  // namespace ddx

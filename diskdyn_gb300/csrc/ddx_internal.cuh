@@ -31,7 +31,11 @@ struct StepArgs {
     int    SWQ, FLQ;
     double Wz, Bstar, Rstar, vswAU, Rmin;
     int    mode;            // DDX_MODE_*
+    int    lose_tile;       // test hook: tile whose copy is never issued (-1: none)
+    unsigned long long wait_ns;   // bound on any one device-side wait
 };
+
+constexpr unsigned long long kDefaultWaitNs = 2000000000ull;   // 2 s
 
 // One massive body at one RK4 stage: position and mass.  32-byte aligned so a record
 // moves with one 256-bit access.
@@ -42,22 +46,79 @@ __host__ __device__ __forceinline__ Body make_body(double x, double y, double z,
     Body b; b.x = x; b.y = y; b.z = z; b.m = m; return b;
 }
 
-// Stage scratch for the massive set.  Positions of the four RK4 stages are kept as
-// {x, y, z, m} records so the dust kernel stages them through shared memory with
-// 16-byte vector copies.  The mixed path also keeps an FP32 hi/lo split of each
-// stage position: x = hi + lo with hi = fp32(x), lo = fp32(x - hi).
-struct MassiveScratch {
-    Body    *P;      // [4][cap] stage positions P1..P4 with the mass
-    float4  *Phi;    // [4][cap] fp32 hi part, m in .w
-    float4  *Plo;    // [4][cap] fp32 lo part
-    double  *A;      // [4][3][cap] stage accelerations A1..A4
-    double  *R;      // [3][3][cap] stage velocities R2..R4
-    int      cap;
+// Two perturbing bodies (sources 1+2k and 2+2k of one RK4 stage) in the layout the mixed
+// dust kernel consumes: every 8-byte slot holds the same quantity of both bodies, so one
+// f32x2 instruction works on the pair.  hi/lo is the FP32 split x = hi + lo with
+// hi = fp32(x), lo = fp32(x - hi).  64 bytes, moved into shared memory by TMA bulk copies.
+struct __align__(16) BodyPair {
+    float hx[2], hy[2], hz[2], m[2];
+    float lx[2], ly[2], lz[2], pad[2];
 };
+
+constexpr int kPairSpan = 8;     // pair records per plain-FP32 partial sum (16 sources)
+
+// Pair records per stage needed for n_grav bodies: sources 1..n_grav-1 in pairs, padded
+// with zero-mass records to a multiple of kPairSpan.
+__host__ __device__ constexpr int pair_count(int n_grav) {
+    const int np = n_grav / 2;   // ceil((n_grav - 1) / 2)
+    return (np + kPairSpan - 1) / kPairSpan * kPairSpan;
+}
+
+// Stage scratch for the massive set.  Positions of the four RK4 stages are kept as
+// {x, y, z, m} records for the FP64 dust kernels.  The mixed path also keeps an FP32
+// hi/lo split of each stage position, per body (Phi/Plo, for the massive passes) and in
+// pair records (PP, for the dust kernel).
+struct MassiveScratch {
+    Body     *P;      // [4][cap] stage positions P1..P4 with the mass
+    float4   *Phi;    // [4][cap] fp32 hi part, m in .w
+    float4   *Plo;    // [4][cap] fp32 lo part
+    BodyPair *PP;     // [4][pcap] pair records of sources 1..n_grav-1
+    double   *A;      // [4][3][cap] stage accelerations A1..A4
+    double   *R;      // [3][3][cap] stage velocities R2..R4
+    int      *status; // device status word: DDX_STATUS_* bits set by kernels
+    int       cap;
+    int       pcap;   // pair records per stage, >= pair_count(cap)
+};
+
+// Bits of the device status word.
+constexpr int kStatusTimeout = 1;   // a bounded mbarrier wait gave up
 
 __device__ __forceinline__ void split_hilo(double v, float& hi, float& lo) {
     hi = __double2float_rn(v);
     lo = __double2float_rn(v - (double)hi);
+}
+
+// Star term of one stage (src/gpu_functions.cu:680-718): gravity reduced by beta+beta_sw,
+// PR + stellar-wind drag, optional Lorentz force.  Returns false when the tracer is
+// inside the sublimation radius.  Written operation for operation like the reference so
+// that the FP64 results agree bit for bit on the same GPU.
+__device__ __forceinline__ bool star_term(double dx, double dy, double dz, double rx, double ry,
+                                          double rz, double m0, float bet, float betsw, float qe,
+                                          double m, const StepArgs& a, double& kx, double& ky,
+                                          double& kz) {
+    const double RR = dx * dx + dy * dy + dz * dz;
+    const double RR3 = RR * sqrt(RR);
+    if (RR <= a.Rmin * a.Rmin) return false;
+    const double Fg = (1.0 - bet - betsw) * m0 / RR3;
+    double Fbase1;
+    if (a.SWQ == 1) Fbase1 = m0 / RR * (bet / kLightAU + betsw / a.vswAU);
+    else            Fbase1 = bet * m0 / kLightAU / RR;
+    const double Fbase2 = (dx * rx + dy * ry + dz * rz) / RR;
+    const double Fdrx = Fbase1 * (Fbase2 * dx + rx);
+    const double Fdry = Fbase1 * (Fbase2 * dy + ry);
+    const double Fdrz = Fbase1 * (Fbase2 * dz + rz);
+    double Flx, Fly;
+    if (a.FLQ == 1) {
+        const double Bz = a.Bstar * a.Rstar * a.Rstar * a.Rstar / RR3;
+        Flx = qe * (ry - a.Wz * dx) * Bz / m;
+        Fly = -qe * (rx + a.Wz * dy) * Bz / m;
+    } else {
+        Flx = 0; Fly = 0;
+    }
+    kx = -Fg * dx - Fdrx + Flx;
+    ky = -Fg * dy - Fdry + Fly;
+    kz = -Fg * dz - Fdrz;
+    return true;
 }
 
 }  // namespace ddx
@@ -72,4 +133,6 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
                                  int precision, cudaStream_t st);
 cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                         const SizeBin* bins, int precision, cudaStream_t st);
+cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
+                              const SizeBin* bins, cudaStream_t st);
 }  // namespace ddx

@@ -25,10 +25,13 @@ constexpr size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 constexpr size_t kOffP = 0;
 constexpr size_t kOffPhi = kOffP + align256(sizeof(Body) * 4 * kCap);
 constexpr size_t kOffPlo = kOffPhi + align256(sizeof(float4) * 4 * kCap);
-constexpr size_t kOffA = kOffPlo + align256(sizeof(float4) * 4 * kCap);
+constexpr int kPcap = pair_count(kCap) + kPairSpan;
+constexpr size_t kOffPP = kOffPlo + align256(sizeof(float4) * 4 * kCap);
+constexpr size_t kOffA = kOffPP + align256(sizeof(BodyPair) * 4 * kPcap);
 constexpr size_t kOffR = kOffA + align256(sizeof(double) * 12 * kCap);
 constexpr size_t kOffBins = kOffR + align256(sizeof(double) * 9 * kCap);
-constexpr size_t kBytes = kOffBins + align256(sizeof(SizeBin) * DDX_MAX_SIZE_BINS);
+constexpr size_t kOffStatus = kOffBins + align256(sizeof(SizeBin) * DDX_MAX_SIZE_BINS);
+constexpr size_t kBytes = kOffStatus + 256;
 
 static __device__ __align__(256) unsigned char g_step_scratch[kBytes];
 
@@ -91,7 +94,10 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     ms.Plo = reinterpret_cast<float4*>(base + kOffPlo);
     ms.A = reinterpret_cast<double*>(base + kOffA);
     ms.R = reinterpret_cast<double*>(base + kOffR);
+    ms.PP = reinterpret_cast<BodyPair*>(base + kOffPP);
+    ms.status = reinterpret_cast<int*>(base + kOffStatus);
     ms.cap = kCap;
+    ms.pcap = kPcap;
     SizeBin* bins = reinterpret_cast<SizeBin*>(base + kOffBins);
 
     StepArgs a;
@@ -108,6 +114,8 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     a.vswAU = p->vsw_AUyr;
     a.Rmin = p->Rmin;
     a.mode = mode;
+    a.lose_tile = -1;
+    a.wait_ns = kDefaultWaitNs;
 
     // Every scratch word a step reads is written earlier in the same step (the packed bins,
     // then the stage records of bodies 0..n_grav-1), so nothing has to be cleared between

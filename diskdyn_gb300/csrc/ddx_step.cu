@@ -22,6 +22,26 @@ namespace ddx {
 // Massive set
 // ---------------------------------------------------------------------------------------
 
+constexpr float kFarAway = 1.0e18f;  // padding source position, AU (mass 0)
+
+// Body i >= 1 into its half of pair record (i-1)/2 of a stage.
+__device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, int i, const float4 h,
+                                                const float4 l) {
+    BodyPair* r = ms.PP + (size_t)stage * ms.pcap + ((i - 1) >> 1);
+    const int k = (i - 1) & 1;
+    r->hx[k] = h.x; r->hy[k] = h.y; r->hz[k] = h.z; r->m[k] = h.w;
+    r->lx[k] = l.x; r->ly[k] = l.y; r->lz[k] = l.z; r->pad[k] = 0.f;
+}
+
+// Zero-mass, far-away filler for the slots past the last perturbing body, so the dust
+// kernel always processes whole spans of kPairSpan records.
+__device__ __forceinline__ void store_pair_padding(MassiveScratch& ms, int n_grav) {
+    const int np = pair_count(n_grav);
+    const float4 h = make_float4(kFarAway, kFarAway, kFarAway, 0.f), l = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int stage = 0; stage < 4; ++stage)
+        for (int i = n_grav; i <= 2 * np; ++i) store_pair_slot(ms, stage, i, h, l);
+}
+
 // P1 = x, P2 = x + v dt/2 (src/gpu_functions.cu:90-99, 219-230).
 __global__ void massive_prepare_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int prec) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,8 +56,11 @@ __global__ void massive_prepare_kernel(ddx_state s, StepArgs a, MassiveScratch m
         split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
         h.w = (float)m; l.w = 0.f;
         ms.Phi[0 * ms.cap + i] = h; ms.Plo[0 * ms.cap + i] = l;
+        if (i > 0) store_pair_slot(ms, 0, i, h, l);
         split_hilo(x2, h.x, l.x); split_hilo(y2, h.y, l.y); split_hilo(z2, h.z, l.z);
         ms.Phi[1 * ms.cap + i] = h; ms.Plo[1 * ms.cap + i] = l;
+        if (i > 0) store_pair_slot(ms, 1, i, h, l);
+        else store_pair_padding(ms, a.n_grav);
     }
 }
 
@@ -135,6 +158,7 @@ __device__ __forceinline__ void store_stage_pos(MassiveScratch& ms, int stage, i
         split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
         h.w = (float)m; l.w = 0.f;
         ms.Phi[stage * ms.cap + i] = h; ms.Plo[stage * ms.cap + i] = l;
+        if (i > 0) store_pair_slot(ms, stage, i, h, l);
     }
 }
 
@@ -197,48 +221,12 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
 enum DustVariant {
     kDustFP64Exact = 0,  // reference arithmetic expression for expression: m/RR/sqrt(RR)
     kDustFP64 = 1,       // FP64 with rsqrt
-    kDustMixed = 2,      // FP32 hi/lo perturbations, Kahan over spans of kSpan sources
 };
 
 constexpr int kDustThreads = 256;
 constexpr int kDustTile = 1024;    // sources per shared-memory tile (32 KiB)
-constexpr int kSpan = 8;           // plain FP32 partial sums over this many sources
-constexpr float kFarAway = 1.0e18f;  // padding source position, AU (mass 0)
 
-// Star term of one stage (src/gpu_functions.cu:680-718): gravity reduced by beta+beta_sw,
-// PR + stellar-wind drag, optional Lorentz force.  Returns false when the tracer is
-// inside the sublimation radius.  Written operation for operation like the reference so
-// that the FP64 results agree bit for bit on the same GPU.
-__device__ __forceinline__ bool star_term(double dx, double dy, double dz, double rx, double ry,
-                                          double rz, double m0, float bet, float betsw, float qe,
-                                          double m, const StepArgs& a, double& kx, double& ky,
-                                          double& kz) {
-    const double RR = dx * dx + dy * dy + dz * dz;
-    const double RR3 = RR * sqrt(RR);
-    if (RR <= a.Rmin * a.Rmin) return false;
-    const double Fg = (1.0 - bet - betsw) * m0 / RR3;
-    double Fbase1;
-    if (a.SWQ == 1) Fbase1 = m0 / RR * (bet / kLightAU + betsw / a.vswAU);
-    else            Fbase1 = bet * m0 / kLightAU / RR;
-    const double Fbase2 = (dx * rx + dy * ry + dz * rz) / RR;
-    const double Fdrx = Fbase1 * (Fbase2 * dx + rx);
-    const double Fdry = Fbase1 * (Fbase2 * dy + ry);
-    const double Fdrz = Fbase1 * (Fbase2 * dz + rz);
-    double Flx, Fly;
-    if (a.FLQ == 1) {
-        const double Bz = a.Bstar * a.Rstar * a.Rstar * a.Rstar / RR3;
-        Flx = qe * (ry - a.Wz * dx) * Bz / m;
-        Fly = -qe * (rx + a.Wz * dy) * Bz / m;
-    } else {
-        Flx = 0; Fly = 0;
-    }
-    kx = -Fg * dx - Fdrx + Flx;
-    ky = -Fg * dy - Fdry + Fly;
-    kz = -Fg * dz - Fdrz;
-    return true;
-}
-
-// Gravity of massive bodies 1..n_grav-1 at stage `st` on every tracer of the block.
+// FP64 gravity of massive bodies 1..n_grav-1 at stage `st` on every tracer of the block.
 // Sources are staged through shared memory tile by tile; every thread of the block takes
 // part in the loads and barriers whether or not its tracer is still alive.
 // Returns false (for the calling thread) on an exact coincidence with a body.
@@ -248,51 +236,7 @@ __device__ __forceinline__ bool dust_perturb(const MassiveScratch& ms, int ng, i
                                              double& ky, double& kz, unsigned char* smem) {
     const int nsrc = ng - 1;
     bool ok = true;
-    if (VAR == kDustMixed) {
-        float4* shi = reinterpret_cast<float4*>(smem);
-        float4* slo = shi + kDustTile;
-        float xh, xl, yh, yl, zh, zl;
-        split_hilo(xt, xh, xl); split_hilo(yt, yh, yl); split_hilo(zt, zh, zl);
-        float Sx = 0.f, Sy = 0.f, Sz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
-        for (int base = 0; base < nsrc; base += kDustTile) {
-            const int cnt = min(kDustTile, nsrc - base);
-            const int padded = (cnt + kSpan - 1) / kSpan * kSpan;
-            __syncthreads();
-            for (int k = threadIdx.x; k < padded; k += blockDim.x) {
-                if (k < cnt) {
-                    shi[k] = ms.Phi[st * ms.cap + 1 + base + k];
-                    slo[k] = ms.Plo[st * ms.cap + 1 + base + k];
-                } else {
-                    shi[k] = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
-                    slo[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-            }
-            __syncthreads();
-            if (alive) {
-                for (int k = 0; k < padded; k += kSpan) {
-                    float px = 0.f, py = 0.f, pz = 0.f;
-#pragma unroll
-                    for (int u = 0; u < kSpan; ++u) {
-                        const float4 h = shi[k + u];
-                        const float4 l = slo[k + u];
-                        const float dX = (xh - h.x) + (xl - l.x);
-                        const float dY = (yh - h.y) + (yl - l.y);
-                        const float dZ = (zh - h.z) + (zl - l.z);
-                        const float RR = fmaf(dX, dX, fmaf(dY, dY, dZ * dZ));
-                        const float ri = rsqrtf(RR);
-                        const float f = h.w * (ri * (ri * ri));
-                        px = fmaf(-f, dX, px); py = fmaf(-f, dY, py); pz = fmaf(-f, dZ, pz);
-                    }
-                    kahan_add(Sx, Cx, px); kahan_add(Sy, Cy, py); kahan_add(Sz, Cz, pz);
-                }
-            }
-        }
-        const double px = (double)Sx - (double)Cx, py = (double)Sy - (double)Cy,
-                     pz = (double)Sz - (double)Cz;
-        // An exact coincidence makes RR = 0, rsqrtf = inf and the sum NaN.
-        if (alive && !(isfinite(px) && isfinite(py) && isfinite(pz))) ok = false;
-        kx += px; ky += py; kz += pz;
-    } else {
+    {
         Body* sP = reinterpret_cast<Body*>(smem);
         for (int base = 0; base < nsrc; base += kDustTile) {
             const int cnt = min(kDustTile, nsrc - base);
@@ -449,7 +393,7 @@ cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScra
     const int blocks = (a.n_dust + kDustThreads - 1) / kDustThreads;
     const size_t smem = (size_t)kDustTile * 32;
     if (precision == DDX_PREC_MIXED) {
-        dust_rk4_kernel<kDustMixed><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
+        return launch_dust_mixed(s, a, ms, bins, st);
     } else if (a.mode == DDX_MODE_REFERENCE) {
         dust_rk4_kernel<kDustFP64Exact><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
     } else {

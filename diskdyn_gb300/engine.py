@@ -163,6 +163,11 @@ class Engine:
         abi.check(fn(self.ctx, C.byref(st._abi), n_grav, st.n_all - n_grav, float(dt), C.byref(phys),
                      precision, mode, C.c_void_p(_stream_handle(stream))), "ddx_" + which)
 
+    def sync_status(self, stream=None) -> int:
+        """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
+        bounded device-side wait since the last call, else 0."""
+        return self.lib.ddx_sync_status(self.ctx, C.c_void_p(_stream_handle(stream)))
+
     # -- flux ---------------------------------------------------------------------------
     def image(self, st: DeviceState, n_grav: int, view: abi.View, wj, out: torch.Tensor | None = None,
               precision: int = abi.DDX_PREC_FP64, stream=None) -> torch.Tensor:

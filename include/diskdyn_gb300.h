@@ -186,6 +186,19 @@ unsigned long long ddx_debug_exact_pixel_count(ddx_ctx *ctx);
  * TFLOP/s (2 flops per FMA); used as the compute-pipe roofline denominators. */
 int ddx_probe_fma_peak(int device, double *fp32_tflops, double *fp64_tflops);
 
+/* Synchronises `stream` and reports whether a kernel of this context gave up a bounded
+ * device-side wait since the last call: DDX_ERR_TIMEOUT if so (the tracers of the
+ * blocks concerned were left unchanged), DDX_OK otherwise.  Clears the report.  No
+ * counterpart in the reference, whose kernels have no waits. */
+int ddx_sync_status(ddx_ctx *ctx, void *stream);
+
+/* Failure-detection test hook (no counterpart in the reference).  The next mixed-precision
+ * dust launch of this context leaves the TMA copy of source tile `tile` (counted over the
+ * four stages) unissued and bounds its waits by wait_ns instead of 2 s, so the blocks
+ * give up, report DDX_ERR_TIMEOUT through ddx_sync_status and leave their tracers
+ * unchanged.  Nothing faults or hangs; the context stays usable. */
+int ddx_debug_lose_tile_copy(ddx_ctx *ctx, int tile, unsigned long long wait_ns);
+
 /* Error string for a status code. */
 const char *ddx_status_string(int status);
 

@@ -170,6 +170,29 @@ def test_star_only_fixed_mode_moves_star_ballistically(engine):
     assert rel_err(g, o).max() < 1e-13
 
 
+def test_lost_tile_copy_reports_timeout_and_context_recovers(engine):
+    """Failure detection without a fault: one TMA tile copy is left unissued, the bounded
+    mbarrier waits (20 ms here) run out, every block reports through the status word and
+    leaves its tracers untouched, and the next step on the same context is normal."""
+    s = small_ring(n_dust=2048, n_plsml=1100)          # 552 pair records: 2 tiles per stage
+    engine.set_size_table(**s.size_table)
+    phys = make_phys(**s.phys)
+    st = DeviceState.from_numpy(s.state)
+    assert engine.sync_status() == 0
+    abi.check(engine.lib.ddx_debug_lose_tile_copy(engine.ctx, 1, 20_000_000), "inject")
+    engine.step(st, s.n_grav, s.dt, phys, abi.DDX_PREC_MIXED)
+    assert engine.sync_status() == 6
+    after = st.to_numpy()
+    ng = s.n_grav
+    for f in FIELDS + ("N",):
+        np.testing.assert_array_equal(after[f][ng:], s.state[f][ng:])
+    assert engine.sync_status() == 0                    # the report was cleared
+    engine.step(st, s.n_grav, s.dt, phys, abi.DDX_PREC_MIXED)
+    assert engine.sync_status() == 0
+    moved = st.to_numpy()
+    assert np.all(moved["x"][ng:] != after["x"][ng:])
+
+
 def test_zero_dust_and_bad_arguments(engine):
     s = synth.solar_like(n_dust=0)
     g = run_gpu(engine, s, 2)
