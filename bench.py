@@ -38,7 +38,7 @@ FLOP_STAR = 45
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n-dust", type=int, default=1048576)
@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", choices=["dusty_ring", "imaging"], default="dusty_ring")
     return p.parse_args()
 
 
@@ -65,7 +66,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", self.index, f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -372,9 +373,66 @@ def run_reference(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_imaging(args, world, rank, local):
+    """Images (10 wavelengths, 1024x1024) and the 200-point SED of 4,194,304 tracers drawn
+    from the solar-like dust distribution: particle-wavelengths/s and HBM GB/s."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_view
+
+    torch.cuda.set_device(local)
+    n = args.n_dust if args.n_dust != 1048576 else 4194304
+    s = synth.imaging(n_dust=n, seed=synth.SEED + rank)
+    eng = Engine(local)
+    eng.set_size_table(**s.size_table)
+    o = s.optics
+    eng.set_optics(o["w"], o["in"], o["Qabs"], o["Qsca"], o["Qpfunc"], o["Td"], o["Rmin"], o["Rmax"])
+    st = DeviceState.from_numpy(s.state)
+    view = make_view(**s.view)
+    n_img = len(s.image_wj)
+    F = torch.empty((n_img, s.view["xsize"], s.view["ysize"]), dtype=torch.float64, device="cuda")
+    Fs = torch.empty(len(o["w"]), dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {}
+    for prec, name in ((abi.DDX_PREC_FP64, "fp64"),):
+        for _ in range(args.warmup):
+            eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=prec)
+            eng.sed(st, s.n_grav, view, out=Fs, precision=prec)
+        ti, ts = [], []
+        for _ in range(args.steps):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(stream)
+            eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=prec)
+            e[1].record(stream)
+            eng.sed(st, s.n_grav, view, out=Fs, precision=prec)
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            ti.append(e[0].elapsed_time(e[1]))
+            ts.append(e[1].elapsed_time(e[2]))
+        t_img = statistics.mean(ti) / 1e3
+        t_sed = statistics.mean(ts) / 1e3
+        npix = s.view["xsize"] * s.view["ysize"]
+        bytes_img = n * 36 + n_img * npix * 8
+        out[name] = {"image_ms": t_img * 1e3, "sed_ms": t_sed * 1e3,
+                     "image_particle_wavelengths_per_s": n * n_img / t_img,
+                     "sed_particle_wavelengths_per_s": n * len(o["w"]) / t_sed,
+                     "image_algorithmic_GBps": bytes_img / t_img / 1e9,
+                     "image_hbm_frac": bytes_img / t_img / 1e9 / measured_peaks().get("hbm_gbs", 6782.1)}
+    line = {"metric": "imaging particle-wavelengths/s", "workload": "imaging", "n_particles": n,
+            "n_img": n_img, "n_wav": len(o["w"]), "image": [s.view["xsize"], s.view["ysize"]],
+            "results": out, "l2": "flushed between timed calls"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
+    if args.workload == "imaging":
+        run_imaging(args, world, rank, local)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank, local)
     else:
