@@ -201,6 +201,25 @@ def run_ours(args, world, rank, local):
     units = allsum((ng + 0.5 * (alive0 + alive1)) * args.steps)
     value = units / t_total
 
+    # spatial-hash collision pass over the grains (the workload detects collisions every step)
+    h_coll = 0.1
+    for _ in range(2):
+        pairs = eng.collide(st, ng, ng + nd, h_coll)
+    torch.cuda.synchronize()
+    coll_ms = []
+    for _ in range(5):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        pairs = eng.collide(st, ng, ng + nd, h_coll)
+        coll_ms.append((time.perf_counter() - t1) * 1e3)
+    collide = {"h_AU": h_coll, "pairs": eng.last_pair_count, "ms_per_call": statistics.median(coll_ms),
+               "bodies_per_s": nd / (statistics.median(coll_ms) / 1e3),
+               "what": "ddx_collide over the grains: hash keys, radix sort, cell ranges, count, scan, "
+                       "write; host wall time, including the count read-back"}
+    step_plus_coll_ms = t_total * 1e3 / args.steps + collide["ms_per_call"]
+    collide["body_steps_per_s_with_collisions"] = (ng + alive1) / (step_plus_coll_ms / 1e3)
+
     # roofline of the dust kernel (FP32-pipe bound in the mixed path)
     fp32_peak, fp64_peak = probe_fma_peak(local)
     inter = 4.0 * 0.5 * (alive0 + alive1) * (ng - 1)
@@ -298,6 +317,7 @@ def run_ours(args, world, rank, local):
         "mixed_over_fp64": value / fp64["value"] if fp64 else None,
         "error_vs_fp64": err_short,
         "error_vs_fp64_long": err_long,
+        "collide": collide,
         "roofline": {"kernel": "dust_rk4_kernel<mixed>", "bound": "fp32_pipe", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "peak_source": "ddx_probe_fma_peak (FMA chains, measured in this run); "

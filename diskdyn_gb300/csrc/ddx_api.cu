@@ -29,6 +29,7 @@ struct ddx_ctx {
     int* status = nullptr;                      // kStatus* bits set by kernels (device)
     int inject_lose_tile = -1;                  // one-shot test hook for the next mixed dust launch
     unsigned long long inject_wait_ns = 0;
+    CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
 };
 
 namespace {
@@ -186,6 +187,7 @@ int ddx_destroy(ddx_ctx* c) {
     free_optics(c);
     cudaFree(c->bins); cudaFree(c->size_d); cudaFree(c->vc); cudaFree(c->od_dev);
     cudaFree(c->sed_partial); cudaFree(c->counters); cudaFree(c->status);
+    collide_free(c->collide);
     delete c;
     return DDX_OK;
 }
@@ -304,6 +306,16 @@ int ddx_small_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double
     if (r) return r;
     take_injection(c, a);
     return cuda_status(launch_dust(*s, a, c->ms, c->bins, precision, (cudaStream_t)stream));
+}
+
+int ddx_collide(ddx_ctx* c, const ddx_state* s, int i0, int i1, double h, int* pairs,
+                long long cap, long long* n_pairs, void* stream) {
+    if (!c || !state_ok(s) || !n_pairs || i0 < 0 || i1 < i0 || cap < 0 || (cap > 0 && !pairs) || !(h > 0.0))
+        return DDX_ERR_ARG;
+    if ((long long)i1 - i0 > (1LL << 30)) return DDX_ERR_RANGE;
+    cudaSetDevice(c->device);
+    return collide_run(c->collide, *s, i0, i1, h, reinterpret_cast<int2*>(pairs), cap, n_pairs,
+                       (cudaStream_t)stream);
 }
 
 int ddx_debug_lose_tile_copy(ddx_ctx* c, int tile, unsigned long long wait_ns) {

@@ -135,4 +135,9 @@ cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScra
                         const SizeBin* bins, int precision, cudaStream_t st);
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                               const SizeBin* bins, cudaStream_t st);
+
+struct CollideScratch;   // ddx_collide.cu
+int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double h, int2* pairs,
+                long long cap, long long* n_pairs, cudaStream_t st);
+void collide_free(CollideScratch*& cs);
 }  // namespace ddx

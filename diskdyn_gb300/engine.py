@@ -163,6 +163,23 @@ class Engine:
         abi.check(fn(self.ctx, C.byref(st._abi), n_grav, st.n_all - n_grav, float(dt), C.byref(phys),
                      precision, mode, C.c_void_p(_stream_handle(stream))), "ddx_" + which)
 
+    def collide(self, st: DeviceState, i0: int, i1: int, h: float, cap: int | None = None,
+                stream=None) -> torch.Tensor:
+        """Collision pairs (m, 2) int32 on the device, ordered by (i, j): live tracers
+        i < j of [i0, i1) with squared separation < h^2.  With cap=None the buffer is
+        sized from a first counting call."""
+        n = C.c_longlong(0)
+        sh = C.c_void_p(_stream_handle(stream))
+        if cap is None:
+            abi.check(self.lib.ddx_collide(self.ctx, C.byref(st._abi), i0, i1, float(h), None, 0,
+                                           C.byref(n), sh), "ddx_collide")
+            cap = n.value
+        out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=st.x.device)
+        abi.check(self.lib.ddx_collide(self.ctx, C.byref(st._abi), i0, i1, float(h),
+                                       C.c_void_p(out.data_ptr()), cap, C.byref(n), sh), "ddx_collide")
+        self.last_pair_count = n.value
+        return out[:min(cap, n.value)]
+
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
         bounded device-side wait since the last call, else 0."""

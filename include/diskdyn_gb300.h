@@ -171,6 +171,17 @@ int ddx_image(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
 int ddx_sed(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
             const ddx_view *view, double *Fsed, int precision, int mode, void *stream);
 
+/* Collision candidates through a spatial-hash grid built by radix sort (no counterpart
+ * in the reference, which has no collision detection).  Two live tracers (N != 0)
+ * i < j of the state range [i0, i1) collide when
+ *     (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2     (FP64, every operation rounded alone),
+ * which makes the list identical to a brute-force test with that expression.  Writes up
+ * to `cap` pairs (i, j) as int pairs[2k], pairs[2k+1] (device pointer), ordered by i then
+ * j, and the total number found to *n_pairs (host); when *n_pairs > cap the call can be
+ * repeated with a larger buffer.  Synchronises `stream`.  At most 2^30 tracers. */
+int ddx_collide(ddx_ctx *ctx, const ddx_state *s, int i0, int i1, double h, int *pairs,
+                long long cap, long long *n_pairs, void *stream);
+
 /* Diagnostics (no reference counterpart).  ddx_debug_pixels writes, for every dust
  * tracer, the pixel index ysize*x + y that ddx_image uses (or -1 for a tracer without
  * optical data or outside the image) to pix[n_dust], and 1/0 to exact[n_dust] when the

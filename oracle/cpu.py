@@ -155,3 +155,15 @@ def dust_temp(w, influx, Qabs, dist, Rmax_AU):
     lib().ora_dust_temp(n_grid, n_wav, _ptr(w), _ptr(influx), _ptr(Qabs), float(dist), C.byref(rmin),
                         C.byref(rmax), _ptr(Td))
     return Td, rmin.value, rmax.value
+
+
+def collide(arrays: dict, i0: int, i1: int, h: float, method: str = "brute", cap: int | None = None):
+    """Collision pairs (m, 2) of live tracers i < j in [i0, i1) closer than h, (i, j) order."""
+    st, os_ = host_state(arrays)
+    f = lib().ora_collide_brute if method == "brute" else lib().ora_collide_grid
+    f.restype = C.c_longlong
+    f.argtypes = [OState, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_longlong]
+    total = f(os_, i0, i1, float(h), None, 0)
+    out = np.zeros((max(total, 1), 2), np.int32)
+    f(os_, i0, i1, float(h), _ptr(out), total)
+    return out[:total]

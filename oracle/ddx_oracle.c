@@ -462,3 +462,132 @@ int ora_dust_temp(int n_grid, int n_wav, const double *w, const double *in, cons
     *Rmax_AU = Rmax / ORA_AU;
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------
+ * Collision pairs (no reference counterpart; the criterion is the one documented for
+ * ddx_collide): live tracers i < j of [i0, i1) with
+ *   (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2, left to right, no contraction.
+ * ------------------------------------------------------------------------------------ */
+static int ora_close(const ora_state *s, int i, int j, double h2) {
+    double ex = s->x[j] - s->x[i], ey = s->y[j] - s->y[i], ez = s->z[j] - s->z[i];
+    double d2 = ex * ex + ey * ey + ez * ez;
+    return d2 < h2;
+}
+
+/* Brute force over all pairs.  Writes up to cap pairs (i, j) to out[2k], out[2k+1] in (i, j)
+ * order; returns the total number found. */
+long long ora_collide_brute(ora_state s, int i0, int i1, double h, int *out, long long cap) {
+    double h2 = h * h;
+    int n = i1 - i0;
+    long long *cnt = (long long *)calloc((size_t)(n > 0 ? n : 1), sizeof(long long));
+    int a;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (a = 0; a < n; ++a) {
+        int i = i0 + a;
+        if (s.N[i] == 0) continue;
+        long long c = 0;
+        for (int j = i + 1; j < i1; ++j)
+            if (s.N[j] != 0 && ora_close(&s, i, j, h2)) ++c;
+        cnt[a] = c;
+    }
+    long long tot = 0;
+    for (a = 0; a < n; ++a) { long long c = cnt[a]; cnt[a] = tot; tot += c; }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (a = 0; a < n; ++a) {
+        int i = i0 + a;
+        if (s.N[i] == 0) continue;
+        long long k = cnt[a];
+        for (int j = i + 1; j < i1; ++j)
+            if (s.N[j] != 0 && ora_close(&s, i, j, h2)) {
+                if (k < cap) { out[2 * k] = i; out[2 * k + 1] = j; }
+                ++k;
+            }
+    }
+    free(cnt);
+    return tot;
+}
+
+/* The same pairs through a cell list (cell side h(1+1e-9), coordinates clamped to
+ * +-(2^20-2)), for sizes where the brute force is too slow. */
+typedef struct { long long id; int i; } ora_cell;
+static int ora_cell_cmp(const void *a, const void *b) {
+    const ora_cell *x = (const ora_cell *)a, *y = (const ora_cell *)b;
+    if (x->id != y->id) return x->id < y->id ? -1 : 1;
+    return (x->i > y->i) - (x->i < y->i);
+}
+static long long ora_cc(double x, double inv) {
+    double c = floor(x * inv), lim = (double)((1LL << 20) - 2);
+    if (c < -lim) c = -lim;
+    if (c > lim) c = lim;
+    return (long long)c;
+}
+static long long ora_pack(long long cx, long long cy, long long cz) {
+    long long o = 1LL << 20;
+    return ((cx + o) << 42) | ((cy + o) << 21) | (cz + o);
+}
+static int ora_int_cmp(const void *a, const void *b) {
+    int x = *(const int *)a, y = *(const int *)b;
+    return (x > y) - (x < y);
+}
+
+long long ora_collide_grid(ora_state s, int i0, int i1, double h, int *out, long long cap) {
+    int n = i1 - i0;
+    if (n <= 1) return 0;
+    double inv = 1.0 / (h * (1.0 + 1e-9)), h2 = h * h;
+    ora_cell *cells = (ora_cell *)malloc(sizeof(ora_cell) * (size_t)n);
+    long long *own = (long long *)malloc(sizeof(long long) * (size_t)n);
+    int m = 0;
+    for (int a = 0; a < n; ++a) {
+        int i = i0 + a;
+        own[a] = -1;
+        if (s.N[i] == 0) continue;
+        own[a] = ora_pack(ora_cc(s.x[i], inv), ora_cc(s.y[i], inv), ora_cc(s.z[i], inv));
+        cells[m].id = own[a];
+        cells[m].i = i;
+        ++m;
+    }
+    qsort(cells, (size_t)m, sizeof(ora_cell), ora_cell_cmp);
+    long long *cnt = (long long *)calloc((size_t)n + 1, sizeof(long long));
+    for (int pass = 0; pass < 2; ++pass) {
+        int a;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (a = 0; a < n; ++a) {
+            if (own[a] < 0) continue;
+            int i = i0 + a;
+            long long o = 1LL << 20, id = own[a];
+            long long cx = ((id >> 42) & 0x1FFFFF) - o, cy = ((id >> 21) & 0x1FFFFF) - o, cz = (id & 0x1FFFFF) - o;
+            long long k = pass ? cnt[a] : 0, k0 = k;
+            for (int dx = -1; dx <= 1; ++dx)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dz = -1; dz <= 1; ++dz) {
+                        long long nid = ora_pack(cx + dx, cy + dy, cz + dz);
+                        int lo = 0, hi = m;           /* first entry with id >= nid */
+                        while (lo < hi) { int mid = (lo + hi) / 2; if (cells[mid].id < nid) lo = mid + 1; else hi = mid; }
+                        for (int r = lo; r < m && cells[r].id == nid; ++r) {
+                            int j = cells[r].i;
+                            if (j <= i || !ora_close(&s, i, j, h2)) continue;
+                            if (pass && k < cap) { out[2 * k] = i; out[2 * k + 1] = j; }
+                            ++k;
+                        }
+                    }
+            if (!pass) cnt[a] = k;
+            else if (k0 < cap) {
+                long long e = k < cap ? k : cap;
+                /* sort this tracer's partners by j */
+                int *tmp = (int *)malloc(sizeof(int) * (size_t)(e - k0 > 0 ? e - k0 : 1));
+                for (long long q = k0; q < e; ++q) tmp[q - k0] = out[2 * q + 1];
+                qsort(tmp, (size_t)(e - k0), sizeof(int), ora_int_cmp);
+                for (long long q = k0; q < e; ++q) out[2 * q + 1] = tmp[q - k0];
+                free(tmp);
+            }
+        }
+        if (!pass) {
+            long long tot = 0;
+            for (int b = 0; b < n; ++b) { long long c = cnt[b]; cnt[b] = tot; tot += c; }
+            cnt[n] = tot;
+        }
+    }
+    long long tot = cnt[n];
+    free(cnt); free(own); free(cells);
+    return tot;
+}
