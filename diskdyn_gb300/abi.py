@@ -76,6 +76,10 @@ SIGNATURES = [
                           C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("ddx_collide", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double, C.c_void_p,
                               C.c_longlong, C.POINTER(C.c_longlong), C.c_void_p]),
+    ("ddx_adjoint_forward", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double, C.c_int,
+                                      C.c_int, C.POINTER(Phys), C.POINTER(View), C.c_void_p, C.c_int,
+                                      C.c_void_p, C.c_void_p]),
+    ("ddx_adjoint_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddx_debug_pixels", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.POINTER(View),
                                    C.c_void_p, C.c_void_p]),
     ("ddx_debug_exact_pixel_count", C.c_ulonglong, [C.c_void_p]),

@@ -1,0 +1,756 @@
+// Discrete adjoint of the RK4 trajectory and of a differentiable image, in FP64.
+// No counterpart in the reference.
+//
+// Model (the forward these kernels differentiate exactly):
+//  - massive set (n_grav <= DDX_ADJ_MAX_GRAV bodies, star at 0): the reference's RK4 with
+//    all-pairs gravity (src/gpu_functions.cu:71-625), integrated first for every step by
+//    one single-warp kernel that keeps the stage positions P_s(n) of every step;
+//  - dust tracers: the reference's RK4 (src/gpu_functions.cu:627-943) under the star term
+//    (gravity reduced by beta + beta_sw, PR + stellar-wind drag; no Lorentz force) and the
+//    gravity of the massive bodies at their stage positions.  Tracers are independent
+//    given P_s(n), so each thread integrates its tracer over all steps in one launch;
+//  - image: the flux of src/gpu_functions.cu:1049-1078 deposited with bilinear weights
+//    on the four pixel centres around the projected position, so the image, and the L2
+//    loss on it, are continuous and piecewise differentiable in every position (the
+//    reference's nearest-pixel binning has a zero gradient almost everywhere).
+//
+// Backward (checkpoint-and-recompute every K steps):
+//  1. image adjoint: dL/dimage -> adjoint of the final tracer positions;
+//  2. per segment, last first: recompute the K steps from the checkpoint, storing each
+//     step's state and stage accelerations a1..a3 (15 doubles per tracer per step);
+//     reverse sweep of the four RK4 stages per tracer with analytic vector-Jacobian
+//     products of the star term and the body gravity; the adjoints of the bodies' stage
+//     positions and masses are reduced per block in a fixed order (warp shuffles, then
+//     shared memory, then block partials summed in block order), so the gradient is
+//     deterministic; a single-warp kernel then runs the reverse sweep of the massive set.
+// Tracers removed during the forward (N = 0) or without optical data emit nothing, so
+// their adjoint is zero and they are skipped.
+#include "ddx_internal.cuh"
+#include "ddx_flux.cuh"
+
+namespace ddx {
+namespace {
+
+constexpr int kMaxGrav = DDX_ADJ_MAX_GRAV;
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr int kSegComp = 15;   // per tracer per step: x, y, z, vx, vy, vz, a1, a2, a3
+
+struct AdjArgs {
+    int ng, nd;
+    double dt;
+    StepArgs sa;            // star-term constants (FLQ = 0)
+    const Body* Ps;         // [n_steps][4][ng]
+    const SizeBin* bins;
+    const int* id;          // [nd]
+};
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Acceleration of a tracer at (x, r) for the stage whose body records are P[0..ng).
+__device__ __forceinline__ bool tracer_accel(const AdjArgs& A, const Body* P, double x, double y, double z,
+                                             double rx, double ry, double rz, float bet, float betsw,
+                                             double& ax, double& ay, double& az) {
+    if (!star_term(x - P[0].x, y - P[0].y, z - P[0].z, rx, ry, rz, P[0].m, bet, betsw, 0.f, 1.0, A.sa, ax,
+                   ay, az))
+        return false;
+    for (int j = 1; j < A.ng; ++j) {
+        const double dx = P[j].x - x, dy = P[j].y - y, dz = P[j].z - z;
+        const double RR = dx * dx + dy * dy + dz * dz;
+        if (RR == 0.0) return false;
+        const double f = P[j].m / (RR * sqrt(RR));
+        ax += f * dx; ay += f * dy; az += f * dz;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------
+// Massive set: forward trajectory and reverse sweep (one warp, one body per lane)
+// ---------------------------------------------------------------------------------------
+
+__device__ __forceinline__ void massive_acc(const double (*sp)[4], int ng, int j, double& ax, double& ay,
+                                            double& az) {
+    ax = ay = az = 0.0;
+    for (int k = 0; k < ng; ++k) {
+        if (k == j) continue;
+        const double dx = sp[k][0] - sp[j][0], dy = sp[k][1] - sp[j][1], dz = sp[k][2] - sp[j][2];
+        const double RR = dx * dx + dy * dy + dz * dz;
+        if (RR > 0.0) {
+            const double f = sp[k][3] / (RR * sqrt(RR));
+            ax += f * dx; ay += f * dy; az += f * dz;
+        }
+    }
+}
+
+__global__ void massive_traj_kernel(int ng, int n_steps, double dt, double* xv, Body* Ps) {
+    __shared__ double sp[kMaxGrav][4];
+    const int j = threadIdx.x;
+    const bool on = j < ng;
+    double x = 0, y = 0, z = 0, vx = 0, vy = 0, vz = 0, m = 0;
+    if (on) {
+        x = xv[0 * ng + j]; y = xv[1 * ng + j]; z = xv[2 * ng + j];
+        vx = xv[3 * ng + j]; vy = xv[4 * ng + j]; vz = xv[5 * ng + j]; m = xv[6 * ng + j];
+    }
+    const double h2 = dt * 0.5, d6 = dt / 6.0;
+    for (int n = 0; n < n_steps; ++n) {
+        double px[4], py[4], pz[4], ax[4], ay[4], az[4];
+        double r2x = 0, r2y = 0, r2z = 0, r3x = 0, r3y = 0, r3z = 0, r4x = 0, r4y = 0, r4z = 0;
+        for (int s = 0; s < 4; ++s) {
+            if (s == 0) { px[0] = x; py[0] = y; pz[0] = z; }
+            else if (s == 1) {
+                r2x = vx + ax[0] * h2; r2y = vy + ay[0] * h2; r2z = vz + az[0] * h2;
+                px[1] = x + vx * h2; py[1] = y + vy * h2; pz[1] = z + vz * h2;
+            } else if (s == 2) {
+                r3x = vx + ax[1] * h2; r3y = vy + ay[1] * h2; r3z = vz + az[1] * h2;
+                px[2] = x + r2x * h2; py[2] = y + r2y * h2; pz[2] = z + r2z * h2;
+            } else {
+                r4x = vx + ax[2] * dt; r4y = vy + ay[2] * dt; r4z = vz + az[2] * dt;
+                px[3] = x + r3x * dt; py[3] = y + r3y * dt; pz[3] = z + r3z * dt;
+            }
+            __syncwarp();
+            if (on) { sp[j][0] = px[s]; sp[j][1] = py[s]; sp[j][2] = pz[s]; sp[j][3] = m; }
+            __syncwarp();
+            if (on) {
+                massive_acc(sp, ng, j, ax[s], ay[s], az[s]);
+                Ps[((size_t)n * 4 + s) * ng + j] = make_body(px[s], py[s], pz[s], m);
+            }
+        }
+        x += d6 * (vx + 2.0 * r2x + 2.0 * r3x + r4x);
+        y += d6 * (vy + 2.0 * r2y + 2.0 * r3y + r4y);
+        z += d6 * (vz + 2.0 * r2z + 2.0 * r3z + r4z);
+        vx += d6 * (ax[0] + 2.0 * ax[1] + 2.0 * ax[2] + ax[3]);
+        vy += d6 * (ay[0] + 2.0 * ay[1] + 2.0 * ay[2] + ay[3]);
+        vz += d6 * (az[0] + 2.0 * az[1] + 2.0 * az[2] + az[3]);
+    }
+    if (on) {
+        xv[0 * ng + j] = x; xv[1 * ng + j] = y; xv[2 * ng + j] = z;
+        xv[3 * ng + j] = vx; xv[4 * ng + j] = vy; xv[5 * ng + j] = vz;
+    }
+}
+
+// Vector-Jacobian product of the all-pairs accelerations at one stage for body j:
+// out_j = sum_k J_jk (m_j g_k - m_k g_j), J(d) v = v/r^3 - 3 (d.v) d/r^5, and the mass
+// adjoint sum_k g_k.(P_j - P_k)/r^3.
+__device__ __forceinline__ void massive_vjp(const double (*sp)[4], const double (*sg)[3], int ng, int j,
+                                            double& ox, double& oy, double& oz, double& om) {
+    ox = oy = oz = om = 0.0;
+    const double mj = sp[j][3];
+    for (int k = 0; k < ng; ++k) {
+        if (k == j) continue;
+        const double dx = sp[j][0] - sp[k][0], dy = sp[j][1] - sp[k][1], dz = sp[j][2] - sp[k][2];
+        const double RR = dx * dx + dy * dy + dz * dz;
+        if (!(RR > 0.0)) continue;
+        const double ri3 = 1.0 / (RR * sqrt(RR)), ri5 = ri3 / RR;
+        const double vx = mj * sg[k][0] - sp[k][3] * sg[j][0];
+        const double vy = mj * sg[k][1] - sp[k][3] * sg[j][1];
+        const double vz = mj * sg[k][2] - sp[k][3] * sg[j][2];
+        const double dv = dx * vx + dy * vy + dz * vz;
+        ox += vx * ri3 - 3.0 * dv * dx * ri5;
+        oy += vy * ri3 - 3.0 * dv * dy * ri5;
+        oz += vz * ri3 - 3.0 * dv * dz * ri5;
+        om += (sg[k][0] * dx + sg[k][1] * dy + sg[k][2] * dz) * ri3;
+    }
+}
+
+__global__ void massive_reverse_kernel(int ng, double dt, const Body* Ps, const double* mu, int n0, int n1,
+                                       double* lam, double* lam_m) {
+    __shared__ double sp[kMaxGrav][4];
+    __shared__ double sg[kMaxGrav][3];
+    const int j = threadIdx.x;
+    const bool on = j < ng;
+    double lx[3] = {0, 0, 0}, lv[3] = {0, 0, 0}, lm = 0.0;
+    if (on) {
+        for (int c = 0; c < 3; ++c) { lx[c] = lam[c * ng + j]; lv[c] = lam[(3 + c) * ng + j]; }
+        lm = lam_m[j];
+    }
+    const double h2 = dt * 0.5, d6 = dt / 6.0;
+    for (int n = n1 - 1; n >= n0; --n) {
+        const int k = n - n0;
+        double Lx[3], Lv[3], Lr2[3], Lr3[3], Lr4[3], La[4][3], LP[3] = {0, 0, 0};
+        for (int c = 0; c < 3; ++c) {
+            Lx[c] = lx[c];
+            Lv[c] = lv[c] + d6 * lx[c];
+            Lr2[c] = Lr3[c] = 2.0 * d6 * lx[c];
+            Lr4[c] = d6 * lx[c];
+            La[0][c] = d6 * lv[c];
+            La[1][c] = La[2][c] = 2.0 * d6 * lv[c];
+            La[3][c] = d6 * lv[c];
+        }
+        for (int s = 3; s >= 0; --s) {
+            __syncwarp();
+            if (on) {
+                const Body b = Ps[((size_t)n * 4 + s) * ng + j];
+                sp[j][0] = b.x; sp[j][1] = b.y; sp[j][2] = b.z; sp[j][3] = b.m;
+                for (int c = 0; c < 3; ++c) sg[j][c] = La[s][c];
+            }
+            __syncwarp();
+            double ox = 0, oy = 0, oz = 0, om = 0;
+            if (on) {
+                massive_vjp(sp, sg, ng, j, ox, oy, oz, om);
+                const double* m4 = mu + (((size_t)k * 4 + s) * ng + j) * 4;
+                LP[0] = ox + m4[0]; LP[1] = oy + m4[1]; LP[2] = oz + m4[2];
+                lm += om + m4[3];
+            }
+            for (int c = 0; c < 3; ++c) {
+                Lx[c] += LP[c];
+                if (s == 3) { Lr3[c] += dt * LP[c]; Lv[c] += Lr4[c]; La[2][c] += dt * Lr4[c]; }
+                else if (s == 2) { Lr2[c] += h2 * LP[c]; Lv[c] += Lr3[c]; La[1][c] += h2 * Lr3[c]; }
+                else if (s == 1) { Lv[c] += h2 * LP[c]; Lv[c] += Lr2[c]; La[0][c] += h2 * Lr2[c]; }
+            }
+        }
+        for (int c = 0; c < 3; ++c) { lx[c] = Lx[c]; lv[c] = Lv[c]; }
+    }
+    if (on) {
+        for (int c = 0; c < 3; ++c) { lam[c * ng + j] = lx[c]; lam[(3 + c) * ng + j] = lv[c]; }
+        lam_m[j] = lm;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Dust: forward (with checkpoints or with per-step storage) and reverse sweep
+// ---------------------------------------------------------------------------------------
+
+// Integrates every tracer over steps [n0, n1).  ck (optional): the state at every step
+// that is a multiple of K (checkpoint c at ck + c*6*nd), including n1 when it is one.
+// seg (optional): per step, the state and the stage accelerations a1..a3.
+__global__ void __launch_bounds__(kThreads)
+dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, double* ck, double* seg) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= A.nd) return;
+    const size_t nd = A.nd;
+    double x = y[0 * nd + i], yy = y[1 * nd + i], z = y[2 * nd + i];
+    double vx = y[3 * nd + i], vy = y[4 * nd + i], vz = y[5 * nd + i];
+    bool alive = N[i] != 0.0;
+    float bet = 0.f, betsw = 0.f;
+    const int id = A.id[i];
+    if (id >= 0) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
+    const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
+    for (int n = n0; n < n1; ++n) {
+        if (ck && n % K == 0) {
+            double* c = ck + (size_t)(n / K) * 6 * nd;
+            c[0 * nd + i] = x; c[1 * nd + i] = yy; c[2 * nd + i] = z;
+            c[3 * nd + i] = vx; c[4 * nd + i] = vy; c[5 * nd + i] = vz;
+        }
+        double a1x = 0, a1y = 0, a1z = 0, a2x = 0, a2y = 0, a2z = 0, a3x = 0, a3y = 0, a3z = 0;
+        if (alive) {
+            const Body* P = A.Ps + (size_t)n * 4 * A.ng;
+            double a4x = 0, a4y = 0, a4z = 0;
+            bool ok = tracer_accel(A, P, x, yy, z, vx, vy, vz, bet, betsw, a1x, a1y, a1z);
+            const double r2x = vx + a1x * h2, r2y = vy + a1y * h2, r2z = vz + a1z * h2;
+            ok = ok && tracer_accel(A, P + A.ng, x + vx * h2, yy + vy * h2, z + vz * h2, r2x, r2y, r2z, bet,
+                                    betsw, a2x, a2y, a2z);
+            const double r3x = vx + a2x * h2, r3y = vy + a2y * h2, r3z = vz + a2z * h2;
+            ok = ok && tracer_accel(A, P + 2 * A.ng, x + r2x * h2, yy + r2y * h2, z + r2z * h2, r3x, r3y, r3z,
+                                    bet, betsw, a3x, a3y, a3z);
+            const double r4x = vx + a3x * dt, r4y = vy + a3y * dt, r4z = vz + a3z * dt;
+            ok = ok && tracer_accel(A, P + 3 * A.ng, x + r3x * dt, yy + r3y * dt, z + r3z * dt, r4x, r4y, r4z,
+                                    bet, betsw, a4x, a4y, a4z);
+            if (seg) {
+                double* S = seg + (size_t)(n - n0) * kSegComp * nd;
+                const double v[kSegComp] = {x, yy, z, vx, vy, vz, a1x, a1y, a1z, a2x, a2y, a2z, a3x, a3y, a3z};
+                for (int c = 0; c < kSegComp; ++c) S[c * nd + i] = v[c];
+            }
+            if (!ok) {
+                alive = false;   // removed: keeps its last state, emits nothing
+            } else {
+                x += d6 * (vx + 2.0 * (r2x + r3x) + r4x);
+                yy += d6 * (vy + 2.0 * (r2y + r3y) + r4y);
+                z += d6 * (vz + 2.0 * (r2z + r3z) + r4z);
+                vx += d6 * (a1x + 2.0 * (a2x + a3x) + a4x);
+                vy += d6 * (a1y + 2.0 * (a2y + a3y) + a4y);
+                vz += d6 * (a1z + 2.0 * (a2z + a3z) + a4z);
+            }
+        }
+    }
+    if (ck && n1 % K == 0) {
+        double* c = ck + (size_t)(n1 / K) * 6 * nd;
+        c[0 * nd + i] = x; c[1 * nd + i] = yy; c[2 * nd + i] = z;
+        c[3 * nd + i] = vx; c[4 * nd + i] = vy; c[5 * nd + i] = vz;
+    }
+    y[0 * nd + i] = x; y[1 * nd + i] = yy; y[2 * nd + i] = z;
+    y[3 * nd + i] = vx; y[4 * nd + i] = vy; y[5 * nd + i] = vz;
+    if (!alive) N[i] = 0.0;
+}
+
+// VJP of the tracer acceleration at one stage with adjoint g: adds to (Lx, Lr) and
+// deposits, per source j, the adjoints of its stage position and mass into wp[j][0..3]
+// (warp-reduced, lane 0 writes).  Called by every lane of the warp.
+__device__ __forceinline__ void tracer_vjp(const AdjArgs& A, const Body* P, bool on, const double* pos,
+                                           const double* r, float bet, float betsw, const double* g,
+                                           double* Lx, double* Lr, double (*wp)[4], int lane) {
+    double s4[4] = {0, 0, 0, 0};
+    if (on) {
+        const double dx = pos[0] - P[0].x, dy = pos[1] - P[0].y, dz = pos[2] - P[0].z;
+        const double RR = dx * dx + dy * dy + dz * dz;
+        const double R = sqrt(RR), R3 = RR * R, R5 = R3 * RR;
+        const double m0 = P[0].m;
+        const double g0 = (1.0 - bet - betsw) * m0;
+        const double Fg = g0 / R3;
+        const double c1 = (A.sa.SWQ == 1) ? m0 * (bet / kLightAU + betsw / A.sa.vswAU) : bet * m0 / kLightAU;
+        const double Fb1 = c1 / RR;
+        const double dr = dx * r[0] + dy * r[1] + dz * r[2];
+        const double Fb2 = dr / RR;
+        const double gd = g[0] * dx + g[1] * dy + g[2] * dz;
+        const double gr = g[0] * r[0] + g[1] * r[1] + g[2] * r[2];
+        const double gD = Fb2 * gd + gr;
+        // a = -Fg d - Fb1 (Fb2 d + r): g^T da/dd = cg g + cd d + cr r ; g^T da/dr = cr d - Fb1 g
+        const double cg = -Fg - Fb1 * Fb2;
+        const double cd = 3.0 * g0 * gd / R5 + 2.0 * c1 * gD / (RR * RR) + 2.0 * Fb1 * gd * dr / (RR * RR);
+        const double cr = -Fb1 * gd / RR;
+        const double d[3] = {dx, dy, dz};
+        for (int c = 0; c < 3; ++c) {
+            const double ld = cg * g[c] + cd * d[c] + cr * r[c];
+            Lx[c] += ld;
+            Lr[c] += cr * d[c] - Fb1 * g[c];
+            s4[c] = -ld;
+        }
+        s4[3] = (-Fg * gd - Fb1 * gD) / m0;
+    }
+    for (int c = 0; c < 4; ++c) {
+        const double t = wsum(s4[c]);
+        if (lane == 0) wp[0][c] = t;
+    }
+    for (int j = 1; j < A.ng; ++j) {
+        double v4[4] = {0, 0, 0, 0};
+        if (on) {
+            const double dx = P[j].x - pos[0], dy = P[j].y - pos[1], dz = P[j].z - pos[2];
+            const double RR = dx * dx + dy * dy + dz * dz;
+            const double ri3 = 1.0 / (RR * sqrt(RR)), ri5 = ri3 / RR;
+            const double gd = g[0] * dx + g[1] * dy + g[2] * dz;
+            const double m = P[j].m;
+            v4[0] = m * (g[0] * ri3 - 3.0 * gd * dx * ri5);
+            v4[1] = m * (g[1] * ri3 - 3.0 * gd * dy * ri5);
+            v4[2] = m * (g[2] * ri3 - 3.0 * gd * dz * ri5);
+            v4[3] = gd * ri3;
+            Lx[0] -= v4[0]; Lx[1] -= v4[1]; Lx[2] -= v4[2];
+        }
+        for (int c = 0; c < 4; ++c) {
+            const double t = wsum(v4[c]);
+            if (lane == 0) wp[j][c] = t;
+        }
+    }
+}
+
+// Reverse sweep over steps [n0, n1) (descending) from the stored states and stage
+// accelerations.  lam [6][nd] holds the adjoint of the state after step n1-1 on entry
+// and of the state before step n0 on exit.  part[block][k][stage][j][4]: this block's
+// sum of the adjoints of the bodies' stage positions and masses.
+__global__ void __launch_bounds__(kThreads)
+dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, double* __restrict__ lam,
+                    const unsigned char* __restrict__ active, double* __restrict__ part) {
+    __shared__ double wpart[kWarps][4][kMaxGrav][4];
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t nd = A.nd;
+    const bool on = i < A.nd && active[i];
+    double lx[3] = {0, 0, 0}, lv[3] = {0, 0, 0};
+    float bet = 0.f, betsw = 0.f;
+    if (on) {
+        for (int c = 0; c < 3; ++c) { lx[c] = lam[c * nd + i]; lv[c] = lam[(3 + c) * nd + i]; }
+        const int id = A.id[i];
+        if (id >= 0) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
+    }
+    const int Kseg = n1 - n0;
+    const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
+    for (int n = n1 - 1; n >= n0; --n) {
+        const int k = n - n0;
+        double st[kSegComp];
+        for (int c = 0; c < kSegComp; ++c) st[c] = on ? seg[((size_t)k * kSegComp + c) * nd + i] : 0.0;
+        const double* x = st;
+        const double* v = st + 3;
+        const double* a1 = st + 6;
+        const double* a2 = st + 9;
+        const double* a3 = st + 12;
+        double x2[3], r2[3], x3[3], r3[3], x4[3], r4[3];
+        for (int c = 0; c < 3; ++c) {
+            x2[c] = x[c] + v[c] * h2; r2[c] = v[c] + a1[c] * h2;
+            x3[c] = x[c] + r2[c] * h2; r3[c] = v[c] + a2[c] * h2;
+            x4[c] = x[c] + r3[c] * dt; r4[c] = v[c] + a3[c] * dt;
+        }
+        double Lx[3], Lv[3], Lr2[3], Lr3[3], Lr4[3], La1[3], La2[3], La3[3], La4[3];
+        for (int c = 0; c < 3; ++c) {
+            Lx[c] = lx[c];
+            Lv[c] = lv[c] + d6 * lx[c];
+            Lr2[c] = Lr3[c] = 2.0 * d6 * lx[c];
+            Lr4[c] = d6 * lx[c];
+            La1[c] = d6 * lv[c];
+            La2[c] = La3[c] = 2.0 * d6 * lv[c];
+            La4[c] = d6 * lv[c];
+        }
+        const Body* P = A.Ps + (size_t)n * 4 * A.ng;
+        double Ls[3], Lq[3];
+        // stage 4: a4 = a(x4, r4); x4 = x + r3 dt; r4 = v + a3 dt
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, P + 3 * A.ng, on, x4, r4, bet, betsw, La4, Ls, Lq, wpart[warp][3], lane);
+        for (int c = 0; c < 3; ++c) {
+            Lr4[c] += Lq[c];
+            Lx[c] += Ls[c]; Lr3[c] += dt * Ls[c];
+            Lv[c] += Lr4[c]; La3[c] += dt * Lr4[c];
+        }
+        // stage 3: a3 = a(x3, r3); x3 = x + r2 h2; r3 = v + a2 h2
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, P + 2 * A.ng, on, x3, r3, bet, betsw, La3, Ls, Lq, wpart[warp][2], lane);
+        for (int c = 0; c < 3; ++c) {
+            Lr3[c] += Lq[c];
+            Lx[c] += Ls[c]; Lr2[c] += h2 * Ls[c];
+            Lv[c] += Lr3[c]; La2[c] += h2 * Lr3[c];
+        }
+        // stage 2: a2 = a(x2, r2); x2 = x + v h2; r2 = v + a1 h2
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, P + A.ng, on, x2, r2, bet, betsw, La2, Ls, Lq, wpart[warp][1], lane);
+        for (int c = 0; c < 3; ++c) {
+            Lr2[c] += Lq[c];
+            Lx[c] += Ls[c]; Lv[c] += h2 * Ls[c];
+            Lv[c] += Lr2[c]; La1[c] += h2 * Lr2[c];
+        }
+        // stage 1: a1 = a(x, v)
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, P, on, x, v, bet, betsw, La1, Ls, Lq, wpart[warp][0], lane);
+        for (int c = 0; c < 3; ++c) {
+            Lx[c] += Ls[c]; Lv[c] += Lq[c];
+            lx[c] = Lx[c]; lv[c] = Lv[c];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < 4 * A.ng * 4; e += kThreads) {
+            const int s = e / (A.ng * 4), j = (e / 4) % A.ng, c = e % 4;
+            double t = 0.0;
+            for (int w = 0; w < kWarps; ++w) t += wpart[w][s][j][c];
+            part[((((size_t)blockIdx.x * Kseg + k) * 4 + s) * A.ng + j) * 4 + c] = t;
+        }
+        __syncthreads();
+    }
+    if (on)
+        for (int c = 0; c < 3; ++c) { lam[c * nd + i] = lx[c]; lam[(3 + c) * nd + i] = lv[c]; }
+}
+
+// mu[k][s][j][c] = sum over blocks of part[b][k][s][j][c], in block order.
+__global__ void reduce_parts_kernel(const double* __restrict__ part, int nblk, int per_block, double* __restrict__ mu) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= per_block) return;
+    double t = 0.0;
+    for (int b = 0; b < nblk; ++b) t += part[(size_t)b * per_block + e];
+    mu[e] = t;
+}
+
+// ---------------------------------------------------------------------------------------
+// Differentiable image: bilinear deposition of the flux, and its adjoint
+// ---------------------------------------------------------------------------------------
+
+struct TracerFlux {
+    double R, cossc, dcos[3];   // gradient of cossc with respect to (x, y, z)
+    bool clamped;
+    double u, w, du[3], dw[3];  // continuous pixel coordinates (pixel centres at integers)
+    double T, dTdR;
+};
+
+__device__ __forceinline__ void tracer_geometry(double x, double y, double z, int id, const ViewConst& v,
+                                                const OpticsDev& o, TracerFlux& g) {
+    const double R = sqrt(x * x + y * y + z * z);
+    g.R = R;
+    const double x1 = x * v.cr - y * v.sr, y1 = x * v.sr + y * v.cr;
+    // scattering-angle cosine (src/gpu_functions.cu:1017-1023) and its gradient
+    const double qx = -x1, qy = v.ly0 - y1, qz = v.lz0 - z;
+    const double L = sqrt(qx * qx + qy * qy + qz * qz);
+    const double num = x1 * x1 + y1 * y1 + z * z - y1 * v.ly0 - z * v.lz0;
+    double c = num / (R * L);
+    g.clamped = false;
+    if (c < -1) { c = -1.0; g.clamped = true; }
+    if (c >= 1.0 - 2.0 / v.ntheta) { c = 1.0 - 2.0 / v.ntheta; g.clamped = true; }
+    g.cossc = c;
+    const double p[3] = {x1, y1, z}, l0[3] = {0.0, v.ly0, v.lz0}, q[3] = {qx, qy, qz};
+    double dp[3];
+    for (int k = 0; k < 3; ++k)
+        dp[k] = g.clamped ? 0.0 : (2.0 * p[k] - l0[k]) / (R * L) - c * (p[k] / (R * R) - q[k] / (L * L));
+    g.dcos[0] = dp[0] * v.cr + dp[1] * v.sr;
+    g.dcos[1] = -dp[0] * v.sr + dp[1] * v.cr;
+    g.dcos[2] = dp[2];
+    // projected coordinates
+    const double y2 = y1 * v.ci + z * v.si;
+    const double X = x1 * v.cp - y2 * v.sp, Y = x1 * v.sp + y2 * v.cp;
+    g.u = X / v.psca + 0.5 * v.xsize - 0.5;
+    g.w = Y / v.psca + 0.5 * v.ysize - 0.5;
+    const double dXdx1 = v.cp, dXdy1 = -v.sp * v.ci, dXdz = -v.sp * v.si;
+    const double dYdx1 = v.sp, dYdy1 = v.cp * v.ci, dYdz = v.cp * v.si;
+    g.du[0] = (dXdx1 * v.cr + dXdy1 * v.sr) / v.psca;
+    g.du[1] = (-dXdx1 * v.sr + dXdy1 * v.cr) / v.psca;
+    g.du[2] = dXdz / v.psca;
+    g.dw[0] = (dYdx1 * v.cr + dYdy1 * v.sr) / v.psca;
+    g.dw[1] = (-dYdx1 * v.sr + dYdy1 * v.cr) / v.psca;
+    g.dw[2] = dYdz / v.psca;
+    // temperature (log-log in R on the nR grid) and its slope
+    const double* Td = o.Td + (size_t)id * kNR;
+    if (R <= o.Rmin) { g.T = Td[0]; g.dTdR = 0.0; }
+    else if (R >= o.Rmax) { g.T = Td[kNR - 1]; g.dTdR = 0.0; }
+    else {
+        const double* lT = o.lTd + (size_t)id * kNR;
+        const double lr = log(R / o.Rmin);
+        int k = (int)(lr / o.fR) + 1;
+        if (k > kNR - 1) k = kNR - 1;
+        const double frac = (lr - (k - 1) * o.fR) / o.fR;
+        g.T = exp(lT[k - 1] + (lT[k] - lT[k - 1]) * frac);
+        g.dTdR = g.T * (lT[k] - lT[k - 1]) / (o.fR * R);
+    }
+}
+
+// Flux at table wavelength wj with its derivatives in R and cossc.
+__device__ __forceinline__ void flux_grad(double n, int id, int wj, const TracerFlux& g, const OpticsDev& o,
+                                          const ViewConst& v, double& F, double& dFdR, double& dFdc) {
+    const double wvl = o.w[wj];
+    const double xq = kHplank * kCspeed / (wvl * kKboltz * g.T);
+    double I = 0.0, dIdT = 0.0;
+    if (xq < 700.0) {
+        const double ex = exp(xq);
+        I = (2 * kHplank * kCspeed * kCspeed) / (o.w5[wj] * (ex - 1.0)) * kPI;
+        dIdT = I * xq * ex / (ex - 1.0) / g.T;
+    }
+    const int nth = v.ntheta;
+    int cm = floor(0.5 * (g.cossc + 1.0) * (nth - 1));
+    const double cosm = (double)cm * 2.0 / (nth - 1) - 1.0, cosp = (double)(cm + 1) * 2.0 / (nth - 1) - 1.0;
+    const double wt = (g.cossc - cosm) / (cosp - cosm);
+    const int nw = o.n_wav;
+    const double lm = o.lQp[(size_t)nw * (o.n_theta * id + cm) + wj];
+    const double lp = o.lQp[(size_t)nw * (o.n_theta * id + cm + 1) + wj];
+    const double P = exp(lm + (lp - lm) * wt);
+    const double dPdc = P * (lp - lm) / (cosp - cosm);
+    const double s = o.size[id];
+    const double Ks = o.in[wj] * kPI * s * s * o.Qsca[(size_t)nw * id + wj] / (g.R * g.R) / kAU / kAU;
+    const double Fscat = Ks * P;
+    const double Kt = s * s * o.Qabs[(size_t)nw * id + wj] / v.dist / v.dist;
+    const double scale = n * 1e26 * wvl * wvl / kCspeed;
+    F = scale * (I * Kt + Fscat);
+    dFdR = scale * (dIdT * g.dTdR * Kt - 2.0 * Fscat / g.R);
+    dFdc = scale * Ks * dPdc;
+}
+
+__global__ void image_splat_kernel(const double* __restrict__ y, const double* __restrict__ N,
+                                   const int* __restrict__ idv, int nd, const ViewConst* __restrict__ vcp,
+                                   OpticsDev o, ImageList il, double* __restrict__ img) {
+    __shared__ ViewConst v;
+    if (threadIdx.x == 0) v = *vcp;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nd) return;
+    const int id = idv[i];
+    const double n = N[i];
+    if (id < 0 || n == 0.0) return;
+    TracerFlux g;
+    tracer_geometry(y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i], id, v, o, g);
+    if (!(g.R > o.Rmin)) return;
+    const int i0 = (int)floor(g.u), j0 = (int)floor(g.w);
+    const double fu = g.u - i0, fw = g.w - j0;
+    const size_t npix = (size_t)v.xsize * v.ysize;
+    for (int k = 0; k < il.n; ++k) {
+        double F, dFdR, dFdc;
+        flux_grad(n, id, il.wj[k], g, o, v, F, dFdR, dFdc);
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) {
+                const int px = i0 + a, py = j0 + b;
+                if (px < 0 || px >= v.xsize || py < 0 || py >= v.ysize) continue;
+                const double wgt = (a ? fu : 1.0 - fu) * (b ? fw : 1.0 - fw);
+                atomicAdd(&img[k * npix + (size_t)v.ysize * px + py], F * wgt);
+            }
+    }
+}
+
+__global__ void image_splat_adjoint_kernel(const double* __restrict__ y, const double* __restrict__ N,
+                                           const int* __restrict__ idv, int nd, const ViewConst* __restrict__ vcp,
+                                           OpticsDev o, ImageList il, const double* __restrict__ G,
+                                           double* __restrict__ lam, unsigned char* __restrict__ active) {
+    __shared__ ViewConst v;
+    if (threadIdx.x == 0) v = *vcp;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nd) return;
+    for (int c = 0; c < 6; ++c) lam[c * (size_t)nd + i] = 0.0;
+    active[i] = 0;
+    const int id = idv[i];
+    const double n = N[i];
+    if (id < 0 || n == 0.0) return;
+    TracerFlux g;
+    tracer_geometry(y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i], id, v, o, g);
+    if (!(g.R > o.Rmin)) return;
+    active[i] = 1;
+    const double pos[3] = {y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i]};
+    const int i0 = (int)floor(g.u), j0 = (int)floor(g.w);
+    const double fu = g.u - i0, fw = g.w - j0;
+    const size_t npix = (size_t)v.xsize * v.ysize;
+    double L[3] = {0, 0, 0};
+    for (int k = 0; k < il.n; ++k) {
+        double F, dFdR, dFdc;
+        flux_grad(n, id, il.wj[k], g, o, v, F, dFdR, dFdc);
+        double Gw = 0.0, Gu = 0.0, Gv = 0.0;   // sum G*w, sum G*dw/du, sum G*dw/dv
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) {
+                const int px = i0 + a, py = j0 + b;
+                if (px < 0 || px >= v.xsize || py < 0 || py >= v.ysize) continue;
+                const double gp = G[k * npix + (size_t)v.ysize * px + py];
+                const double wu = a ? fu : 1.0 - fu, wv = b ? fw : 1.0 - fw;
+                Gw += gp * wu * wv;
+                Gu += gp * (a ? 1.0 : -1.0) * wv;
+                Gv += gp * wu * (b ? 1.0 : -1.0);
+            }
+        for (int c = 0; c < 3; ++c) {
+            const double dF = dFdR * pos[c] / g.R + dFdc * g.dcos[c];
+            L[c] += Gw * dF + F * (Gu * g.du[c] + Gv * g.dw[c]);
+        }
+    }
+    for (int c = 0; c < 3; ++c) lam[c * (size_t)nd + i] = L[c];
+}
+
+// Splits the SoA ddx_state into the adjoint's layouts.
+__global__ void gather_state_kernel(ddx_state s, int ng, int nd, double* xv_m, double* y, double* N, int* idv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ng) {
+        xv_m[0 * ng + i] = s.x[i]; xv_m[1 * ng + i] = s.y[i]; xv_m[2 * ng + i] = s.z[i];
+        xv_m[3 * ng + i] = s.vx[i]; xv_m[4 * ng + i] = s.vy[i]; xv_m[5 * ng + i] = s.vz[i];
+        xv_m[6 * ng + i] = s.m[i];
+    }
+    if (i < nd) {
+        const int t = ng + i;
+        y[0 * (size_t)nd + i] = s.x[t]; y[1 * (size_t)nd + i] = s.y[t]; y[2 * (size_t)nd + i] = s.z[t];
+        y[3 * (size_t)nd + i] = s.vx[t]; y[4 * (size_t)nd + i] = s.vy[t]; y[5 * (size_t)nd + i] = s.vz[t];
+        N[i] = s.N[t];
+        idv[i] = s.id[t];
+    }
+}
+
+// grad [6][ng + nd] <- massive adjoint [6][ng] and tracer adjoint [6][nd].
+__global__ void scatter_grad_kernel(int ng, int nd, const double* lam_m, const double* lam, double* grad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t na = (size_t)ng + nd;
+    if (i < ng)
+        for (int c = 0; c < 6; ++c) grad[c * na + i] = lam_m[c * ng + i];
+    if (i < nd)
+        for (int c = 0; c < 6; ++c) grad[c * na + ng + i] = lam[c * (size_t)nd + i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// Host orchestration
+// ---------------------------------------------------------------------------------------
+
+struct AdjointScratch {
+    int ng = 0, nd = 0, n_steps = 0, K = 0, nck = 0, nblk = 0;
+    double dt = 0;
+    StepArgs sa{};
+    ddx_view view{};
+    ImageList il{};
+    bool ready = false;
+    // buffers
+    double *xv_m = nullptr, *y0 = nullptr, *y = nullptr, *N0 = nullptr, *N = nullptr, *ck = nullptr,
+           *seg = nullptr, *lam = nullptr, *part = nullptr, *mu = nullptr, *lam_m = nullptr, *lam_mass = nullptr;
+    int* idv = nullptr;
+    unsigned char* active = nullptr;
+    Body* Ps = nullptr;
+    ViewConst* vc = nullptr;
+    size_t bytes = 0;
+};
+
+void adjoint_free(AdjointScratch*& a) {
+    if (!a) return;
+    cudaFree(a->xv_m); cudaFree(a->y0); cudaFree(a->y); cudaFree(a->N0); cudaFree(a->N); cudaFree(a->ck);
+    cudaFree(a->seg); cudaFree(a->lam); cudaFree(a->part); cudaFree(a->mu); cudaFree(a->lam_m);
+    cudaFree(a->lam_mass); cudaFree(a->idv); cudaFree(a->active); cudaFree(a->Ps); cudaFree(a->vc);
+    delete a;
+    a = nullptr;
+}
+
+static AdjArgs adj_args(const AdjointScratch& a, const SizeBin* bins) {
+    AdjArgs A;
+    A.ng = a.ng;
+    A.nd = a.nd;
+    A.dt = a.dt;
+    A.sa = a.sa;
+    A.Ps = a.Ps;
+    A.bins = bins;
+    A.id = a.idv;
+    return A;
+}
+
+int adjoint_forward(AdjointScratch*& a, const ddx_state& s, int ng, int nd, double dt, int n_steps, int K,
+                    const StepArgs& sa, const ddx_view& view, const ImageList& il, const SizeBin* bins,
+                    const OpticsDev& o, double* image, cudaStream_t st) {
+    adjoint_free(a);
+    a = new AdjointScratch();
+    a->ng = ng; a->nd = nd; a->dt = dt; a->n_steps = n_steps; a->K = K; a->sa = sa; a->view = view; a->il = il;
+    a->nck = n_steps / K + 1;
+    a->nblk = (nd + kThreads - 1) / kThreads;
+    const size_t nd6 = 6ull * nd;
+    bool fail = cudaMalloc(&a->xv_m, sizeof(double) * 7 * ng) || cudaMalloc(&a->y0, sizeof(double) * nd6) ||
+                cudaMalloc(&a->y, sizeof(double) * nd6) || cudaMalloc(&a->N0, sizeof(double) * nd) ||
+                cudaMalloc(&a->N, sizeof(double) * nd) || cudaMalloc(&a->ck, sizeof(double) * nd6 * a->nck) ||
+                cudaMalloc(&a->seg, sizeof(double) * (size_t)kSegComp * nd * K) ||
+                cudaMalloc(&a->lam, sizeof(double) * nd6) ||
+                cudaMalloc(&a->part, sizeof(double) * (size_t)a->nblk * K * 4 * ng * 4) ||
+                cudaMalloc(&a->mu, sizeof(double) * (size_t)K * 4 * ng * 4) ||
+                cudaMalloc(&a->lam_m, sizeof(double) * 6 * ng) || cudaMalloc(&a->lam_mass, sizeof(double) * ng) ||
+                cudaMalloc(&a->idv, sizeof(int) * nd) || cudaMalloc(&a->active, nd) ||
+                cudaMalloc(&a->Ps, sizeof(Body) * (size_t)n_steps * 4 * ng) || cudaMalloc(&a->vc, sizeof(ViewConst));
+    if (fail) {
+        adjoint_free(a);
+        cudaGetLastError();
+        return DDX_ERR_NOMEM;
+    }
+    const int thr = 256;
+    const int blk = ((nd > ng ? nd : ng) + thr - 1) / thr;
+    gather_state_kernel<<<blk, thr, 0, st>>>(s, ng, nd, a->xv_m, a->y0, a->N0, a->idv);
+    massive_traj_kernel<<<1, 32, 0, st>>>(ng, n_steps, dt, a->xv_m, a->Ps);
+    cudaMemcpyAsync(a->y, a->y0, sizeof(double) * nd6, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
+    const AdjArgs A = adj_args(*a, bins);
+    if (nd > 0)
+        dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, 0, n_steps, K, a->ck, nullptr);
+    if (launch_view_setup(a->vc, view, o.n_theta, st) != cudaSuccess) return DDX_ERR_CUDA;
+    const size_t npix = (size_t)view.xsize * view.ysize;
+    cudaMemsetAsync(image, 0, sizeof(double) * npix * il.n, st);
+    if (nd > 0)
+        image_splat_kernel<<<(nd + 255) / 256, 256, 0, st>>>(a->y, a->N, a->idv, nd, a->vc, o, il, image);
+    if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
+    a->ready = true;
+    return DDX_OK;
+}
+
+int adjoint_backward(AdjointScratch* a, const double* G, double* grad_state, double* grad_mass,
+                     const SizeBin* bins, const OpticsDev& o, cudaStream_t st) {
+    if (!a || !a->ready) return DDX_ERR_STATE;
+    const int ng = a->ng, nd = a->nd, K = a->K;
+    const AdjArgs A = adj_args(*a, bins);
+    cudaMemsetAsync(a->lam_m, 0, sizeof(double) * 6 * ng, st);
+    cudaMemsetAsync(a->lam_mass, 0, sizeof(double) * ng, st);
+    if (nd > 0)
+        image_splat_adjoint_kernel<<<(nd + 255) / 256, 256, 0, st>>>(a->y, a->N, a->idv, nd, a->vc, o, a->il, G,
+                                                                    a->lam, a->active);
+    const int nseg = (a->n_steps + K - 1) / K;
+    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+        const int n0 = sgi * K, n1 = (n0 + K < a->n_steps) ? n0 + K : a->n_steps;
+        const int Kseg = n1 - n0;
+        if (nd > 0) {
+            // recompute the segment from its checkpoint; the N flags are not needed since only
+            // tracers alive at the end carry an adjoint, and those were alive throughout
+            cudaMemcpyAsync(a->y, a->ck + (size_t)(n0 / K) * 6 * nd, sizeof(double) * 6 * nd,
+                            cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
+            dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, n0, n1, K, nullptr, a->seg);
+            dust_reverse_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->seg, n0, n1, a->lam, a->active, a->part);
+            const int per = Kseg * 4 * ng * 4;
+            reduce_parts_kernel<<<(per + 255) / 256, 256, 0, st>>>(a->part, a->nblk, per, a->mu);
+        } else {
+            cudaMemsetAsync(a->mu, 0, sizeof(double) * (size_t)Kseg * 4 * ng * 4, st);
+        }
+        massive_reverse_kernel<<<1, 32, 0, st>>>(ng, a->dt, a->Ps, a->mu, n0, n1, a->lam_m, a->lam_mass);
+    }
+    const int thr = 256, blk = ((nd > ng ? nd : ng) + thr - 1) / thr;
+    scatter_grad_kernel<<<blk, thr, 0, st>>>(ng, nd, a->lam_m, a->lam, grad_state);
+    cudaMemcpyAsync(grad_mass, a->lam_mass, sizeof(double) * ng, cudaMemcpyDeviceToDevice, st);
+    // restore the final state for a later image/backward (the recompute overwrote y and N)
+    if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
+    a->ready = false;
+    return DDX_OK;
+}
+
+}  // namespace ddx

@@ -30,6 +30,7 @@ struct ddx_ctx {
     int inject_lose_tile = -1;                  // one-shot test hook for the next mixed dust launch
     unsigned long long inject_wait_ns = 0;
     CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
+    AdjointScratch* adjoint = nullptr;          // trajectory checkpoints of the last adjoint forward
 };
 
 namespace {
@@ -188,6 +189,7 @@ int ddx_destroy(ddx_ctx* c) {
     cudaFree(c->bins); cudaFree(c->size_d); cudaFree(c->vc); cudaFree(c->od_dev);
     cudaFree(c->sed_partial); cudaFree(c->counters); cudaFree(c->status);
     collide_free(c->collide);
+    adjoint_free(c->adjoint);
     delete c;
     return DDX_OK;
 }
@@ -316,6 +318,37 @@ int ddx_collide(ddx_ctx* c, const ddx_state* s, int i0, int i1, double h, int* p
     cudaSetDevice(c->device);
     return collide_run(c->collide, *s, i0, i1, h, reinterpret_cast<int2*>(pairs), cap, n_pairs,
                        (cudaStream_t)stream);
+}
+
+int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,
+                        int ckpt_every, const ddx_phys* phys, const ddx_view* view, const int* wj, int n_img,
+                        double* image, void* stream) {
+    if (!c || !state_ok(s) || !phys || !view || !wj || !image || n_steps < 1 || ckpt_every < 1) return DDX_ERR_ARG;
+    if (phys->FLQ != 0) return DDX_ERR_ARG;   // the adjoint does not cover the Lorentz force
+    if (n_grav > DDX_ADJ_MAX_GRAV) return DDX_ERR_RANGE;
+    if (n_img < 1 || n_img > kMaxImages || view->xsize < 1 || view->ysize < 1 || !(view->fov > 0.0)) return DDX_ERR_ARG;
+    if (!c->bins || !c->optics_set) return DDX_ERR_STATE;
+    StepArgs a;
+    int r = make_step_args(phys, n_grav, n_dust, dt, DDX_MODE_FIXED, a);
+    if (r) return r;
+    ImageList il;
+    il.n = n_img;
+    for (int k = 0; k < n_img; ++k) {
+        if (wj[k] < 0 || wj[k] >= c->od.n_wav) return DDX_ERR_ARG;
+        il.wj[k] = wj[k];
+    }
+    cudaSetDevice(c->device);
+    const int K = ckpt_every < n_steps ? ckpt_every : n_steps;
+    return adjoint_forward(c->adjoint, *s, n_grav, n_dust, dt, n_steps, K, a, *view, il, c->bins, c->od, image,
+                           (cudaStream_t)stream);
+}
+
+int ddx_adjoint_backward(ddx_ctx* c, const double* dL_dimage, double* grad_state, double* grad_mass,
+                         void* stream) {
+    if (!c || !dL_dimage || !grad_state || !grad_mass) return DDX_ERR_ARG;
+    if (!c->adjoint) return DDX_ERR_STATE;
+    cudaSetDevice(c->device);
+    return adjoint_backward(c->adjoint, dL_dimage, grad_state, grad_mass, c->bins, c->od, (cudaStream_t)stream);
 }
 
 int ddx_debug_lose_tile_copy(ddx_ctx* c, int tile, unsigned long long wait_ns) {

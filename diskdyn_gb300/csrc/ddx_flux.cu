@@ -359,6 +359,11 @@ cudaError_t launch_image(const ddx_state& s, int n_grav, int n_dust, const ddx_v
     return cudaGetLastError();
 }
 
+cudaError_t launch_view_setup(ViewConst* vc, const ddx_view& view, int n_theta, cudaStream_t st) {
+    view_setup_kernel<<<1, 32, 0, st>>>(vc, view, n_theta);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pixels(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
                           int n_theta, ViewConst* vc, int* pix, int* exact, cudaStream_t st) {
     view_setup_kernel<<<1, 32, 0, st>>>(vc, view, n_theta);

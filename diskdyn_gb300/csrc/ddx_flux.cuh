@@ -41,6 +41,16 @@ cudaError_t launch_sed(const ddx_state& s, int n_grav, int n_dust, const ddx_vie
                        const OpticsDev& o, ViewConst* vc, double* partial, int mode,
                        double* Fsed, cudaStream_t st);
 int sed_blocks(int n_dust);
+cudaError_t launch_view_setup(ViewConst* vc, const ddx_view& view, int n_theta, cudaStream_t st);
+
+// Discrete adjoint (ddx_adjoint.cu).
+struct AdjointScratch;
+int adjoint_forward(AdjointScratch*& a, const ddx_state& s, int ng, int nd, double dt, int n_steps, int K,
+                    const StepArgs& sa, const ddx_view& view, const ImageList& il, const SizeBin* bins,
+                    const OpticsDev& o, double* image, cudaStream_t st);
+int adjoint_backward(AdjointScratch* a, const double* G, double* grad_state, double* grad_mass,
+                     const SizeBin* bins, const OpticsDev& o, cudaStream_t st);
+void adjoint_free(AdjointScratch*& a);
 cudaError_t launch_pixels(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
                           int n_theta, ViewConst* vc, int* pix, int* exact, cudaStream_t st);
 

@@ -182,6 +182,29 @@ int ddx_sed(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
 int ddx_collide(ddx_ctx *ctx, const ddx_state *s, int i0, int i1, double h, int *pairs,
                 long long cap, long long *n_pairs, void *stream);
 
+/* Discrete adjoint of the trajectory and image (no counterpart in the reference).
+ *
+ * ddx_adjoint_forward integrates the initial state `s` (read only) for n_steps fixed-dt
+ * RK4 steps in FP64 -- the massive set (at most DDX_ADJ_MAX_GRAV bodies) and the dust
+ * tracers under the physics of ddx_step except the Lorentz force (phys->FLQ must be 0) --
+ * keeping a checkpoint of the tracer state every ckpt_every steps in the context.  It
+ * then writes image[n_img][xsize*ysize] (device): the flux of ddx_image deposited with
+ * bilinear weights on the four pixel centres around each tracer's projected position
+ * (pixel (x, y) centred at psca*(x + 1/2 - xsize/2)), which is continuous in the
+ * positions, unlike the nearest-pixel binning of ddx_image.
+ *
+ * ddx_adjoint_backward takes dL/dimage (device, the layout of image) for any scalar L
+ * and writes dL/d(initial state) to grad_state[6][n_grav + n_dust] (rows x, y, z, vx, vy,
+ * vz; device) and dL/d(mass*4pi^2) of the massive bodies to grad_mass[n_grav] (device),
+ * by checkpoint-and-recompute: every segment is recomputed from its checkpoint and swept
+ * backwards through the RK4 stages.  One backward per forward. */
+#define DDX_ADJ_MAX_GRAV 32
+int ddx_adjoint_forward(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
+                        int n_steps, int ckpt_every, const ddx_phys *phys, const ddx_view *view,
+                        const int *wj, int n_img, double *image, void *stream);
+int ddx_adjoint_backward(ddx_ctx *ctx, const double *dL_dimage, double *grad_state,
+                         double *grad_mass, void *stream);
+
 /* Diagnostics (no reference counterpart).  ddx_debug_pixels writes, for every dust
  * tracer, the pixel index ysize*x + y that ddx_image uses (or -1 for a tracer without
  * optical data or outside the image) to pix[n_dust], and 1/0 to exact[n_dust] when the
