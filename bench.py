@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", choices=["dusty_ring", "imaging"], default="dusty_ring")
+    p.add_argument("--adjoint-steps", type=int, default=2000)
     return p.parse_args()
 
 
@@ -329,12 +330,90 @@ def run_ours(args, world, rank, local):
         "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
     }
+    if rank == 0 and args.adjoint_steps > 0:
+        line["adjoint"] = adjoint_leg(local, n_steps=args.adjoint_steps)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(sysm, args.cpu_sample)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
+    """Adjoint/forward wall-time ratio on the image-loss workload: L2 loss between the
+    image of the dusty-ring system (262,144 grains, 512x512, 2,000 steps) and a target
+    made by the same code with planet 1 at 1.2x the mass and a + 2 AU; gradients with
+    respect to planet masses, a, e, i and every grain's initial state by
+    checkpoint-and-recompute every 100 steps.  Also a central finite-difference check of
+    dL/dm of planet 1 (h = 1e-6 relative)."""
+    import torch
+    from diskdyn_gb300 import adjoint as adj
+    from diskdyn_gb300.engine import Engine, make_phys, make_view
+
+    s = adj.adjoint_system(n_dust=n_dust, xsize=512, ysize=512, n_steps=n_steps)
+    eng = Engine(local)
+    eng.set_size_table(**s.size_table)
+    o = s.optics
+    eng.set_optics(o["w"], o["in"], o["Qabs"], o["Qsca"], o["Qpfunc"], o["Td"], o["Rmin"], o["Rmax"])
+    ng = s.n_grav
+    dev = f"cuda:{local}"
+    N = torch.tensor(s.state["N"][ng:], dtype=torch.float64, device=dev)
+    ids = torch.tensor(s.state["id"][ng:], dtype=torch.int32, device=dev)
+    dust0 = torch.tensor(np.stack([s.state[k][ng:] for k in ("x", "y", "z", "vx", "vy", "vz")], 1),
+                         dtype=torch.float64, device=dev)
+    phys, view = make_phys(**s.phys), make_view(**s.view)
+    el = adj.planet_elements(s)
+
+    def elements(grad):
+        t = {k: torch.tensor(np.asarray(v, dtype=np.float64), device=dev) for k, v in el.items()}
+        if grad:
+            for k in ("m", "a", "e", "i"):
+                t[k].requires_grad_(True)
+        return t
+
+    def image(t, dust):
+        M = adj.planet_state(t["Mstar"], t["m"], t["a"], t["e"], t["i"], t["w"], t["o"], t["nu"])
+        return adj.trajectory_image(eng, M, dust, N, ids, s.dt, n_steps, ckpt, phys, view, s.image_wj)
+
+    with torch.no_grad():
+        tt = elements(False)
+        tt["m"][0] *= 1.2
+        tt["a"][0] += 2.0
+        target = image(tt, dust0)
+        image(elements(False), dust0)          # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        img = image(elements(False), dust0)
+        L0 = ((img - target) ** 2).sum().item()
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    t = elements(True)
+    d = dust0.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L = ((image(t, d) - target) ** 2).sum()
+    L.backward()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    g_m = t["m"].grad[0].item()
+    base = el["m"][0]
+    h = 1e-6 * base
+    vals = []
+    for sgn in (1.0, -1.0):
+        with torch.no_grad():
+            tp = elements(False)
+            tp["m"][0] = base + sgn * h
+            vals.append(((image(tp, dust0) - target) ** 2).sum().item())
+    fd = (vals[0] - vals[1]) / (2 * h)
+    eng.close()
+    return {"workload": "image loss, 3 massive + %d grains, %dx%d, %d steps, checkpoints every %d"
+                        % (n_dust, 512, 512, n_steps, ckpt),
+            "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "adjoint_over_forward": t_grad / t_fwd,
+            "loss": L0, "dL_dm_planet1_adjoint": g_m, "dL_dm_planet1_fd": fd,
+            "fd_rel_err": abs(g_m - fd) / abs(fd) if fd != 0 else None,
+            "grad_norm_a": t["a"].grad.norm().item(), "grad_norm_dust": d.grad.norm().item()}
 
 
 def cpu_baseline(sysm, n_sample):

@@ -16,13 +16,18 @@
 //
 // Backward (checkpoint-and-recompute every K steps):
 //  1. image adjoint: dL/dimage -> adjoint of the final tracer positions;
-//  2. per segment, last first: recompute the K steps from the checkpoint, storing each
-//     step's state and stage accelerations a1..a3 (15 doubles per tracer per step);
-//     reverse sweep of the four RK4 stages per tracer with analytic vector-Jacobian
-//     products of the star term and the body gravity; the adjoints of the bodies' stage
-//     positions and masses are reduced per block in a fixed order (warp shuffles, then
-//     shared memory, then block partials summed in block order), so the gradient is
-//     deterministic; a single-warp kernel then runs the reverse sweep of the massive set.
+//  2. per segment, last first: recompute the K steps from the checkpoint (the forward
+//     already kept the last segment), storing each step's state, stage accelerations
+//     a1..a3 and the stages' reciprocal distances (31 doubles per tracer per step for three
+//     bodies); reverse sweep of the four RK4 stages per tracer with analytic
+//     vector-Jacobian products of the star term and the body gravity; the adjoints of the
+//     bodies' stage positions and masses are reduced per block in a fixed order (a
+//     transposed shared-memory tile per warp, then the warps, then block partials summed
+//     in block order), so the gradient is deterministic; a single-warp kernel then runs
+//     the reverse sweep of the massive set.
+// FP64 runs at ~1/75 of the FP32 rate here, so the kernels are bound by their count of
+// FP64 operations: the forward takes one division and one square root for the star and
+// one rsqrt per body per stage, and the reverse reuses them from the record.
 // Tracers removed during the forward (N = 0) or without optical data emit nothing, so
 // their adjoint is zero and they are skipped.
 #include "ddx_internal.cuh"
@@ -35,9 +40,12 @@ constexpr int kMaxGrav = DDX_ADJ_MAX_GRAV;
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSegComp = 15;   // per tracer per step: x, y, z, vx, vy, vz, a1, a2, a3
+constexpr int kMaxStoredIr = 3; // bodies whose 1/|e| the recompute keeps (n_grav <= 4)
 
 struct AdjArgs {
     int ng, nd;
+    int nir;                // bodies 1..nir have their 1/|e| kept per stage
+    int ncomp;              // doubles per tracer per step in the recompute record
     double dt;
     StepArgs sa;            // star-term constants (FLQ = 0)
     const Body* Ps;         // [n_steps][4][ng]
@@ -45,25 +53,48 @@ struct AdjArgs {
     const int* id;          // [nd]
 };
 
-__device__ __forceinline__ double wsum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
+
+// Per-tracer constants of the star term: a = -Fg d - Fb1 (Fb2 d + r) with
+// Fg = g0/R^3, Fb1 = c1/R^2, Fb2 = (d.r)/R^2 (src/gpu_functions.cu:691-704).
+struct StarConst {
+    double g0, c1, inv_m0;
+};
+__device__ __forceinline__ StarConst star_const(const AdjArgs& A, double m0, float bet, float betsw) {
+    StarConst k;
+    k.g0 = (1.0 - bet - betsw) * m0;
+    k.c1 = (A.sa.SWQ == 1) ? m0 * (bet / kLightAU + betsw / A.sa.vswAU) : bet * m0 / kLightAU;
+    k.inv_m0 = 1.0 / m0;
+    return k;
 }
 
-// Acceleration of a tracer at (x, r) for the stage whose body records are P[0..ng).
-__device__ __forceinline__ bool tracer_accel(const AdjArgs& A, const Body* P, double x, double y, double z,
-                                             double rx, double ry, double rz, float bet, float betsw,
-                                             double& ax, double& ay, double& az) {
-    if (!star_term(x - P[0].x, y - P[0].y, z - P[0].z, rx, ry, rz, P[0].m, bet, betsw, 0.f, 1.0, A.sa, ax,
-                   ay, az))
-        return false;
+// Acceleration of a tracer at (x, r) for the stage whose body records are P[0..ng), with one
+// square root and one division for the star and one rsqrt per body.  Returns false on
+// sublimation (R <= Rmin) or an exact coincidence with a body.  rc (optional, stride rs):
+// receives 1/R^2 and 1/R of the star and 1/|e| of bodies 1..nir, which the reverse sweep
+// reuses instead of dividing and taking roots again (FP64 division and square root are
+// ~9 dependent FP64 operations each, on a pipe 75x slower than FP32).
+__device__ __forceinline__ bool tracer_accel(const AdjArgs& A, const StarConst& K, const Body* P, double x,
+                                             double y, double z, double rx, double ry, double rz,
+                                             double& ax, double& ay, double& az, double* rc, size_t rs) {
+    const double dx = x - P[0].x, dy = y - P[0].y, dz = z - P[0].z;
+    const double RR = dx * dx + dy * dy + dz * dz;
+    if (RR <= A.sa.Rmin * A.sa.Rmin) return false;
+    const double iRR = 1.0 / RR;
+    const double iR = sqrt(iRR);
+    const double iR3 = iR * iRR;
+    if (rc) { rc[0] = iRR; rc[rs] = iR; }
+    const double Fg = K.g0 * iR3, Fb1 = K.c1 * iRR, Fb2 = (dx * rx + dy * ry + dz * rz) * iRR;
+    ax = -Fg * dx - Fb1 * (Fb2 * dx + rx);
+    ay = -Fg * dy - Fb1 * (Fb2 * dy + ry);
+    az = -Fg * dz - Fb1 * (Fb2 * dz + rz);
     for (int j = 1; j < A.ng; ++j) {
-        const double dx = P[j].x - x, dy = P[j].y - y, dz = P[j].z - z;
-        const double RR = dx * dx + dy * dy + dz * dz;
-        if (RR == 0.0) return false;
-        const double f = P[j].m / (RR * sqrt(RR));
-        ax += f * dx; ay += f * dy; az += f * dz;
+        const double ex = P[j].x - x, ey = P[j].y - y, ez = P[j].z - z;
+        const double R2 = ex * ex + ey * ey + ez * ez;
+        if (R2 == 0.0) return false;
+        const double ir = rsqrt(R2);
+        if (rc && j <= A.nir) rc[(1 + j) * rs] = ir;
+        const double f = P[j].m * (ir * ir * ir);
+        ax += f * ex; ay += f * ey; az += f * ez;
     }
     return true;
 }
@@ -216,9 +247,11 @@ __global__ void massive_reverse_kernel(int ng, double dt, const Body* Ps, const 
 
 // Integrates every tracer over steps [n0, n1).  ck (optional): the state at every step
 // that is a multiple of K (checkpoint c at ck + c*6*nd), including n1 when it is one.
-// seg (optional): per step, the state and the stage accelerations a1..a3.
+// seg (optional): for every step n >= seg_n0, record n - seg_n0 holds the state, the stage
+// accelerations a1..a3 and each stage's reciprocal distances (A.ncomp doubles per tracer).
 __global__ void __launch_bounds__(kThreads)
-dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, double* ck, double* seg) {
+dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, double* ck, double* seg,
+                    int seg_n0) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     if (i >= A.nd) return;
     const size_t nd = A.nd;
@@ -228,6 +261,7 @@ dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, doub
     float bet = 0.f, betsw = 0.f;
     const int id = A.id[i];
     if (id >= 0) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
+    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw);
     const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
     for (int n = n0; n < n1; ++n) {
         if (ck && n % K == 0) {
@@ -238,21 +272,23 @@ dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, doub
         double a1x = 0, a1y = 0, a1z = 0, a2x = 0, a2y = 0, a2z = 0, a3x = 0, a3y = 0, a3z = 0;
         if (alive) {
             const Body* P = A.Ps + (size_t)n * 4 * A.ng;
+            double* S = (seg && n >= seg_n0) ? seg + (size_t)(n - seg_n0) * A.ncomp * nd + i : nullptr;
+            const size_t rstage = (size_t)(2 + A.nir) * nd;   // record stride between stages
+            double* rc = S ? S + kSegComp * nd : nullptr;
             double a4x = 0, a4y = 0, a4z = 0;
-            bool ok = tracer_accel(A, P, x, yy, z, vx, vy, vz, bet, betsw, a1x, a1y, a1z);
+            bool ok = tracer_accel(A, K0, P, x, yy, z, vx, vy, vz, a1x, a1y, a1z, rc, nd);
             const double r2x = vx + a1x * h2, r2y = vy + a1y * h2, r2z = vz + a1z * h2;
-            ok = ok && tracer_accel(A, P + A.ng, x + vx * h2, yy + vy * h2, z + vz * h2, r2x, r2y, r2z, bet,
-                                    betsw, a2x, a2y, a2z);
+            ok = ok && tracer_accel(A, K0, P + A.ng, x + vx * h2, yy + vy * h2, z + vz * h2, r2x, r2y, r2z,
+                                    a2x, a2y, a2z, S ? rc + rstage : nullptr, nd);
             const double r3x = vx + a2x * h2, r3y = vy + a2y * h2, r3z = vz + a2z * h2;
-            ok = ok && tracer_accel(A, P + 2 * A.ng, x + r2x * h2, yy + r2y * h2, z + r2z * h2, r3x, r3y, r3z,
-                                    bet, betsw, a3x, a3y, a3z);
+            ok = ok && tracer_accel(A, K0, P + 2 * A.ng, x + r2x * h2, yy + r2y * h2, z + r2z * h2, r3x, r3y,
+                                    r3z, a3x, a3y, a3z, S ? rc + 2 * rstage : nullptr, nd);
             const double r4x = vx + a3x * dt, r4y = vy + a3y * dt, r4z = vz + a3z * dt;
-            ok = ok && tracer_accel(A, P + 3 * A.ng, x + r3x * dt, yy + r3y * dt, z + r3z * dt, r4x, r4y, r4z,
-                                    bet, betsw, a4x, a4y, a4z);
-            if (seg) {
-                double* S = seg + (size_t)(n - n0) * kSegComp * nd;
+            ok = ok && tracer_accel(A, K0, P + 3 * A.ng, x + r3x * dt, yy + r3y * dt, z + r3z * dt, r4x, r4y,
+                                    r4z, a4x, a4y, a4z, S ? rc + 3 * rstage : nullptr, nd);
+            if (S) {
                 const double v[kSegComp] = {x, yy, z, vx, vy, vz, a1x, a1y, a1z, a2x, a2y, a2z, a3x, a3y, a3z};
-                for (int c = 0; c < kSegComp; ++c) S[c * nd + i] = v[c];
+                for (int c = 0; c < kSegComp; ++c) S[c * nd] = v[c];
             }
             if (!ok) {
                 alive = false;   // removed: keeps its last state, emits nothing
@@ -276,73 +312,104 @@ dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, doub
     if (!alive) N[i] = 0.0;
 }
 
-// VJP of the tracer acceleration at one stage with adjoint g: adds to (Lx, Lr) and
-// deposits, per source j, the adjoints of its stage position and mass into wp[j][0..3]
-// (warp-reduced, lane 0 writes).  Called by every lane of the warp.
-__device__ __forceinline__ void tracer_vjp(const AdjArgs& A, const Body* P, bool on, const double* pos,
-                                           const double* r, float bet, float betsw, const double* g,
-                                           double* Lx, double* Lr, double (*wp)[4], int lane) {
-    double s4[4] = {0, 0, 0, 0};
-    if (on) {
-        const double dx = pos[0] - P[0].x, dy = pos[1] - P[0].y, dz = pos[2] - P[0].z;
-        const double RR = dx * dx + dy * dy + dz * dz;
-        const double R = sqrt(RR), R3 = RR * R, R5 = R3 * RR;
-        const double m0 = P[0].m;
-        const double g0 = (1.0 - bet - betsw) * m0;
-        const double Fg = g0 / R3;
-        const double c1 = (A.sa.SWQ == 1) ? m0 * (bet / kLightAU + betsw / A.sa.vswAU) : bet * m0 / kLightAU;
-        const double Fb1 = c1 / RR;
-        const double dr = dx * r[0] + dy * r[1] + dz * r[2];
-        const double Fb2 = dr / RR;
-        const double gd = g[0] * dx + g[1] * dy + g[2] * dz;
-        const double gr = g[0] * r[0] + g[1] * r[1] + g[2] * r[2];
-        const double gD = Fb2 * gd + gr;
-        // a = -Fg d - Fb1 (Fb2 d + r): g^T da/dd = cg g + cd d + cr r ; g^T da/dr = cr d - Fb1 g
-        const double cg = -Fg - Fb1 * Fb2;
-        const double cd = 3.0 * g0 * gd / R5 + 2.0 * c1 * gD / (RR * RR) + 2.0 * Fb1 * gd * dr / (RR * RR);
-        const double cr = -Fb1 * gd / RR;
-        const double d[3] = {dx, dy, dz};
-        for (int c = 0; c < 3; ++c) {
-            const double ld = cg * g[c] + cd * d[c] + cr * r[c];
-            Lx[c] += ld;
-            Lr[c] += cr * d[c] - Fb1 * g[c];
-            s4[c] = -ld;
-        }
-        s4[3] = (-Fg * gd - Fb1 * gD) / m0;
+// Warp-wide sums of the per-tracer adjoints of the bodies' stage positions and masses.
+// Each source adds 4 rows (x, y, z, m) to a 32 x 32 shared-memory tile, one column per
+// lane; row r holds lane k's value at column (k + r) mod 32, so row-wise reads by the 32
+// lanes fall in different banks.  A full tile (8 sources) or the end of a step flushes it:
+// p = 32 / rows lanes (a power of two) share a row, each adds 32/p columns in lane order
+// and a fixed shuffle tree joins the p partials.  Sums land in wp in the order the sources
+// were put, a fixed order, so the result is deterministic.  A whole step of three bodies
+// (48 rows) costs 49 FP64 additions per lane, against 240 for a shuffle tree per value.
+struct RowTile {
+    double (*tb)[32];
+    double* wp;
+    int rows, base, lane;
+
+    __device__ __forceinline__ void flush() {
+        if (rows == 0) return;
+        __syncwarp();
+        int p = 1;
+        while (2 * p * rows <= 32) p *= 2;
+        const int w = 32 / p, row = lane / p, part = lane % p;
+        double t = 0.0;
+        if (row < rows)
+            for (int k = 0; k < w; ++k) t += tb[row][(part * w + k + row) & 31];
+        for (int o = p / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (row < rows && part == 0) wp[base + row] = t;
+        base += rows;
+        rows = 0;
+        __syncwarp();
     }
-    for (int c = 0; c < 4; ++c) {
-        const double t = wsum(s4[c]);
-        if (lane == 0) wp[0][c] = t;
+    __device__ __forceinline__ void put4(const double* v) {
+        if (rows == 32) flush();
+        for (int c = 0; c < 4; ++c) tb[rows + c][(lane + rows + c) & 31] = v[c];
+        rows += 4;
+    }
+};
+
+// VJP of the tracer acceleration at one stage with adjoint g: adds to (Lx, Lr) and puts,
+// per source j, the tracer's adjoints of that source's stage position and mass into T.
+// rc (stride rs): the stage's reciprocal distances kept by the recompute.  Called by
+// every lane of the warp.
+__device__ __forceinline__ void tracer_vjp(const AdjArgs& A, const StarConst& K, const Body* P, bool on,
+                                           const double* pos, const double* r, const double* g, double* Lx,
+                                           double* Lr, const double* rc, size_t rs, RowTile& T) {
+    {   // star (source 0)
+        double s4[4] = {0, 0, 0, 0};
+        if (on) {
+            const double dx = pos[0] - P[0].x, dy = pos[1] - P[0].y, dz = pos[2] - P[0].z;
+            const double iRR = rc[0];
+            const double iR3 = rc[rs] * iRR, iR5 = iR3 * iRR;
+            const double Fg = K.g0 * iR3, Fb1 = K.c1 * iRR;
+            const double dr = dx * r[0] + dy * r[1] + dz * r[2];
+            const double Fb2 = dr * iRR;
+            const double gd = g[0] * dx + g[1] * dy + g[2] * dz;
+            const double gr = g[0] * r[0] + g[1] * r[1] + g[2] * r[2];
+            const double gD = Fb2 * gd + gr;
+            // a = -Fg d - Fb1 (Fb2 d + r): g^T da/dd = cg g + cd d + cr r ; g^T da/dr = cr d - Fb1 g
+            const double cg = -Fg - Fb1 * Fb2;
+            const double cd = 3.0 * K.g0 * gd * iR5 + 2.0 * (K.c1 * gD + Fb1 * gd * dr) * (iRR * iRR);
+            const double cr = -Fb1 * gd * iRR;
+            const double d[3] = {dx, dy, dz};
+            for (int c = 0; c < 3; ++c) {
+                const double ld = cg * g[c] + cd * d[c] + cr * r[c];
+                Lx[c] += ld;
+                Lr[c] += cr * d[c] - Fb1 * g[c];
+                s4[c] = -ld;
+            }
+            s4[3] = (-Fg * gd - Fb1 * gD) * K.inv_m0;
+        }
+        T.put4(s4);
     }
     for (int j = 1; j < A.ng; ++j) {
         double v4[4] = {0, 0, 0, 0};
         if (on) {
             const double dx = P[j].x - pos[0], dy = P[j].y - pos[1], dz = P[j].z - pos[2];
-            const double RR = dx * dx + dy * dy + dz * dz;
-            const double ri3 = 1.0 / (RR * sqrt(RR)), ri5 = ri3 / RR;
+            const double ir = (j <= A.nir) ? rc[(1 + j) * rs] : rsqrt(dx * dx + dy * dy + dz * dz);
+            const double ir2 = ir * ir;
+            const double ri3 = ir2 * ir, ri5 = ri3 * ir2;
             const double gd = g[0] * dx + g[1] * dy + g[2] * dz;
             const double m = P[j].m;
-            v4[0] = m * (g[0] * ri3 - 3.0 * gd * dx * ri5);
-            v4[1] = m * (g[1] * ri3 - 3.0 * gd * dy * ri5);
-            v4[2] = m * (g[2] * ri3 - 3.0 * gd * dz * ri5);
+            const double t3 = 3.0 * gd * ri5;
+            v4[0] = m * (g[0] * ri3 - t3 * dx);
+            v4[1] = m * (g[1] * ri3 - t3 * dy);
+            v4[2] = m * (g[2] * ri3 - t3 * dz);
             v4[3] = gd * ri3;
             Lx[0] -= v4[0]; Lx[1] -= v4[1]; Lx[2] -= v4[2];
         }
-        for (int c = 0; c < 4; ++c) {
-            const double t = wsum(v4[c]);
-            if (lane == 0) wp[j][c] = t;
-        }
+        T.put4(v4);
     }
 }
 
-// Reverse sweep over steps [n0, n1) (descending) from the stored states and stage
-// accelerations.  lam [6][nd] holds the adjoint of the state after step n1-1 on entry
-// and of the state before step n0 on exit.  part[block][k][stage][j][4]: this block's
-// sum of the adjoints of the bodies' stage positions and masses.
+// Reverse sweep over steps [n0, n1) (descending) from the recompute records.  lam [6][nd]
+// holds the adjoint of the state after step n1-1 on entry and of the state before step n0
+// on exit.  part[block][k][stage][j][4]: this block's sum of the adjoints of the bodies'
+// stage positions and masses.
 __global__ void __launch_bounds__(kThreads)
 dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, double* __restrict__ lam,
                     const unsigned char* __restrict__ active, double* __restrict__ part) {
-    __shared__ double wpart[kWarps][4][kMaxGrav][4];
+    __shared__ double wpart[kWarps][16 * kMaxGrav];   // per warp: [3 - stage][j][4], one step
+    __shared__ double tbuf[kWarps][32][32];
     const int i = blockIdx.x * kThreads + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t nd = A.nd;
@@ -354,12 +421,17 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
         const int id = A.id[i];
         if (id >= 0) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
     }
+    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw);
+    RowTile T{tbuf[warp], wpart[warp], 0, 0, lane};
     const int Kseg = n1 - n0;
     const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
+    const size_t rstage = (size_t)(2 + A.nir) * nd;
     for (int n = n1 - 1; n >= n0; --n) {
         const int k = n - n0;
+        const double* S = seg + (size_t)k * A.ncomp * nd + (on ? i : 0);
+        const double* rc = S + kSegComp * nd;
         double st[kSegComp];
-        for (int c = 0; c < kSegComp; ++c) st[c] = on ? seg[((size_t)k * kSegComp + c) * nd + i] : 0.0;
+        for (int c = 0; c < kSegComp; ++c) st[c] = on ? S[c * nd] : 0.0;
         const double* x = st;
         const double* v = st + 3;
         const double* a1 = st + 6;
@@ -385,7 +457,7 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
         double Ls[3], Lq[3];
         // stage 4: a4 = a(x4, r4); x4 = x + r3 dt; r4 = v + a3 dt
         Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
-        tracer_vjp(A, P + 3 * A.ng, on, x4, r4, bet, betsw, La4, Ls, Lq, wpart[warp][3], lane);
+        tracer_vjp(A, K0, P + 3 * A.ng, on, x4, r4, La4, Ls, Lq, rc + 3 * rstage, nd, T);
         for (int c = 0; c < 3; ++c) {
             Lr4[c] += Lq[c];
             Lx[c] += Ls[c]; Lr3[c] += dt * Ls[c];
@@ -393,7 +465,7 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
         }
         // stage 3: a3 = a(x3, r3); x3 = x + r2 h2; r3 = v + a2 h2
         Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
-        tracer_vjp(A, P + 2 * A.ng, on, x3, r3, bet, betsw, La3, Ls, Lq, wpart[warp][2], lane);
+        tracer_vjp(A, K0, P + 2 * A.ng, on, x3, r3, La3, Ls, Lq, rc + 2 * rstage, nd, T);
         for (int c = 0; c < 3; ++c) {
             Lr3[c] += Lq[c];
             Lx[c] += Ls[c]; Lr2[c] += h2 * Ls[c];
@@ -401,7 +473,7 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
         }
         // stage 2: a2 = a(x2, r2); x2 = x + v h2; r2 = v + a1 h2
         Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
-        tracer_vjp(A, P + A.ng, on, x2, r2, bet, betsw, La2, Ls, Lq, wpart[warp][1], lane);
+        tracer_vjp(A, K0, P + A.ng, on, x2, r2, La2, Ls, Lq, rc + rstage, nd, T);
         for (int c = 0; c < 3; ++c) {
             Lr2[c] += Lq[c];
             Lx[c] += Ls[c]; Lv[c] += h2 * Ls[c];
@@ -409,16 +481,18 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
         }
         // stage 1: a1 = a(x, v)
         Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
-        tracer_vjp(A, P, on, x, v, bet, betsw, La1, Ls, Lq, wpart[warp][0], lane);
+        tracer_vjp(A, K0, P, on, x, v, La1, Ls, Lq, rc, nd, T);
         for (int c = 0; c < 3; ++c) {
             Lx[c] += Ls[c]; Lv[c] += Lq[c];
             lx[c] = Lx[c]; lv[c] = Lv[c];
         }
+        T.flush();
+        T.base = 0;
         __syncthreads();
         for (int e = threadIdx.x; e < 4 * A.ng * 4; e += kThreads) {
-            const int s = e / (A.ng * 4), j = (e / 4) % A.ng, c = e % 4;
+            const int s = 3 - e / (A.ng * 4), j = (e / 4) % A.ng, c = e % 4;
             double t = 0.0;
-            for (int w = 0; w < kWarps; ++w) t += wpart[w][s][j][c];
+            for (int w = 0; w < kWarps; ++w) t += wpart[w][e];
             part[((((size_t)blockIdx.x * Kseg + k) * 4 + s) * A.ng + j) * 4 + c] = t;
         }
         __syncthreads();
@@ -660,10 +734,17 @@ void adjoint_free(AdjointScratch*& a) {
     a = nullptr;
 }
 
+// Recompute record per tracer per step: state + a1..a3, then per stage 1/R^2 and 1/R of
+// the star and 1/|e| of bodies 1..nir (all bodies when n_grav <= 4).
+static int record_nir(int ng) { return ng - 1 <= kMaxStoredIr ? ng - 1 : 0; }
+static int record_comps(int ng) { return kSegComp + 4 * (2 + record_nir(ng)); }
+
 static AdjArgs adj_args(const AdjointScratch& a, const SizeBin* bins) {
     AdjArgs A;
     A.ng = a.ng;
     A.nd = a.nd;
+    A.nir = record_nir(a.ng);
+    A.ncomp = record_comps(a.ng);
     A.dt = a.dt;
     A.sa = a.sa;
     A.Ps = a.Ps;
@@ -684,7 +765,7 @@ int adjoint_forward(AdjointScratch*& a, const ddx_state& s, int ng, int nd, doub
     bool fail = cudaMalloc(&a->xv_m, sizeof(double) * 7 * ng) || cudaMalloc(&a->y0, sizeof(double) * nd6) ||
                 cudaMalloc(&a->y, sizeof(double) * nd6) || cudaMalloc(&a->N0, sizeof(double) * nd) ||
                 cudaMalloc(&a->N, sizeof(double) * nd) || cudaMalloc(&a->ck, sizeof(double) * nd6 * a->nck) ||
-                cudaMalloc(&a->seg, sizeof(double) * (size_t)kSegComp * nd * K) ||
+                cudaMalloc(&a->seg, sizeof(double) * (size_t)record_comps(ng) * nd * K) ||
                 cudaMalloc(&a->lam, sizeof(double) * nd6) ||
                 cudaMalloc(&a->part, sizeof(double) * (size_t)a->nblk * K * 4 * ng * 4) ||
                 cudaMalloc(&a->mu, sizeof(double) * (size_t)K * 4 * ng * 4) ||
@@ -703,8 +784,11 @@ int adjoint_forward(AdjointScratch*& a, const ddx_state& s, int ng, int nd, doub
     cudaMemcpyAsync(a->y, a->y0, sizeof(double) * nd6, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
     const AdjArgs A = adj_args(*a, bins);
+    // the forward also keeps the records of the last segment, which the backward then
+    // does not recompute
+    const int last0 = ((n_steps + K - 1) / K - 1) * K;
     if (nd > 0)
-        dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, 0, n_steps, K, a->ck, nullptr);
+        dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, 0, n_steps, K, a->ck, a->seg, last0);
     if (launch_view_setup(a->vc, view, o.n_theta, st) != cudaSuccess) return DDX_ERR_CUDA;
     const size_t npix = (size_t)view.xsize * view.ysize;
     cudaMemsetAsync(image, 0, sizeof(double) * npix * il.n, st);
@@ -730,12 +814,15 @@ int adjoint_backward(AdjointScratch* a, const double* G, double* grad_state, dou
         const int n0 = sgi * K, n1 = (n0 + K < a->n_steps) ? n0 + K : a->n_steps;
         const int Kseg = n1 - n0;
         if (nd > 0) {
-            // recompute the segment from its checkpoint; the N flags are not needed since only
-            // tracers alive at the end carry an adjoint, and those were alive throughout
-            cudaMemcpyAsync(a->y, a->ck + (size_t)(n0 / K) * 6 * nd, sizeof(double) * 6 * nd,
-                            cudaMemcpyDeviceToDevice, st);
-            cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
-            dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, n0, n1, K, nullptr, a->seg);
+            // recompute the segment from its checkpoint (the last one's records are still
+            // there from the forward); the N flags are not needed since only tracers alive at
+            // the end carry an adjoint, and those were alive throughout
+            if (sgi != nseg - 1) {
+                cudaMemcpyAsync(a->y, a->ck + (size_t)(n0 / K) * 6 * nd, sizeof(double) * 6 * nd,
+                                cudaMemcpyDeviceToDevice, st);
+                cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
+                dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, n0, n1, K, nullptr, a->seg, n0);
+            }
             dust_reverse_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->seg, n0, n1, a->lam, a->active, a->part);
             const int per = Kseg * 4 * ng * 4;
             reduce_parts_kernel<<<(per + 255) / 256, 256, 0, st>>>(a->part, a->nblk, per, a->mu);
