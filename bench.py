@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -264,22 +265,7 @@ def run_ours(args, world, rank, local):
     # long-horizon error: err_steps steps of a smaller shard, mixed vs FP64
     err_long = None
     if args.err_steps > 0 and rank == 0:
-        small = synth.dusty_ring(n_dust=args.err_dust, n_plsml=args.n_plsml, seed=synth.SEED + 17)
-        sa = DeviceState.from_numpy(small.state)
-        sb = DeviceState.from_numpy(small.state)
-        eng.evolve(sa, small.n_grav, small.dt, args.err_steps, phys, F64)
-        eng.evolve(sb, small.n_grav, small.dt, args.err_steps, phys, MIX)
-        torch.cuda.synchronize()
-        ea = rel_err({k: getattr(sa, k) for k in ("x", "y", "z", "N")}, sb)
-        dm = torch.sqrt((sa.x[:small.n_grav] - sb.x[:small.n_grav]) ** 2 + (sa.y[:small.n_grav] - sb.y[:small.n_grav]) ** 2
-                        + (sa.z[:small.n_grav] - sb.z[:small.n_grav]) ** 2)
-        rm = torch.sqrt(sa.x[:small.n_grav] ** 2 + sa.y[:small.n_grav] ** 2 + sa.z[:small.n_grav] ** 2)
-        err_long = {"steps": args.err_steps, "n_dust": args.err_dust, "n_grav": small.n_grav,
-                    "dust_rel_pos_err_median": float(np.median(ea)),
-                    "dust_rel_pos_err_p90": float(np.quantile(ea, 0.9)),
-                    "dust_rel_pos_err_p99": float(np.quantile(ea, 0.99)),
-                    "dust_rel_pos_err_max": float(ea.max()),
-                    "massive_rel_pos_err_max": float((dm[1:] / rm[1:]).max().item())}
+        err_long = long_error_leg(eng, phys, args)
 
     # end to end through the C ABI with host buffers: per step, H2D of the state from
     # pinned memory, the step, D2H of the updated state
@@ -338,6 +324,104 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def massive_energy(st, ng):
+    """Total energy of the massive set, sum m v^2 / 2 - sum_{i<j} m_i m_j / r_ij, in the
+    state's units (masses carry the 4 pi^2, so the pair potential needs no G)."""
+    import torch
+    x = torch.stack([st.x[:ng], st.y[:ng], st.z[:ng]], 1)
+    v = torch.stack([st.vx[:ng], st.vy[:ng], st.vz[:ng]], 1)
+    m = st.m[:ng]
+    e = 0.5 * (m * (v * v).sum(1)).sum()
+    j = torch.arange(ng, device=x.device)
+    for i0 in range(0, ng, 512):
+        i1 = min(ng, i0 + 512)
+        d = torch.sqrt(((x[i0:i1, None, :] - x[None, :, :]) ** 2).sum(-1))
+        upper = j[None, :] > torch.arange(i0, i1, device=x.device)[:, None]
+        e = e - torch.where(upper, m[i0:i1, None] * m[None, :] / torch.where(upper, d, 1.0), 0.0).sum()
+    return e.item()
+
+
+def image_profiles(img, n_r=48, n_phi=36):
+    """Radial profile (flux in annuli about the image centre, out to the frame's half
+    width; beyond it the last annulus) and azimuthal profile (flux in n_phi sectors) of
+    one image."""
+    import torch
+    X, Y = img.shape
+    ii = torch.arange(X, device=img.device, dtype=torch.float64) - (X - 1) / 2.0
+    jj = torch.arange(Y, device=img.device, dtype=torch.float64) - (Y - 1) / 2.0
+    I, J = torch.meshgrid(ii, jj, indexing="ij")
+    rb = (torch.sqrt(I * I + J * J) / (0.5 * X) * n_r).long().clamp(max=n_r - 1).flatten()
+    pb = ((torch.atan2(J, I) + math.pi) / (2 * math.pi) * n_phi).long().clamp(max=n_phi - 1).flatten()
+    f = img.flatten()
+    radial = torch.zeros(n_r, dtype=torch.float64, device=img.device).index_add_(0, rb, f)
+    azim = torch.zeros(n_phi, dtype=torch.float64, device=img.device).index_add_(0, pb, f)
+    return radial, azim
+
+
+def long_error_leg(eng, phys, args):
+    """Mixed precision against FP64 over err_steps steps of a dusty-ring shard (all massive
+    bodies, err_dust grains): relative position error of grains and massive bodies, the
+    massive set's energy drift, and the error of the radial and azimuthal profiles of the
+    final images (1.25 um and 100 um, 512 x 512, 300 AU).  The same figures between two
+    FP64 forms (rsqrt-based vs the reference's m/RR/sqrt(RR) expression) give the floor
+    that FP64 rounding alone sets on this chaotic system."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_view
+    small = synth.ring_imaging(synth.dusty_ring(n_dust=args.err_dust, n_plsml=args.n_plsml, seed=synth.SEED + 17))
+    ng = small.n_grav
+    runs = {}
+    for name, prec, mode in (("fp64", abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED),
+                             ("mixed", abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED),
+                             ("fp64_ref_expr", abi.DDX_PREC_FP64, abi.DDX_MODE_REFERENCE)):
+        st = DeviceState.from_numpy(small.state)
+        e0 = massive_energy(st, ng)
+        eng.evolve(st, ng, small.dt, args.err_steps, phys, prec, mode)
+        torch.cuda.synchronize()
+        runs[name] = (st, (massive_energy(st, ng) - e0) / abs(e0))
+    ie = Engine(torch.cuda.current_device())
+    ie.set_size_table(**small.size_table)
+    o = small.optics
+    ie.set_optics(o["w"], o["in"], o["Qabs"], o["Qsca"], o["Qpfunc"], o["Td"], o["Rmin"], o["Rmax"])
+    view = make_view(**small.view)
+    imgs = {k: ie.image(st, ng, view, small.image_wj) for k, (st, _) in runs.items()}
+    torch.cuda.synchronize()
+    ie.close()
+
+    def compare(name):
+        a, b = runs["fp64"][0], runs[name][0]
+        live = (a.N[ng:] != 0) & (b.N[ng:] != 0)
+        d = torch.sqrt((a.x - b.x) ** 2 + (a.y - b.y) ** 2 + (a.z - b.z) ** 2)
+        r = torch.sqrt(a.x ** 2 + a.y ** 2 + a.z ** 2)
+        e = (d / r)[ng:][live].double().cpu().numpy()
+        em = (d / r)[1:ng].double().cpu().numpy()
+        out = {"dust_rel_pos_err_median": float(np.median(e)),
+               "dust_rel_pos_err_p90": float(np.quantile(e, 0.9)),
+               "dust_rel_pos_err_p99": float(np.quantile(e, 0.99)),
+               "dust_rel_pos_err_max": float(e.max()),
+               "massive_rel_pos_err_median": float(np.median(em)),
+               "massive_rel_pos_err_max": float(em.max()),
+               "massive_energy_drift": runs[name][1],
+               "dust_removed_differently": int((a.N[ng:] != b.N[ng:]).sum().item())}
+        prof = []
+        for k in range(len(small.image_wj)):
+            ra, pa = image_profiles(imgs["fp64"][k])
+            rb, pb = image_profiles(imgs[name][k])
+            prof.append({"wavelength_um": float(small.optics["w"][small.image_wj[k]] * 1e6),
+                         "radial_profile_err": float(((rb - ra).abs().max() / ra.abs().max()).item()),
+                         "azimuthal_profile_err": float(((pb - pa).abs().max() / pa.abs().max()).item()),
+                         "total_flux_rel_err": float(((rb.sum() - ra.sum()) / ra.sum()).abs().item())})
+        out["image"] = prof
+        return out
+
+    return {"steps": args.err_steps, "n_dust": args.err_dust, "n_grav": ng, "n_planets": small.phys["n_planets"],
+            "fp64_massive_energy_drift": runs["fp64"][1],
+            "mixed_vs_fp64": compare("mixed"),
+            "fp64_floor_ref_expr_vs_fp64": compare("fp64_ref_expr"),
+            "profile_error_definition": "max over bins of |profile - FP64 profile| / max FP64 profile; "
+                                        "48 annuli to the frame half-width, 36 sectors"}
 
 
 def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):

@@ -40,7 +40,8 @@ class State(C.Structure):
 class Phys(C.Structure):
     _fields_ = [("radQ", C.c_int), ("SWQ", C.c_int), ("FLQ", C.c_int),
                 ("Wz", C.c_double), ("Bstar", C.c_double), ("Rstar", C.c_double),
-                ("rho", C.c_double), ("vsw_AUyr", C.c_double), ("Rmin", C.c_double)]
+                ("rho", C.c_double), ("vsw_AUyr", C.c_double), ("Rmin", C.c_double),
+                ("n_planets", C.c_int)]
 
 
 class View(C.Structure):
@@ -83,6 +84,9 @@ SIGNATURES = [
     ("ddx_debug_pixels", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.POINTER(View),
                                    C.c_void_p, C.c_void_p]),
     ("ddx_debug_exact_pixel_count", C.c_ulonglong, [C.c_void_p]),
+    ("ddx_det_step", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_void_p, C.c_int,
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                               C.c_void_p]),
     ("ddx_sync_status", C.c_int, [C.c_void_p, C.c_void_p]),
     ("ddx_debug_lose_tile_copy", C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong]),
     ("ddx_probe_fma_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

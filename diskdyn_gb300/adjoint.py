@@ -112,17 +112,7 @@ def adjoint_system(n_dust=262144, xsize=512, ysize=512, n_steps=2000, seed=synth
     a 512 x 512 image, 300 AU across, at 30 deg inclination, at 1.25 um (scattered light)
     and 100 um (thermal)."""
     s = synth.dusty_ring(n_dust=n_dust, n_plsml=0, seed=seed, n_steps=n_steps)
-    n_grid = len(s.size_table["size"])
-    opt = synth.hg_optics(n_grid=n_grid, n_wav=200, dist=10 * synth.PC, L=8.7, Rmin=0.1, Rmax=400.0,
-                          Teff=7500.0, Rstar=2.0 * synth.RSun, smin=s.size_table["size"][0],
-                          smax=s.size_table["size"][-1])
-    opt["size"] = s.size_table["size"]
-    w = opt["w"]
-    wj = [int(np.argmin(abs(w - 1.25e-6))), int(np.argmin(abs(w - 100e-6)))]
-    s.optics = opt
-    s.view = dict(dist=10 * synth.PC, fov=300.0, PA=0.0, inc=math.radians(30.0), longitude=0.0,
-                  xsize=xsize, ysize=ysize)
-    s.image_wj = wj
+    synth.ring_imaging(s, xsize, ysize)
     s.name = "adjoint_ring"
     return s
 

@@ -19,7 +19,9 @@ OBJ = PKG / "_build"
 LIB = PKG / "libddx.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+# Host code without FP contraction, so host-side arithmetic (ddx_det_step) rounds the same
+# on x86-64 and on Arm, like the reference's host code built for x86-64.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-diag-suppress", "1444", "-I", str(ROOT / "include")]
 
 
@@ -52,6 +54,13 @@ def build(verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
     srcs = sorted(CSRC.glob("*.cu"))
     hmt = _headers_mtime()
+    # objects built with other flags are stale
+    stamp = OBJ / "flags.txt"
+    flags = " ".join(ARCH + NVCC_FLAGS)
+    if not stamp.exists() or stamp.read_text() != flags:
+        for o in OBJ.glob("*.o"):
+            o.unlink()
+        stamp.write_text(flags)
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(lambda s: _compile(s, hmt, verbose), srcs))
     newest = max(o.stat().st_mtime for o in objs)

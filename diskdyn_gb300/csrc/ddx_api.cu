@@ -31,6 +31,7 @@ struct ddx_ctx {
     unsigned long long inject_wait_ns = 0;
     CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
     AdjointScratch* adjoint = nullptr;          // trajectory checkpoints of the last adjoint forward
+    DetStepScratch* detstep = nullptr;          // body scan of ddx_det_step
 };
 
 namespace {
@@ -87,7 +88,9 @@ bool state_ok(const ddx_state* s) {
 int make_step_args(const ddx_phys* p, int n_grav, int n_dust, double dt, int mode, StepArgs& a) {
     if (!p || n_grav < 1 || n_dust < 0) return DDX_ERR_ARG;
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
+    if (p->n_planets < 0 || p->n_planets > n_grav) return DDX_ERR_ARG;
     a.n_grav = n_grav;
+    a.n_exact = p->n_planets > 1 ? p->n_planets : 1;
     a.n_dust = n_dust;
     a.dt = dt;
     a.dt2 = dt * 0.5;          // src/grid.cu:711,716 pass dt*0.5
@@ -190,6 +193,7 @@ int ddx_destroy(ddx_ctx* c) {
     cudaFree(c->sed_partial); cudaFree(c->counters); cudaFree(c->status);
     collide_free(c->collide);
     adjoint_free(c->adjoint);
+    det_step_free(c->detstep);
     delete c;
     return DDX_OK;
 }
@@ -318,6 +322,37 @@ int ddx_collide(ddx_ctx* c, const ddx_state* s, int i0, int i1, double h, int* p
     cudaSetDevice(c->device);
     return collide_run(c->collide, *s, i0, i1, h, reinterpret_cast<int2*>(pairs), cap, n_pairs,
                        (cudaStream_t)stream);
+}
+
+int ddx_det_step(ddx_ctx* c, const ddx_state* s, int n_grav, int n_step, const double* disk_Rin,
+                 int n_disks, const double* blob_a, const double* blob_ecc, const double* blob_sigma,
+                 int n_blobs, double* dt, void* stream) {
+    if (!c || !s || !s->x || !s->y || !s->z || !s->m || !dt || n_grav < 1 || n_step < 1 || n_disks < 0 ||
+        n_blobs < 0 || (n_disks > 0 && !disk_Rin) || (n_blobs > 0 && (!blob_a || !blob_ecc || !blob_sigma)))
+        return DDX_ERR_ARG;
+    cudaSetDevice(c->device);
+    std::vector<double> rr, mi;
+    double m0 = 0.0;
+    const int r = det_step_scan(c->detstep, *s, n_grav, (cudaStream_t)stream, rr, mi, m0);
+    if (r) return r;
+    // src/grid.cu:315-341, term by term (this file is compiled without FP contraction)
+    const double PI2 = 6.28318530717958623200;   // src/ddyn.cuh:29
+    double dtdynmin = 1e137;
+    for (size_t k = 0; k < rr.size(); ++k) {
+        const double R = pow(rr[k], 3.0 / 2.0);
+        const double dttmp = PI2 * sqrt(R / (m0 + mi[k])) / n_step;
+        if (dttmp < dtdynmin) dtdynmin = dttmp;
+    }
+    for (int i = 0; i < n_disks; ++i) {
+        const double dttmp = PI2 * sqrt(disk_Rin[i] / (m0)) / n_step;
+        if (dttmp < dtdynmin) dtdynmin = dttmp;
+    }
+    for (int i = 0; i < n_blobs; ++i) {
+        const double dttmp = PI2 * sqrt((blob_a[i] * (1.0 - blob_ecc[i]) - blob_sigma[i]) / (m0)) / n_step;
+        if (dttmp < dtdynmin) dtdynmin = dttmp;
+    }
+    *dt = dtdynmin;
+    return DDX_OK;
 }
 
 int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,

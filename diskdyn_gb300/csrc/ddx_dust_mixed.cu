@@ -1,10 +1,10 @@
 // Mixed-precision RK4 of the dust tracers on sm_103a (src/gpu_functions.cu:627-943).
 //
 // FP64: tracer state, stage positions and velocities, the star term (reduced gravity,
-// PR + stellar-wind drag, Lorentz force) and the RK4 combination.  FP32: the gravity of
-// the perturbing bodies, on hi/lo split positions so the separation keeps FP32 relative
-// precision at any distance from the star, with plain sums over spans of 16 sources and a
-// Kahan sum across spans.
+// PR + stellar-wind drag, Lorentz force), the gravity of the planets (bodies
+// 1..n_exact-1) and the RK4 combination.  FP32: the gravity of the planetesimals, on
+// hi/lo split positions so the separation keeps FP32 relative precision at any distance
+// from the star, with plain sums over spans of 16 sources and a Kahan sum across spans.
 //
 // Blackwell mapping:
 //  - perturbers arrive as 64-byte pair records (two bodies per record, one quantity of
@@ -126,7 +126,7 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
         }
     }
 
-    const int npairs = pair_count(ng);
+    const int npairs = pair_count(ng - a.n_exact);
     const int ntiles = (npairs + kTilePairs - 1) / kTilePairs;
     const int G = 4 * ntiles;                       // tiles over all four stages
     const uint32_t mb[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
@@ -184,6 +184,16 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
                            kx, ky, kz)) {
                 alive = false; removed = 1; removed_stage = st;
             }
+        }
+        // the planets, in FP64
+        for (int j = 1; alive && j < a.n_exact; ++j) {
+            const Body p = ms.P[st * ms.cap + j];
+            const double ex = p.x - xt, ey = p.y - yt, ez = p.z - zt;
+            const double RR = ex * ex + ey * ey + ez * ez;
+            if (RR == 0.0) { alive = false; removed = 2; removed_stage = st; break; }
+            const double ri = rsqrt(RR);
+            const double f = p.m * (ri * ri * ri);
+            kx = fma(f, ex, kx); ky = fma(f, ey, ky); kz = fma(f, ez, kz);
         }
         float xh, xl, yh, yl, zh, zl;
         split_hilo(xt, xh, xl); split_hilo(yt, yh, yl); split_hilo(zt, zh, zl);

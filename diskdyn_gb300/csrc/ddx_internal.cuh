@@ -5,6 +5,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <vector>
 #include "../../include/diskdyn_gb300.h"
 
 namespace ddx {
@@ -27,6 +28,7 @@ struct __align__(16) SizeBin {
 // Scalars of one RK4 step, passed by value to the kernels.
 struct StepArgs {
     int    n_grav, n_dust;
+    int    n_exact;         // bodies 0..n_exact-1 (star, planets) act in FP64 in the mixed path
     double dt, dt2, dt6;    // dt, dt/2, dt/6 formed exactly as the reference forms them
     int    SWQ, FLQ;
     double Wz, Bstar, Rstar, vswAU, Rmin;
@@ -57,10 +59,10 @@ struct __align__(16) BodyPair {
 
 constexpr int kPairSpan = 8;     // pair records per plain-FP32 partial sum (16 sources)
 
-// Pair records per stage needed for n_grav bodies: sources 1..n_grav-1 in pairs, padded
-// with zero-mass records to a multiple of kPairSpan.
-__host__ __device__ constexpr int pair_count(int n_grav) {
-    const int np = n_grav / 2;   // ceil((n_grav - 1) / 2)
+// Pair records per stage for n_src FP32 sources (bodies n_exact..n_grav-1) in pairs,
+// padded with zero-mass records to a multiple of kPairSpan.
+__host__ __device__ constexpr int pair_count(int n_src) {
+    const int np = (n_src + 1) / 2;
     return (np + kPairSpan - 1) / kPairSpan * kPairSpan;
 }
 
@@ -140,4 +142,18 @@ struct CollideScratch;   // ddx_collide.cu
 int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double h, int2* pairs,
                 long long cap, long long* n_pairs, cudaStream_t st);
 void collide_free(CollideScratch*& cs);
+
+// ddx_detstep.cu: the massive bodies that can set the time step, with their squared
+// distance to the star (formed without contraction) and mass; synchronizes the stream.
+constexpr int kDetCandidates = 256;
+struct DetStepScratch {
+    double* rr = nullptr;
+    unsigned long long* kmin = nullptr;
+    int* count = nullptr;
+    int* cand = nullptr;
+    int cap_bodies = 0;
+};
+int det_step_scan(DetStepScratch*& d, const ddx_state& s, int n_grav, cudaStream_t st,
+                  std::vector<double>& rr, std::vector<double>& mi, double& m0);
+void det_step_free(DetStepScratch*& d);
 }  // namespace ddx

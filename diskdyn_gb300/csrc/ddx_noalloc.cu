@@ -82,6 +82,7 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     if (n_grav < 1 || n_dust < 0 || n_grid < 1 || !beta || !betasw || !q) return DDX_ERR_ARG;
     if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
+    if (p->n_planets < 0 || p->n_planets > n_grav) return DDX_ERR_ARG;
     if (n_grav > DDX_NOALLOC_MAX_GRAV || n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
     if (cudaSetDevice(device) != cudaSuccess) return DDX_ERR_CUDA;
     unsigned char* base = nullptr;
@@ -102,6 +103,7 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
 
     StepArgs a;
     a.n_grav = n_grav;
+    a.n_exact = p->n_planets > 1 ? p->n_planets : 1;
     a.n_dust = n_dust;
     a.dt = dt;
     a.dt2 = dt * 0.5;

@@ -24,22 +24,23 @@ namespace ddx {
 
 constexpr float kFarAway = 1.0e18f;  // padding source position, AU (mass 0)
 
-// Body i >= 1 into its half of pair record (i-1)/2 of a stage.
-__device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, int i, const float4 h,
+// FP32 source q = i - n_exact (body i >= n_exact) into its half of pair record q/2 of a
+// stage.
+__device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, int q, const float4 h,
                                                 const float4 l) {
-    BodyPair* r = ms.PP + (size_t)stage * ms.pcap + ((i - 1) >> 1);
-    const int k = (i - 1) & 1;
+    BodyPair* r = ms.PP + (size_t)stage * ms.pcap + (q >> 1);
+    const int k = q & 1;
     r->hx[k] = h.x; r->hy[k] = h.y; r->hz[k] = h.z; r->m[k] = h.w;
     r->lx[k] = l.x; r->ly[k] = l.y; r->lz[k] = l.z; r->pad[k] = 0.f;
 }
 
-// Zero-mass, far-away filler for the slots past the last perturbing body, so the dust
-// kernel always processes whole spans of kPairSpan records.
-__device__ __forceinline__ void store_pair_padding(MassiveScratch& ms, int n_grav) {
-    const int np = pair_count(n_grav);
+// Zero-mass, far-away filler for the slots past the last FP32 source, so the dust kernel
+// always processes whole spans of kPairSpan records.
+__device__ __forceinline__ void store_pair_padding(MassiveScratch& ms, int n_src) {
+    const int np = pair_count(n_src);
     const float4 h = make_float4(kFarAway, kFarAway, kFarAway, 0.f), l = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int stage = 0; stage < 4; ++stage)
-        for (int i = n_grav; i <= 2 * np; ++i) store_pair_slot(ms, stage, i, h, l);
+        for (int q = n_src; q < 2 * np; ++q) store_pair_slot(ms, stage, q, h, l);
 }
 
 // P1 = x, P2 = x + v dt/2 (src/gpu_functions.cu:90-99, 219-230).
@@ -56,11 +57,11 @@ __global__ void massive_prepare_kernel(ddx_state s, StepArgs a, MassiveScratch m
         split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
         h.w = (float)m; l.w = 0.f;
         ms.Phi[0 * ms.cap + i] = h; ms.Plo[0 * ms.cap + i] = l;
-        if (i > 0) store_pair_slot(ms, 0, i, h, l);
+        if (i >= a.n_exact) store_pair_slot(ms, 0, i - a.n_exact, h, l);
         split_hilo(x2, h.x, l.x); split_hilo(y2, h.y, l.y); split_hilo(z2, h.z, l.z);
         ms.Phi[1 * ms.cap + i] = h; ms.Plo[1 * ms.cap + i] = l;
-        if (i > 0) store_pair_slot(ms, 1, i, h, l);
-        else store_pair_padding(ms, a.n_grav);
+        if (i >= a.n_exact) store_pair_slot(ms, 1, i - a.n_exact, h, l);
+        if (i == 0) store_pair_padding(ms, a.n_grav - a.n_exact);
     }
 }
 
@@ -107,10 +108,11 @@ __device__ __forceinline__ void pair32(const float4 hi, const float4 li, const f
 
 // One warp per target body i, lanes stride over the sources, fixed-order butterfly
 // reduction (deterministic).  Evaluates the accelerations at two stages sa, sb at once.
-// In the mixed path every pair that involves the star (index 0) stays FP64; the other
-// pairs run in FP32 with a per-lane Kahan sum.
+// In the mixed path the star's own acceleration and every pull of the star or a planet
+// (sources 0..n_exact-1) stay FP64; the pulls of the planetesimals run in FP32 with a
+// per-lane Kahan sum.
 template <int PREC>
-__device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms, int ng, int i,
+__device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms, int ng, int n_exact, int i,
                                                          int sa, int sb, double a_out[6]) {
     const int lane = threadIdx.x & 31;
     double ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
@@ -129,7 +131,7 @@ __device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms
         const float4 hb = ms.Phi[sb * ms.cap + i], lb = ms.Plo[sb * ms.cap + i];
         for (int j = lane; j < ng; j += 32) {
             if (j == i) continue;
-            if (i == 0 || j == 0) {
+            if (i == 0 || j < n_exact) {
                 pair64(pa, ms.P[sa * ms.cap + j], ax, ay, az);
                 pair64(pb, ms.P[sb * ms.cap + j], bx, by, bz);
             } else {
@@ -151,14 +153,14 @@ __device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms
 }
 
 __device__ __forceinline__ void store_stage_pos(MassiveScratch& ms, int stage, int i, double x,
-                                                double y, double z, double m, int prec) {
+                                                double y, double z, double m, int prec, int n_exact) {
     ms.P[stage * ms.cap + i] = make_body(x, y, z, m);
     if (prec == DDX_PREC_MIXED) {
         float4 h, l;
         split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
         h.w = (float)m; l.w = 0.f;
         ms.Phi[stage * ms.cap + i] = h; ms.Plo[stage * ms.cap + i] = l;
-        if (i > 0) store_pair_slot(ms, stage, i, h, l);
+        if (i >= n_exact) store_pair_slot(ms, stage, i - n_exact, h, l);
     }
 }
 
@@ -169,7 +171,7 @@ __global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.n_grav) return;  // warp-uniform
     double acc[6];
-    massive_two_stage_accel<PREC>(ms, a.n_grav, i, 0, 1, acc);
+    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 0, 1, acc);
     if ((threadIdx.x & 31) != 0) return;
     const int c = ms.cap;
     double* A = ms.A;
@@ -184,8 +186,8 @@ __global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     const double k4x = x + k3rx * a.dt, k4y = y + k3ry * a.dt, k4z = z + k3rz * a.dt;
     R[(0 * 3 + 0) * c + i] = k2rx; R[(0 * 3 + 1) * c + i] = k2ry; R[(0 * 3 + 2) * c + i] = k2rz;
     R[(1 * 3 + 0) * c + i] = k3rx; R[(1 * 3 + 1) * c + i] = k3ry; R[(1 * 3 + 2) * c + i] = k3rz;
-    store_stage_pos(ms, 2, i, k3x, k3y, k3z, m, PREC);
-    store_stage_pos(ms, 3, i, k4x, k4y, k4z, m, PREC);
+    store_stage_pos(ms, 2, i, k3x, k3y, k3z, m, PREC, a.n_exact);
+    store_stage_pos(ms, 3, i, k4x, k4y, k4z, m, PREC, a.n_exact);
 }
 
 // Pass 2: A3 at P3, A4 at P4; R4; final combination (src/gpu_functions.cu:613-625).
@@ -195,7 +197,7 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.n_grav) return;
     double acc[6];
-    massive_two_stage_accel<PREC>(ms, a.n_grav, i, 2, 3, acc);
+    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 2, 3, acc);
     if ((threadIdx.x & 31) != 0) return;
     const int c = ms.cap;
     double* A = ms.A;

@@ -70,9 +70,9 @@ class DeviceState:
 
 
 def make_phys(radQ=0, SWQ=0, FLQ=0, Wz=0.0, Bstar=0.0, Rstar=0.0, rho=0.0, vsw_AUyr=1.0,
-              Rmin=0.0) -> abi.Phys:
+              Rmin=0.0, n_planets=1) -> abi.Phys:
     return abi.Phys(int(radQ), int(SWQ), int(FLQ), float(Wz), float(Bstar), float(Rstar),
-                    float(rho), float(vsw_AUyr), float(Rmin))
+                    float(rho), float(vsw_AUyr), float(Rmin), int(n_planets))
 
 
 def make_view(dist, fov, PA, inc, longitude, xsize, ysize) -> abi.View:
@@ -179,6 +179,23 @@ class Engine:
                                        C.c_void_p(out.data_ptr()), cap, C.byref(n), sh), "ddx_collide")
         self.last_pair_count = n.value
         return out[:min(cap, n.value)]
+
+    def det_step(self, st: DeviceState, n_grav: int, n_step: int, disk_Rin=(), blobs=(), stream=None) -> float:
+        """Time step of a run with n_step steps per orbit (Grid::det_step): the shortest
+        of the massive bodies' Kepler periods about the star, the disks' sqrt(Rin/m0) terms
+        and the blobs' sqrt((a(1-ecc)-sigma)/m0) terms, times 2 pi / n_step.  blobs is a
+        sequence of (a, ecc, sigma)."""
+        rin = np.ascontiguousarray(disk_Rin, dtype=np.float64)
+        bl = np.ascontiguousarray(np.reshape(blobs, (-1, 3)), dtype=np.float64)
+        ba, be, bs = (np.ascontiguousarray(bl[:, k]) for k in range(3))
+        dt = C.c_double(0.0)
+
+        def ptr(a):
+            return C.c_void_p(a.ctypes.data) if a.size else None
+        abi.check(self.lib.ddx_det_step(self.ctx, C.byref(st._abi), int(n_grav), int(n_step), ptr(rin), rin.size,
+                                        ptr(ba), ptr(be), ptr(bs), ba.size, C.byref(dt),
+                                        C.c_void_p(_stream_handle(stream))), "ddx_det_step")
+        return dt.value
 
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a

@@ -179,7 +179,7 @@ def solar_like(n_dust: int = 16384, seed: int = SEED, with_ids: bool = False, n_
     state = _pack(px, py, pz, pvx, pvy, pvz, pm, dx, dy, dz, dvx, dvy, dvz,
                   np.zeros(n_dust), np.ones(n_dust), did)
     phys = dict(radQ=0, SWQ=0, FLQ=0, Wz=0.0, Bstar=0.0, Rstar=RSun / AU, rho=2700.0,
-                vsw_AUyr=400e3 * YEAR / AU, Rmin=0.05)
+                vsw_AUyr=400e3 * YEAR / AU, Rmin=0.05, n_planets=n_pl + 1)
     return System("solar_like", n_pl + 1, state, 0.05, 1000, phys, _empty_size_table(n_bins),
                   meta={"seed": seed})
 
@@ -245,7 +245,7 @@ def dusty_ring(n_dust: int = 1048576, n_plsml: int = 4096, seed: int = SEED, n_s
                   np.concatenate([pm, mm]), dx, dy, dz, dvx, dvy, dvz, dm, np.ones(n_dust), did)
     dt = math.sqrt(120.0 ** 3 / Ms) / 300.0
     phys = dict(radQ=1, SWQ=1, FLQ=0, Wz=365.2422 / 25.0, Bstar=0.0, Rstar=2.0 * RSun / AU,
-                rho=rho, vsw_AUyr=vsw * YEAR / AU, Rmin=0.5)
+                rho=rho, vsw_AUyr=vsw * YEAR / AU, Rmin=0.5, n_planets=3)
     size_table = {"size": sbin, "beta": beta, "betasw": betasw,
                   "q": np.zeros(n_grid, np.float32)}
     return System("dusty_ring", 3 + n_plsml, state, dt, n_steps, phys, size_table,
@@ -272,6 +272,24 @@ def hg_optics(n_grid=64, n_theta=181, n_wav=200, wmin=0.5e-6, wmax=850e-6, Teff=
     size = np.logspace(np.log10(smin), np.log10(smax), n_grid)
     return {"w": w, "in": influx, "Qabs": Qabs, "Qsca": Qsca, "Qpfunc": Qp, "Td": Td,
             "Rmin": Rmin, "Rmax": Rmax, "size": size, "g": gg}
+
+
+def ring_imaging(s: System, xsize=512, ysize=512) -> System:
+    """Attach optics and a view to a `dusty_ring` system: HG tables on its grains' size
+    bins, grey grains at T = 278.3 L^(1/4) (r/AU)^(-1/2) K, a 7500 K star of 2 Rsun at
+    10 pc; an image 300 AU across at 30 deg inclination, at 1.25 um (scattered light) and
+    100 um (thermal)."""
+    n_grid = len(s.size_table["size"])
+    opt = hg_optics(n_grid=n_grid, n_wav=200, dist=10 * PC, L=8.7, Rmin=0.1, Rmax=400.0,
+                    Teff=7500.0, Rstar=2.0 * RSun, smin=s.size_table["size"][0],
+                    smax=s.size_table["size"][-1])
+    opt["size"] = s.size_table["size"]
+    w = opt["w"]
+    s.optics = opt
+    s.view = dict(dist=10 * PC, fov=300.0, PA=0.0, inc=np.deg2rad(30.0), longitude=0.0,
+                  xsize=xsize, ysize=ysize)
+    s.image_wj = [int(np.argmin(abs(w - 1.25e-6))), int(np.argmin(abs(w - 100e-6)))]
+    return s
 
 
 def imaging(n_dust: int = 4194304, seed: int = SEED, xsize=1024, ysize=1024, n_img=10) -> System:

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define DDX_ABI_VERSION 1
+#define DDX_ABI_VERSION 2
 
 /* Status codes.  The reference exits the process instead (src/error.cu:75-91,
  * src/ddyn.cuh:400-408). */
@@ -69,6 +69,12 @@ typedef struct {
     double rho;             /* bulk density, kg/m^3 (unused by the force; kept for parity) */
     double vsw_AUyr;        /* stellar-wind speed, AU/yr */
     double Rmin;            /* sublimation radius, AU */
+    int    n_planets;       /* star + planets, the leading massive bodies (cconfig.n_planets:
+                               the star is planet 0, src/read_in.cu:62-65,94).
+                               DDX_PREC_MIXED computes the gravity of bodies
+                               0..n_planets-1 in FP64 and only that of the planetesimals
+                               n_planets..n_grav-1 in FP32.  0 <= n_planets <= n_grav;
+                               0 counts as 1 (the star alone). */
 } ddx_phys;
 
 /* Observer geometry, in the units the reference passes to calc_flux_driver
@@ -181,6 +187,19 @@ int ddx_sed(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
  * repeated with a larger buffer.  Synchronises `stream`.  At most 2^30 tracers. */
 int ddx_collide(ddx_ctx *ctx, const ddx_state *s, int i0, int i1, double h, int *pairs,
                 long long cap, long long *n_pairs, void *stream);
+
+/* Time step of a run; replaces Grid::det_step (src/grid.cu:312-342), called once at the
+ * start of Grid::evolve (src/grid.cu:349).  With n_step steps per orbit:
+ *   dt = min( 2 pi sqrt(pow(|x_i - x_0|^2, 3/2) / (m_0 + m_i)) / n_step, i = 1..n_grav-1,
+ *             2 pi sqrt(disk_Rin[k] / m_0) / n_step,
+ *             2 pi sqrt((blob_a[k] (1 - blob_ecc[k]) - blob_sigma[k]) / m_0) / n_step )
+ * and 1e137 when there is no term, the reference's expressions and rounding to the bit
+ * (the disk and blob terms take sqrt(R / m_0), not R^(3/2), as the reference does).  The
+ * body scan runs on the GPU over the device state; the disk and blob arrays are host
+ * pointers (configuration data) and *dt is written on the host.  Synchronises `stream`. */
+int ddx_det_step(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_step, const double *disk_Rin,
+                 int n_disks, const double *blob_a, const double *blob_ecc, const double *blob_sigma,
+                 int n_blobs, double *dt, void *stream);
 
 /* Discrete adjoint of the trajectory and image (no counterpart in the reference).
  *

@@ -157,6 +157,19 @@ def dust_temp(w, influx, Qabs, dist, Rmax_AU):
     return Td, rmin.value, rmax.value
 
 
+def det_step(arrays: dict, n_grav: int, n_step: int, disk_Rin=(), blobs=()) -> float:
+    """Grid::det_step (src/grid.cu:312-342); blobs is a sequence of (a, ecc, sigma)."""
+    xs = [np.ascontiguousarray(arrays[k][:max(n_grav, 1)], np.float64) for k in ("x", "y", "z", "m")]
+    rin = np.ascontiguousarray(disk_Rin, np.float64)
+    bl = np.ascontiguousarray(np.reshape(blobs, (-1, 3)), np.float64)
+    ba, be, bs = (np.ascontiguousarray(bl[:, k]) for k in range(3))
+    f = lib().ora_det_step
+    f.restype = C.c_double
+    f.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 3 + [C.c_int]
+    return f(*[_ptr(a) for a in xs], int(n_grav), int(n_step), _ptr(rin), rin.size, _ptr(ba), _ptr(be),
+             _ptr(bs), ba.size)
+
+
 def collide(arrays: dict, i0: int, i1: int, h: float, method: str = "brute", cap: int | None = None):
     """Collision pairs (m, 2) of live tracers i < j in [i0, i1) closer than h, (i, j) order."""
     st, os_ = host_state(arrays)

@@ -464,6 +464,37 @@ int ora_dust_temp(int n_grid, int n_wav, const double *w, const double *in, cons
 }
 
 /* ------------------------------------------------------------------------------------
+ * Time step: Grid::det_step, src/grid.cu:312-342 (PI2 from src/ddyn.cuh:29), over host
+ * arrays x, y, z, m of the massive bodies; disks give Rin, blobs (a, ecc, sigma).
+ * ------------------------------------------------------------------------------------ */
+double ora_det_step(const double *x, const double *y, const double *z, const double *m, int n_grav,
+                    int n_step, const double *disk_Rin, int n_disks, const double *blob_a,
+                    const double *blob_ecc, const double *blob_sigma, int n_blobs) {
+    const double PI2 = 6.28318530717958623200;
+    double dtdynmin = 1e137;
+    if (n_grav > 1) {
+        double R = pow((x[1] - x[0]) * (x[1] - x[0]) + (y[1] - y[0]) * (y[1] - y[0]) +
+                           (z[1] - z[0]) * (z[1] - z[0]), 3.0 / 2.0);
+        dtdynmin = PI2 * sqrt(R / (m[0] + m[1])) / n_step;
+        for (int i = 2; i < n_grav; i++) {
+            R = pow((x[i] - x[0]) * (x[i] - x[0]) + (y[i] - y[0]) * (y[i] - y[0]) +
+                        (z[i] - z[0]) * (z[i] - z[0]), 3.0 / 2.0);
+            double dttmp = PI2 * sqrt(R / (m[0] + m[i])) / n_step;
+            if (dttmp < dtdynmin) dtdynmin = dttmp;
+        }
+    }
+    for (int i = 0; i < n_disks; i++) {
+        double dttmp = PI2 * sqrt(disk_Rin[i] / (m[0])) / n_step;
+        if (dttmp < dtdynmin) dtdynmin = dttmp;
+    }
+    for (int i = 0; i < n_blobs; i++) {
+        double dttmp = PI2 * sqrt((blob_a[i] * (1.0 - blob_ecc[i]) - blob_sigma[i]) / (m[0])) / n_step;
+        if (dttmp < dtdynmin) dtdynmin = dttmp;
+    }
+    return dtdynmin;
+}
+
+/* ------------------------------------------------------------------------------------
  * Collision pairs (no reference counterpart; the criterion is the one documented for
  * ddx_collide): live tracers i < j of [i0, i1) with
  *   (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2, left to right, no contraction.

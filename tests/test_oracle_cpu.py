@@ -154,3 +154,19 @@ def test_dust_temperature_table_follows_equilibrium_scaling():
     k = np.searchsorted(R, 1.0)
     assert Td[0, k] * math.sqrt(R[k]) == pytest.approx(278.6, rel=0.02)
     assert Td[0, 0] == pytest.approx(2000.0, rel=0.01)   # Rmin is the sublimation radius
+
+
+def test_det_step_is_the_shortest_kepler_period_over_n_step():
+    # Grid::det_step: 2 pi sqrt(r^3 / (m0 + mi)) / n_step with masses carrying 4 pi^2 is
+    # the orbital period in years over n_step; the innermost body sets it
+    st = two_body(a=1.0, mp=0.0)
+    st = {k: np.concatenate([v, v[1:]]) for k, v in st.items()}
+    st["x"][2] = 4.0                                    # a second body at 4 AU
+    dt = oc.det_step(st, 3, 100)
+    assert dt == pytest.approx(0.01, rel=1e-15)
+    # disks and blobs enter as 2 pi sqrt(R / m0) / n_step, the reference's expression
+    assert oc.det_step(st, 3, 100, disk_Rin=[0.5]) == pytest.approx(2 * math.pi * math.sqrt(0.5 / synth.GRAV) / 100,
+                                                                    rel=1e-15)
+    assert oc.det_step(st, 3, 100, blobs=[(2.0, 0.5, 0.5)]) == pytest.approx(
+        2 * math.pi * math.sqrt(0.5 / synth.GRAV) / 100, rel=1e-15)
+    assert oc.det_step(st, 1, 100) == 1e137           # a lone star, no disk: the initial value
