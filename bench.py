@@ -578,7 +578,8 @@ def run_imaging(args, world, rank, local):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     out = {}
-    for prec, name in ((abi.DDX_PREC_FP64, "fp64"),):
+    results = {}
+    for prec, name in ((abi.DDX_PREC_FP64, "fp64"), (abi.DDX_PREC_MIXED, "mixed")):
         for _ in range(args.warmup):
             eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=prec)
             eng.sed(st, s.n_grav, view, out=Fs, precision=prec)
@@ -603,6 +604,16 @@ def run_imaging(args, world, rank, local):
                      "sed_particle_wavelengths_per_s": n * len(o["w"]) / t_sed,
                      "image_algorithmic_GBps": bytes_img / t_img / 1e9,
                      "image_hbm_frac": bytes_img / t_img / 1e9 / measured_peaks().get("hbm_gbs", 6782.1)}
+        results[name] = (F.clone(), Fs.clone())
+    (F64, S64), (Fm, Sm) = results["fp64"], results["mixed"]
+    lit = F64 != 0
+    out["mixed_vs_fp64"] = {
+        "lit_pixels_identical": bool(torch.equal(lit, Fm != 0)),
+        "image_pixel_rel_err_max": float(((Fm - F64).abs()[lit] / F64[lit].abs()).max().item()),
+        "image_total_flux_rel_err_max": float(((Fm.sum((1, 2)) - F64.sum((1, 2))).abs() / F64.sum((1, 2))).max().item()),
+        "sed_rel_err_max": float(((Sm - S64).abs() / S64.abs()).max().item()),
+        "image_speedup": out["fp64"]["image_ms"] / out["mixed"]["image_ms"],
+        "sed_speedup": out["fp64"]["sed_ms"] / out["mixed"]["sed_ms"]}
     line = {"metric": "imaging particle-wavelengths/s", "workload": "imaging", "n_particles": n,
             "n_img": n_img, "n_wav": len(o["w"]), "image": [s.view["xsize"], s.view["ysize"]],
             "results": out, "l2": "flushed between timed calls"}

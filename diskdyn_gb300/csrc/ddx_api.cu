@@ -22,6 +22,9 @@ struct ddx_ctx {
     OpticsDev* od_dev = nullptr;
     double *w = nullptr, *in = nullptr, *Qabs = nullptr, *Qsca = nullptr, *Qp = nullptr,
            *Td = nullptr, *lQp = nullptr, *lTd = nullptr, *w5 = nullptr;
+    float2* lQp32p = nullptr;                   // FP32 log tables (mixed photometry)
+    float* lTd32 = nullptr;
+    PhotoConst photo{};                         // per-call FP32 coefficients, max(n_wav, kMaxImages) slots
     ViewConst* vc = nullptr;
     double* sed_partial = nullptr;
     int sed_partial_cap = 0;
@@ -137,7 +140,12 @@ int enqueue_step(ddx_ctx* c, const ddx_state& s, StepArgs a, int precision, cuda
 void free_optics(ddx_ctx* c) {
     cudaFree(c->w); cudaFree(c->in); cudaFree(c->Qabs); cudaFree(c->Qsca); cudaFree(c->Qp);
     cudaFree(c->Td); cudaFree(c->lQp); cudaFree(c->lTd); cudaFree(c->w5);
+    cudaFree(c->lQp32p); cudaFree(c->lTd32);
+    cudaFree(c->photo.A); cudaFree(c->photo.C2); cudaFree(c->photo.esh);
     c->w = c->in = c->Qabs = c->Qsca = c->Qp = c->Td = c->lQp = c->lTd = c->w5 = nullptr;
+    c->lQp32p = nullptr;
+    c->lTd32 = nullptr;
+    c->photo = PhotoConst{};
     c->optics_set = false;
 }
 
@@ -230,9 +238,12 @@ int ddx_set_optics(ddx_ctx* c, int n_grid, int n_wav, int n_theta, const double*
     free_optics(c);
     const size_t nq = (size_t)n_grid * n_theta * n_wav, nw = (size_t)n_grid * n_wav,
                  nt = (size_t)n_grid * DDX_NR;
+    const size_t nslot = (size_t)(n_wav > kMaxImages ? n_wav : kMaxImages);
     if (dalloc(&c->w, n_wav) || dalloc(&c->in, n_wav) || dalloc(&c->Qabs, nw) || dalloc(&c->Qsca, nw) ||
         dalloc(&c->Qp, nq) || dalloc(&c->Td, nt) || dalloc(&c->lQp, nq) || dalloc(&c->lTd, nt) ||
-        dalloc(&c->w5, n_wav)) {
+        dalloc(&c->w5, n_wav) || dalloc(&c->lQp32p, (size_t)n_grid * (n_theta - 1) * n_wav) ||
+        dalloc(&c->lTd32, nt) || dalloc(&c->photo.A, n_grid * nslot) ||
+        dalloc(&c->photo.C2, nslot) || dalloc(&c->photo.esh, nslot)) {
         free_optics(c);
         cudaGetLastError();
         return DDX_ERR_NOMEM;
@@ -248,6 +259,7 @@ int ddx_set_optics(ddx_ctx* c, int n_grid, int n_wav, int n_theta, const double*
     OpticsDev& o = c->od;
     o.w = c->w; o.in = c->in; o.Qabs = c->Qabs; o.Qsca = c->Qsca; o.Qp = c->Qp; o.Td = c->Td;
     o.size = c->size_d; o.lQp = c->lQp; o.lTd = c->lTd; o.w5 = c->w5;
+    o.lQp32p = c->lQp32p; o.lTd32 = c->lTd32;
     o.Rmin = Rmin; o.Rmax = Rmax; o.fR = 0.0;
     o.n_grid = n_grid; o.n_wav = n_wav; o.n_theta = n_theta;
     if (cudaMemcpy(c->od_dev, &o, sizeof(OpticsDev), cudaMemcpyHostToDevice) != cudaSuccess) return DDX_ERR_CUDA;
@@ -417,6 +429,9 @@ int ddx_image(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_
         il.wj[k] = wj[k];
     }
     cudaSetDevice(c->device);
+    if (precision == DDX_PREC_MIXED)
+        return cuda_status(launch_image_mixed(*s, n_grav, n_dust, *view, c->od, il, c->vc, c->photo, Fd,
+                                              c->counters, (cudaStream_t)stream));
     return cuda_status(launch_image(*s, n_grav, n_dust, *view, c->od, il, c->vc, Fd, c->counters,
                                     (cudaStream_t)stream));
 }
@@ -438,6 +453,9 @@ int ddx_sed(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_vi
         if (dalloc(&c->sed_partial, need) != cudaSuccess) return DDX_ERR_NOMEM;
         c->sed_partial_cap = need;
     }
+    if (precision == DDX_PREC_MIXED)
+        return cuda_status(launch_sed_mixed(*s, n_grav, n_dust, *view, c->od, c->vc, c->photo, c->sed_partial,
+                                            mode, Fsed, (cudaStream_t)stream));
     return cuda_status(launch_sed(*s, n_grav, n_dust, *view, c->od, c->vc, c->sed_partial, mode,
                                   Fsed, (cudaStream_t)stream));
 }

@@ -323,8 +323,17 @@ __global__ void optics_prepare_kernel(OpticsDev o) {
     const size_t nt = (size_t)o.n_grid * kNR;
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nq; k += (size_t)gridDim.x * blockDim.x)
         o.lQp[k] = log(o.Qp[k]);
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nt; k += (size_t)gridDim.x * blockDim.x)
+    const size_t nq2 = (size_t)o.n_grid * (o.n_theta - 1) * o.n_wav;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nq2; k += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = k % o.n_wav, r = k / o.n_wav;
+        const size_t cm = r % (o.n_theta - 1), g = r / (o.n_theta - 1);
+        const size_t q = (g * o.n_theta + cm) * o.n_wav + j;
+        o.lQp32p[k] = make_float2((float)log2(o.Qp[q]), (float)log2(o.Qp[q + o.n_wav]));
+    }
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nt; k += (size_t)gridDim.x * blockDim.x) {
         o.lTd[k] = log(o.Td[k]);
+        o.lTd32[k] = (float)o.lTd[k];
+    }
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < (size_t)o.n_wav; k += (size_t)gridDim.x * blockDim.x)
         o.w5[k] = pow(o.w[k], 5);
 }
@@ -376,6 +385,399 @@ cudaError_t launch_pixels(const ddx_state& s, int n_grav, int n_dust, const ddx_
 int sed_blocks(int n_dust) {
     int b = (n_dust + kSedThreads - 1) / kSedThreads;
     return b < 1 ? 1 : (b > 1216 ? 1216 : b);
+}
+
+// ---------------------------------------------------------------------------------------
+// Mixed precision: FP32 photometry, pixel indices still bit-identical to the reference
+// ---------------------------------------------------------------------------------------
+//
+// FP64 runs at 1/73 of the FP32 rate here, and the FP64 kernels above spend it on
+// transcendental functions per tracer and wavelength.  The mixed kernels do the whole
+// per-tracer chain in FP32 and keep FP64 only where a result must be exact:
+//  - pixel index: the FP32 projection is trusted when it lies farther than
+//    64 eps32 (R/psca + |u| + 1) pixel from an edge (a bound on its rounding error, 3x
+//    the worst case of the operation chain); otherwise the FP64 fast projection and, in
+//    its own band, the reference's exact sequence decide, as in image_kernel;
+//  - R > Rmin: decided in FP64 when R is within 1e-5 of Rmin;
+//  - the per-pixel sums: FP64 atomics.  The FP32 flux is converted to FP64 exactly, by
+//    moving its bits (scaling by 2^-esh on the way), so the SM's FP64 pipe is not used.
+// The FP64 -> FP32 conversions of the state truncate by moving bits too (1 ulp).
+
+namespace {
+
+constexpr float kEps32 = 5.9604645e-8f;   // 2^-24
+
+// FP32 constants of a view, formed on the host (FP32 roundings of the exact values; the
+// guard band above allows for them) and passed by value, so no block spends FP64
+// divisions on them.
+struct View32 {
+    float cr, sr, ci, si, cp, sp;
+    float inv_psca, hx, hy;               // 1/psca, 0.5 psca xsize, 0.5 psca ysize
+    float inv_d;                          // 1/dist
+    float htheta, cmax;                   // (ntheta-1)/2, 1 - 2/ntheta
+    float Rmin, Rmax, fR, inv_fR;
+    int xsize, ysize, ntheta;
+};
+
+View32 make_view32(const ddx_view& v, const OpticsDev& o) {
+    View32 w;
+    const double psca = v.xsize >= v.ysize ? v.fov / v.xsize : v.fov / v.ysize;
+    w.cr = (float)cos(v.longitude); w.sr = (float)sin(v.longitude);
+    w.ci = (float)cos(v.inc); w.si = (float)sin(v.inc);
+    w.cp = (float)cos(v.PA); w.sp = (float)sin(v.PA);
+    w.inv_psca = (float)(1.0 / psca);
+    w.hx = (float)(0.5 * psca * v.xsize);
+    w.hy = (float)(0.5 * psca * v.ysize);
+    w.inv_d = (float)(1.0 / v.dist);
+    w.htheta = 0.5f * (float)(o.n_theta - 1);
+    w.cmax = (float)(1.0 - 2.0 / o.n_theta);
+    w.Rmin = (float)o.Rmin; w.Rmax = (float)o.Rmax;
+    w.fR = (float)o.fR; w.inv_fR = (float)(1.0 / o.fR);
+    w.xsize = v.xsize; w.ysize = v.ysize; w.ntheta = o.n_theta;
+    return w;
+}
+
+// FP64 -> FP32 by truncating the significand (error < 1 ulp of the float); values below
+// the FP32 normal range become zero.
+__device__ __forceinline__ float d2f_trunc(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    if (e < -126) return __uint_as_float(sign);
+    if (e > 127) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned int)(e + 127) << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
+}
+
+// f * 2^sh as FP64, exactly, for normal f (zero and subnormal f give 0).
+__device__ __forceinline__ double f2d_scaled(float f, int sh) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xffu;
+    if (e == 0) return 0.0;
+    const unsigned long long d = ((unsigned long long)(b & 0x80000000u) << 32) |
+                                 ((unsigned long long)(e - 127 + 1023 + sh) << 52) |
+                                 ((unsigned long long)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)d);
+}
+
+__device__ __forceinline__ bool near_edge32(float u, float g) {
+    const float f = u - floorf(u);
+    return f < g || f > 1.0f - g;
+}
+
+// The FP64 decisions of the mixed image, out of line so that none of their FP64 work is
+// hoisted into the common FP32 path.
+__device__ __noinline__ void pixel_fp64(double x, double y, double z, const ViewConst& v, int& xim, int& yim,
+                                        unsigned long long* counters) {
+    atomicAdd(&counters[1], 1ull);
+    const double Rd = sqrt(x * x + y * y + z * z);
+    double ud, wd;
+    fast_pixel_coord(x, y, z, v, ud, wd);
+    const double gd = guard_width(Rd, fmax(fabs(ud), fabs(wd)), v);
+    if (near_edge(ud, gd) || near_edge(wd, gd)) {
+        double cs;
+        exact_pixel(x, y, z, v, xim, yim, cs);
+        atomicAdd(&counters[0], 1ull);
+    } else {
+        xim = (int)floor(ud);
+        yim = (int)floor(wd);
+    }
+}
+
+__device__ __noinline__ bool outside_rmin_fp64(double x, double y, double z, double Rmin) {
+    return sqrt(x * x + y * y + z * z) > Rmin;
+}
+
+__device__ __forceinline__ float ex2_approx(float a) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+__device__ __forceinline__ float rcp_approx(float a) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
+// Scattering-angle cosine of src/gpu_functions.cu:1017-1023 rewritten for FP32 range:
+// with A = x1^2 + y1^2 + z^2, q = y1 sin(i) - z cos(i) and d the distance,
+// (A + d q) / (R sqrt(A + 2 d q + d^2)) = (A/d + q) / (R sqrt(A/d^2 + 2 q/d + 1));
+// clamped like the reference.  A = R^2, or R^2 + z^2 where the reference rotates by the
+// spherical radius.
+__device__ __forceinline__ float scatter_cos32(float y1, float z, float R, float A, const View32& v) {
+    const float q = y1 * v.si - z * v.ci;
+    const float ad = A * v.inv_d;
+    float c = (ad + q) / (R * sqrtf(fmaf(ad, v.inv_d, fmaf(2.0f * q, v.inv_d, 1.0f))));
+    if (c < -1.0f) c = -1.0f;
+    if (c >= v.cmax) c = v.cmax;
+    return c;
+}
+
+// Everything about a tracer that does not depend on the wavelength, in FP32.
+struct Tracer32 {
+    float n, invR2, wt, rT;
+    int id, cm;
+};
+
+// Accuracy: the Planck factor 1/(exp(x) - 1), x = hc/(lambda k T), turns a relative
+// error d in T into about x d in the flux, and x reaches tens on the Wien side.  So T (once
+// per tracer) and exp(x) use the accurate logf/expf; the phase function, whose error is
+// not amplified, takes one ex2.approx on a table of base-2 logs.
+__device__ __forceinline__ void tracer32_photometry(float R, float cossc, int id, float n, const View32& v,
+                                                    const OpticsDev& o, Tracer32& t) {
+    int cm = (int)floorf((cossc + 1.0f) * v.htheta);
+    cm = cm < 0 ? 0 : (cm > v.ntheta - 2 ? v.ntheta - 2 : cm);
+    t.cm = cm;
+    t.wt = (cossc - ((float)cm / v.htheta - 1.0f)) * v.htheta;
+    const float* lT = o.lTd32 + (size_t)id * kNR;
+    float lTv;
+    if (R >= v.Rmax) {
+        lTv = lT[kNR - 1];
+    } else {
+        const float lr = logf(R / v.Rmin);
+        int Rid = (int)(lr * v.inv_fR) + 1;
+        Rid = Rid < 1 ? 1 : (Rid > kNR - 1 ? kNR - 1 : Rid);
+        const float frac = (lr - (float)(Rid - 1) * v.fR) * v.inv_fR;
+        lTv = lT[Rid - 1] + (lT[Rid] - lT[Rid - 1]) * frac;
+    }
+    t.rT = expf(-lTv);                    // 1/T
+    t.invR2 = 1.0f / (R * R);
+    t.n = n;
+    t.id = id;
+}
+
+// Scaled flux of tracer t at wavelength slot j (table wavelength J).  lq2: the tracer's
+// row of base-2 log phase-function pairs (bin, cos bracket cm): lq2[J] = (log2 P(cm),
+// log2 P(cm+1)); A: its bin's row of (At, As).  One 8-byte load each.
+__device__ __forceinline__ float flux32(const Tracer32& t, const float2* lq2, const float2* A, int j, int J,
+                                        float C2j) {
+    const float x = C2j * t.rT;
+    const float e = expf(x);
+    // exp(x) - 1 loses digits for small x: Taylor series there (error < x^8/8! < 1e-7 rel)
+    const float ser = x * (1.0f + x * (0.5f + x * (1.0f / 6 + x * (1.0f / 24 + x * (1.0f / 120 + x * (1.0f / 720 + x * (1.0f / 5040)))))));
+    const float em1 = x < 0.5f ? ser : e - 1.0f;
+    const float pl = rcp_approx(em1);     // 0 once the exponential overflows
+    const float2 l = lq2[J];
+    const float P = ex2_approx(l.x + (l.y - l.x) * t.wt);
+    const float2 a = A[j];
+    return t.n * fmaf(a.x, pl, a.y * P * t.invR2);
+}
+
+}  // namespace
+
+// At, As, C2, esh for the wavelength slots of one call: one block per slot.
+__global__ void photo_prepare_kernel(OpticsDev o, const ViewConst* __restrict__ vcp, ImageList il, int use_list,
+                                     PhotoConst pc) {
+    __shared__ double smax[256];
+    const int j = blockIdx.x;
+    const int J = use_list ? il.wj[j] : j;
+    const double dist = vcp->dist;
+    const double wvl = o.w[J];
+    const double common = 1e26 * wvl * wvl / kCspeed;
+    const double ct = (2 * kHplank * kCspeed * kCspeed) / o.w5[J] * kPI / dist / dist * common;
+    const double cs = o.in[J] * kPI / kAU / kAU * common;
+    double m = 0.0;
+    for (int k = threadIdx.x; k < o.n_grid; k += blockDim.x) {
+        const double s2 = o.size[k] * o.size[k];
+        const double at = ct * s2 * o.Qabs[(size_t)o.n_wav * k + J];
+        const double as = cs * s2 * o.Qsca[(size_t)o.n_wav * k + J];
+        m = fmax(m, fmax(fabs(at), fabs(as)));
+    }
+    smax[threadIdx.x] = m;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + h]);
+        __syncthreads();
+    }
+    int e = 0;
+    if (smax[0] > 0.0 && isfinite(smax[0])) { frexp(smax[0], &e); e = 1 - e; }
+    const double scale = ldexp(1.0, e);
+    for (int k = threadIdx.x; k < o.n_grid; k += blockDim.x) {
+        const double s2 = o.size[k] * o.size[k];
+        pc.A[(size_t)k * pc.n_lam + j] = make_float2((float)(ct * s2 * o.Qabs[(size_t)o.n_wav * k + J] * scale),
+                                                     (float)(cs * s2 * o.Qsca[(size_t)o.n_wav * k + J] * scale));
+    }
+    if (threadIdx.x == 0) {
+        pc.C2[j] = (float)(kHplank * kCspeed / (wvl * kKboltz));
+        pc.esh[j] = e;
+    }
+}
+
+// Images, mixed precision: one thread per tracer, every image wavelength in one pass.
+__global__ void __launch_bounds__(256)
+image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ vcp, View32 v32, OpticsDev o,
+                   ImageList il, PhotoConst pc, double* __restrict__ Fd, unsigned long long* __restrict__ counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_dust) return;
+    const int t = n_grav + i;
+    const int id = s.id[t];
+    if (id < 0) return;
+    const double x = s.x[t], y = s.y[t], z = s.z[t];
+    const float xf = d2f_trunc(x), yf = d2f_trunc(y), zf = d2f_trunc(z);
+    const float R = sqrtf(fmaf(xf, xf, fmaf(yf, yf, zf * zf)));
+    const float x1 = xf * v32.cr - yf * v32.sr;
+    const float y1 = xf * v32.sr + yf * v32.cr;
+    const float y2 = y1 * v32.ci + zf * v32.si;
+    const float u = (x1 * v32.cp - y2 * v32.sp + v32.hx) * v32.inv_psca;
+    const float w = (x1 * v32.sp + y2 * v32.cp + v32.hy) * v32.inv_psca;
+    const float g = 64.0f * kEps32 * (R * v32.inv_psca + fmaxf(fabsf(u), fabsf(w)) + 1.0f);
+    int xim, yim;
+    if (near_edge32(u, g) || near_edge32(w, g)) {
+        pixel_fp64(x, y, z, *vcp, xim, yim, counters);
+    } else {
+        xim = (int)floorf(u);
+        yim = (int)floorf(w);
+    }
+    if (xim < 0 || xim > v32.xsize - 1 || yim < 0 || yim > v32.ysize - 1) return;
+    if (!(R > v32.Rmin * (1.0f + 1e-5f))) {
+        if (R < v32.Rmin * (1.0f - 1e-5f)) return;
+        if (!outside_rmin_fp64(x, y, z, o.Rmin)) return;
+    }
+    Tracer32 tr;
+    tracer32_photometry(R, scatter_cos32(y1, zf, R, R * R, v32), id, d2f_trunc(s.N[t]), v32, o, tr);
+    const size_t npix = (size_t)v32.xsize * v32.ysize;
+    const size_t pix = (size_t)v32.ysize * xim + yim;
+    const float2* lq2 = o.lQp32p + ((size_t)tr.id * (o.n_theta - 1) + tr.cm) * o.n_wav;
+    const float2* A = pc.A + (size_t)tr.id * pc.n_lam;
+    for (int k = 0; k < il.n; ++k) {
+        const float F = flux32(tr, lq2, A, k, il.wj[k], pc.C2[k]);
+        if (F != 0.0f) atomicAdd(&Fd[k * npix + pix], f2d_scaled(F, -pc.esh[k]));
+    }
+}
+
+// SED, mixed precision.  Each warp takes 32 tracers at a time; lane l accumulates the
+// wavelengths lam0 + l + 32 c (c < kSedChunks) over all of them, so the table reads of a
+// step are contiguous across the lanes and no per-wavelength reduction is needed inside
+// the loop.  Per lane: a plain FP32 sum over each group of 32 tracers, added to an FP32
+// Kahan sum; then FP64 sums over the warps in a fixed order and over the blocks in
+// sed_final_kernel.  Deterministic.
+constexpr int kSedChunks = 8;   // wavelengths per pass: 32 * kSedChunks
+
+__global__ void __launch_bounds__(kSedThreads, 3)
+sed_mixed_kernel(ddx_state s, int n_grav, int n_dust, View32 v32, OpticsDev o,
+                 PhotoConst pc, int mode, int lam0, double* __restrict__ partial) {
+    __shared__ double red[kSedThreads / 32][32 * kSedChunks];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (kSedThreads / 32) + warp, nw = gridDim.x * (kSedThreads / 32);
+    float S[kSedChunks], Cc[kSedChunks], C2r[kSedChunks];
+    const int rem = pc.n_lam - lam0;
+    const int nchunks = rem >= 32 * kSedChunks ? kSedChunks : (rem + 31) / 32;
+#pragma unroll
+    for (int c = 0; c < kSedChunks; ++c) {
+        S[c] = 0.f; Cc[c] = 0.f;
+        const int j = lam0 + c * 32 + lane;
+        C2r[c] = j < pc.n_lam ? pc.C2[j] : 0.f;
+    }
+    for (int base = gw * 32; base < n_dust; base += nw * 32) {
+        const int i = base + lane;
+        Tracer32 tr;
+        bool on = false;
+        tr.n = 0.f; tr.invR2 = 0.f; tr.wt = 0.f; tr.rT = 0.f; tr.id = 0; tr.cm = 0;
+        if (i < n_dust) {
+            const int t = n_grav + i;
+            const int id = s.id[t];
+            if (id >= 0) {
+                const double x = s.x[t], y = s.y[t], z = s.z[t];
+                const float xf = d2f_trunc(x), yf = d2f_trunc(y), zf = d2f_trunc(z);
+                const float R = sqrtf(fmaf(xf, xf, fmaf(yf, yf, zf * zf)));
+                float y1 = xf * v32.sr + yf * v32.cr;
+                float A = R * R;
+                if (mode == DDX_MODE_REFERENCE) {
+                    // the reference rotates by the spherical radius (src/gpu_functions.cu:1106-1107)
+                    const float Rd = sqrtf(fmaf(xf, xf, yf * yf));
+                    y1 = Rd > 0.f ? y1 * (R / Rd) : R * v32.sr;
+                    A = fmaf(zf, zf, A);
+                }
+                on = R > v32.Rmin * (1.0f + 1e-5f) ||
+                     (R >= v32.Rmin * (1.0f - 1e-5f) && outside_rmin_fp64(x, y, z, o.Rmin));
+                if (on) tracer32_photometry(R, scatter_cos32(y1, zf, R, A, v32), id, d2f_trunc(s.N[t]), v32, o, tr);
+            }
+        }
+        const unsigned live = __ballot_sync(0xffffffffu, on);
+        float G[kSedChunks];                                      // this group's plain sums
+#pragma unroll
+        for (int c = 0; c < kSedChunks; ++c) G[c] = 0.f;
+        const int off = lam0 + lane;                              // this lane's first wavelength
+        for (unsigned m = live; m; m &= m - 1) {
+            const int src = __ffs(m) - 1;
+            Tracer32 b;
+            b.n = __shfl_sync(0xffffffffu, tr.n, src);
+            b.invR2 = __shfl_sync(0xffffffffu, tr.invR2, src);
+            b.wt = __shfl_sync(0xffffffffu, tr.wt, src);
+            b.rT = __shfl_sync(0xffffffffu, tr.rT, src);
+            b.id = __shfl_sync(0xffffffffu, tr.id, src);
+            b.cm = __shfl_sync(0xffffffffu, tr.cm, src);
+            const float2* lq2 = o.lQp32p + ((size_t)b.id * (o.n_theta - 1) + b.cm) * o.n_wav + off;
+            const float2* A = pc.A + (size_t)b.id * pc.n_lam + off;
+#pragma unroll
+            for (int c = 0; c < kSedChunks; ++c) {
+                if (c >= nchunks) break;                          // warp-uniform
+                if (off + c * 32 < pc.n_lam) G[c] += flux32(b, lq2, A, c * 32, c * 32, C2r[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kSedChunks; ++c) {
+            const float yk = G[c] - Cc[c];
+            const float tk = S[c] + yk;
+            Cc[c] = (tk - S[c]) - yk;
+            S[c] = tk;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kSedChunks; ++c) {
+        const int j = lam0 + c * 32 + lane;
+        red[warp][c * 32 + lane] = j < pc.n_lam ? f2d_scaled(S[c], -pc.esh[j]) - f2d_scaled(Cc[c], -pc.esh[j]) : 0.0;
+    }
+    __syncthreads();
+    for (int jj = threadIdx.x; jj < 32 * kSedChunks; jj += blockDim.x) {
+        const int j = lam0 + jj;
+        if (j >= pc.n_lam) continue;
+        double b = 0.0;
+        for (int w = 0; w < kSedThreads / 32; ++w) b += red[w][jj];
+        partial[(size_t)blockIdx.x * o.n_wav + j] = b;
+    }
+}
+
+int sed_mixed_blocks(int n_dust) { return sed_blocks(n_dust); }
+
+cudaError_t launch_photo_prepare(const OpticsDev& o, const ViewConst* vc, const ImageList* il,
+                                 PhotoConst pc, cudaStream_t st) {
+    ImageList none{};
+    photo_prepare_kernel<<<pc.n_lam, 256, 0, st>>>(o, vc, il ? *il : none, il ? 1 : 0, pc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_image_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
+                               const OpticsDev& o, const ImageList& il, ViewConst* vc, PhotoConst pc,
+                               double* Fd, unsigned long long* counters, cudaStream_t st) {
+    view_setup_kernel<<<1, 32, 0, st>>>(vc, view, o.n_theta);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    pc.n_lam = il.n;
+    if ((e = launch_photo_prepare(o, vc, &il, pc, st)) != cudaSuccess) return e;
+    const size_t npix = (size_t)view.xsize * view.ysize;
+    if ((e = cudaMemsetAsync(Fd, 0, sizeof(double) * npix * il.n, st)) != cudaSuccess) return e;
+    if (n_dust <= 0) return cudaSuccess;
+    image_mixed_kernel<<<(n_dust + 255) / 256, 256, 0, st>>>(s, n_grav, n_dust, vc, make_view32(view, o), o, il,
+                                                             pc, Fd, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sed_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
+                             const OpticsDev& o, ViewConst* vc, PhotoConst pc, double* partial, int mode,
+                             double* Fsed, cudaStream_t st) {
+    view_setup_kernel<<<1, 32, 0, st>>>(vc, view, o.n_theta);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    pc.n_lam = o.n_wav;
+    if ((e = launch_photo_prepare(o, vc, nullptr, pc, st)) != cudaSuccess) return e;
+    const int nb = sed_mixed_blocks(n_dust);
+    const View32 v32 = make_view32(view, o);
+    for (int lam0 = 0; lam0 < o.n_wav; lam0 += 32 * kSedChunks) {
+        sed_mixed_kernel<<<nb, kSedThreads, 0, st>>>(s, n_grav, n_dust, v32, o, pc, mode, lam0, partial);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    sed_final_kernel<<<(o.n_wav + 127) / 128, 128, 0, st>>>(partial, nb, o.n_wav, Fsed);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,

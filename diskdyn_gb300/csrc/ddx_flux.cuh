@@ -18,6 +18,10 @@ struct ViewConst {
 struct OpticsDev {
     const double *w, *in, *Qabs, *Qsca, *Qp, *Td, *size;
     double *lQp, *lTd, *w5;          // derived on the device
+    // mixed photometry: lQp32p[k][cm][j] = (log2 Qp[k][cm][j], log2 Qp[k][cm+1][j]), the
+    // bracket of a scattering-angle bin in one 8-byte load; lTd32 = (float) log Td
+    float2* lQp32p;                  // [n_grid][n_theta-1][n_wav]
+    float* lTd32;                    // [n_grid][100]
     double Rmin, Rmax, fR;           // fR = log(Rmax/Rmin)/(nR-1)
     int n_grid, n_wav, n_theta;
 };
@@ -26,6 +30,28 @@ struct ImageList {
     int n;
     int wj[kMaxImages];
 };
+
+// Per-call FP32 photometry coefficients of the mixed path, for n_lam wavelengths
+// (the image list, or every table wavelength for the SED).  The flux of a tracer of bin k
+// at wavelength slot j, before its multiplicity N, is
+//   (At[k][j] / (exp(C2[j] / T) - 1) + As[k][j] P / R^2) * 2^-esh[j]
+// with At, As scaled by 2^esh[j] so that their largest value over the bins lies in [1, 2).
+struct PhotoConst {
+    float2* A;                       // [n_grid][n_lam] = (At, As)
+    float* C2;                       // [n_lam] h c / (lambda k), K
+    int* esh;                        // [n_lam]
+    int n_lam;
+};
+
+cudaError_t launch_photo_prepare(const OpticsDev& o, const ViewConst* vc, const ImageList* il,
+                                 PhotoConst pc, cudaStream_t st);
+cudaError_t launch_image_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
+                               const OpticsDev& o, const ImageList& il, ViewConst* vc, PhotoConst pc,
+                               double* Fd, unsigned long long* counters, cudaStream_t st);
+cudaError_t launch_sed_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
+                             const OpticsDev& o, ViewConst* vc, PhotoConst pc, double* partial, int mode,
+                             double* Fsed, cudaStream_t st);
+int sed_mixed_blocks(int n_dust);
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll

@@ -131,9 +131,10 @@ def test_pixel_indices_bit_identical_to_reference(engine, refk, img_sys):
     check_pixels_against_reference(engine, refk, s, sub)
 
 
-def edge_tracers(s, n=3000, seed=3):
+def edge_tracers(s, n=3000, seed=3, spread=None):
     """Tracers placed so that their projected coordinates fall within ~1e-13 pixel of a
-    pixel edge (x, y or both), by inverting the projection of the view."""
+    pixel edge (x, y or both), by inverting the projection of the view.  spread=(lo, hi):
+    at a distance log-uniform in [lo, hi] pixel from the edge instead, on either side."""
     v = s.view
     g = synth.rng(seed)
     psca = v["fov"] / max(v["xsize"], v["ysize"])
@@ -141,6 +142,8 @@ def edge_tracers(s, n=3000, seed=3):
     iy = g.integers(1, v["ysize"] - 1, n).astype(np.float64)
     frac = lambda: g.uniform(0.2, 0.8, n)
     tiny = g.uniform(-3e-13, 3e-13, n)
+    if spread is not None:
+        tiny = np.sign(g.uniform(-1, 1, n)) * 10.0 ** g.uniform(math.log10(spread[0]), math.log10(spread[1]), n)
     kind = g.integers(0, 3, n)
     u = np.where(kind != 1, ix + tiny, ix + frac())
     w = np.where(kind != 0, iy + tiny, iy + frac())
@@ -171,6 +174,56 @@ def test_pixel_indices_at_pixel_edges_bit_identical_to_reference(engine, refk):
     st = edge_tracers(s)
     ex = check_pixels_against_reference(engine, refk, s, st, max_batches=400)
     assert ex.sum() > 0.9 * len(ex)      # the guard band sent them down the exact path
+
+
+def gpu_image_prec(engine, s, state, precision, wj=None):
+    setup_engine(engine, s)
+    st = DeviceState.from_numpy(state)
+    F = engine.image(st, s.n_grav, make_view(**s.view), wj if wj is not None else s.image_wj, precision=precision)
+    torch.cuda.synchronize()
+    return F.cpu().numpy()
+
+
+def test_mixed_image_matches_fp64(engine, img_sys):
+    """FP32 photometry: every pixel within 1e-5 of the FP64 image (a pixel is a sum of
+    positive terms, each within ~1e-6), the same pixels lit, total flux within 1e-6."""
+    s = img_sys
+    F = gpu_image_prec(engine, s, s.state, abi.DDX_PREC_FP64)
+    Fm = gpu_image_prec(engine, s, s.state, abi.DDX_PREC_MIXED)
+    assert np.array_equal(F != 0, Fm != 0)
+    np.testing.assert_allclose(Fm, F, rtol=1e-5, atol=0)
+    for k in range(len(F)):
+        assert abs(Fm[k].sum() / F[k].sum() - 1.0) < 1e-6
+
+
+@pytest.mark.parametrize("spread", [None, (1e-7, 1e-2)])
+def test_mixed_pixel_indices_match_fp64_near_edges(engine, spread):
+    """The mixed image puts every tracer in the FP64 kernel's pixel (which is the
+    reference's): tracers within 3e-13 pixel of an edge, and tracers at 1e-7..1e-2 pixel
+    on either side, across the FP32 guard band.  Batches of tracers at least 3 pixels
+    apart, so equal lit-pixel sets mean equal pixels tracer by tracer."""
+    s = synth.imaging(n_dust=16, xsize=300, ysize=240)
+    s.view.update(inc=math.radians(37.0), PA=math.radians(23.0), longitude=math.radians(11.0))
+    st = edge_tracers(s, n=2000, seed=4, spread=spread)
+    pix, _ = gpu_pixels(engine, s, st)
+    ng = s.n_grav
+    R = np.sqrt(st["x"][ng:] ** 2 + st["y"][ng:] ** 2 + st["z"][ng:] ** 2)
+    batches = spread_batches(np.where(R > s.optics["Rmin"], pix, -1), 3, s.view["ysize"])
+    for b in batches:
+        sub = {k: np.concatenate([v[:ng], v[ng:][b]]) for k, v in st.items()}
+        F = gpu_image_prec(engine, s, sub, abi.DDX_PREC_FP64, [s.image_wj[0]])
+        Fm = gpu_image_prec(engine, s, sub, abi.DDX_PREC_MIXED, [s.image_wj[0]])
+        assert np.array_equal(F != 0, Fm != 0)
+
+
+def test_mixed_sed_matches_fp64_both_modes(engine, img_sys):
+    s = img_sys
+    setup_engine(engine, s)
+    st = DeviceState.from_numpy(s.state)
+    for mode in (abi.DDX_MODE_FIXED, abi.DDX_MODE_REFERENCE):
+        F = engine.sed(st, s.n_grav, make_view(**s.view), mode=mode).cpu().numpy()
+        Fm = engine.sed(st, s.n_grav, make_view(**s.view), precision=abi.DDX_PREC_MIXED, mode=mode).cpu().numpy()
+        np.testing.assert_allclose(Fm, F, rtol=1e-5)
 
 
 def test_image_rejects_bad_arguments(engine, img_sys):
