@@ -49,7 +49,8 @@ def parse():
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["dusty_ring", "imaging"], default="dusty_ring")
+    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale"], default="dusty_ring")
+    p.add_argument("--scale-err-steps", type=int, default=60)
     p.add_argument("--adjoint-steps", type=int, default=2000)
     return p.parse_args()
 
@@ -360,7 +361,7 @@ def image_profiles(img, n_r=48, n_phi=36):
     return radial, azim
 
 
-def long_error_leg(eng, phys, args):
+def long_error_leg(eng, phys, args, n_plsml=None, seed=None, n_steps=None, floor=True):
     """Mixed precision against FP64 over err_steps steps of a dusty-ring shard (all massive
     bodies, err_dust grains): relative position error of grains and massive bodies, the
     massive set's energy drift, and the error of the radial and azimuthal profiles of the
@@ -370,15 +371,19 @@ def long_error_leg(eng, phys, args):
     import torch
     from diskdyn_gb300 import abi, synth
     from diskdyn_gb300.engine import DeviceState, Engine, make_view
-    small = synth.ring_imaging(synth.dusty_ring(n_dust=args.err_dust, n_plsml=args.n_plsml, seed=synth.SEED + 17))
+    n_plsml = args.n_plsml if n_plsml is None else n_plsml
+    seed = synth.SEED + 17 if seed is None else seed
+    n_steps = args.err_steps if n_steps is None else n_steps
+    small = synth.ring_imaging(synth.dusty_ring(n_dust=args.err_dust, n_plsml=n_plsml, seed=seed))
     ng = small.n_grav
     runs = {}
-    for name, prec, mode in (("fp64", abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED),
-                             ("mixed", abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED),
-                             ("fp64_ref_expr", abi.DDX_PREC_FP64, abi.DDX_MODE_REFERENCE)):
+    forms = [("fp64", abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED), ("mixed", abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)]
+    if floor:
+        forms.append(("fp64_ref_expr", abi.DDX_PREC_FP64, abi.DDX_MODE_REFERENCE))
+    for name, prec, mode in forms:
         st = DeviceState.from_numpy(small.state)
         e0 = massive_energy(st, ng)
-        eng.evolve(st, ng, small.dt, args.err_steps, phys, prec, mode)
+        eng.evolve(st, ng, small.dt, n_steps, phys, prec, mode)
         torch.cuda.synchronize()
         runs[name] = (st, (massive_energy(st, ng) - e0) / abs(e0))
     ie = Engine(torch.cuda.current_device())
@@ -416,12 +421,86 @@ def long_error_leg(eng, phys, args):
         out["image"] = prof
         return out
 
-    return {"steps": args.err_steps, "n_dust": args.err_dust, "n_grav": ng, "n_planets": small.phys["n_planets"],
-            "fp64_massive_energy_drift": runs["fp64"][1],
-            "mixed_vs_fp64": compare("mixed"),
-            "fp64_floor_ref_expr_vs_fp64": compare("fp64_ref_expr"),
-            "profile_error_definition": "max over bins of |profile - FP64 profile| / max FP64 profile; "
-                                        "48 annuli to the frame half-width, 36 sectors"}
+    out = {"steps": n_steps, "n_dust": args.err_dust, "n_grav": ng, "n_planets": small.phys["n_planets"],
+           "fp64_massive_energy_drift": runs["fp64"][1],
+           "mixed_vs_fp64": compare("mixed"),
+           "profile_error_definition": "max over bins of |profile - FP64 profile| / max FP64 profile; "
+                                       "48 annuli to the frame half-width, 36 sectors"}
+    if floor:
+        out["fp64_floor_ref_expr_vs_fp64"] = compare("fp64_ref_expr")
+    return out
+
+
+def run_scale(args, world, rank, local):
+    """Mixed precision at scale: 16,777,216 grains + 65,536 gravitating planetesimals with
+    the dusty ring's star and two planets.  Times `steps` full steps (L2 flushed between
+    them) and reports the error against FP64 on a shard of err_dust grains with the same
+    massive set over --scale-err-steps steps: grains are test particles given the massive
+    trajectories, so a shard follows the dynamics of the full run."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys, probe_fma_peak
+
+    torch.cuda.set_device(local)
+    n_dust = args.n_dust if args.n_dust != 1048576 else 16777216
+    n_plsml = args.n_plsml if args.n_plsml != 4096 else 65536
+    seed = synth.SEED + 4243 + 7919 * rank
+    sysm = synth.dusty_ring(n_dust=n_dust, n_plsml=n_plsml, seed=seed, n_steps=500)
+    ng = sysm.n_grav
+    eng = Engine(local)
+    eng.set_size_table(**sysm.size_table)
+    phys = make_phys(**sysm.phys)
+    st = DeviceState.from_numpy(sysm.state, device=f"cuda:{local}")
+    del sysm.state
+    MIX = abi.DDX_PREC_MIXED
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def one_step(ev):
+        ev[0].record(stream)
+        eng.stage("massive_rk4", st, ng, sysm.dt, phys, MIX)
+        ev[1].record(stream)
+        eng.stage("small_rk4", st, ng, sysm.dt, phys, MIX)
+        ev[2].record(stream)
+        eng.stage("massive_final", st, ng, sysm.dt, phys, MIX)
+        ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        one_step([torch.cuda.Event(enable_timing=True) for _ in range(4)])
+    torch.cuda.synchronize()
+    alive0 = int((st.N[ng:] != 0).sum().item())
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    with Clocks(smi_index(local)) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            one_step(evs[k])
+        torch.cuda.synchronize()
+    alive1 = int((st.N[ng:] != 0).sum().item())
+    step_ms = [e[0].elapsed_time(e[3]) for e in evs]
+    massive_ms = [e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3]) for e in evs]
+    dust_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    value = (ng + 0.5 * (alive0 + alive1)) * args.steps / (sum(step_ms) / 1e3)
+    fp32_peak, _ = probe_fma_peak(local)
+    inter = 4.0 * 0.5 * (alive0 + alive1) * (ng - 1)
+    flops = FLOP_PAIR * inter + FLOP_STAR * 4.0 * 0.5 * (alive0 + alive1)
+    achieved = flops / (statistics.mean(dust_ms) / 1e3) / 1e12
+    line = {"metric": "RK4 body-steps/s (mixed precision, FP64-error stated)", "value": value,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 state + f32 perturbations (mixed)",
+            "data": "synthetic (seeded Philox), mixed precision at scale",
+            "config": {"workload": "scale", "n_grav": ng, "n_dust": n_dust, "n_planetesimals": n_plsml,
+                       "dt_yr": sysm.dt, "precision": "mixed", "l2": "flushed between timed steps (256 MiB write)"},
+            "dust_kernel_ms": statistics.mean(dust_ms), "massive_ms": statistics.mean(massive_ms),
+            "roofline": {"kernel": "dust_rk4_kernel<mixed>", "bound": "fp32_pipe", "achieved": achieved,
+                         "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak},
+            "clocks": clk.summary()}
+    del st
+    torch.cuda.empty_cache()
+    if args.scale_err_steps > 0:
+        line["error_vs_fp64"] = long_error_leg(eng, phys, args, n_plsml=n_plsml, seed=seed,
+                                               n_steps=args.scale_err_steps, floor=False)
+    print(json.dumps(line), flush=True)
 
 
 def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
@@ -626,6 +705,9 @@ def main():
     world, rank, local = dist_setup(args)
     if args.workload == "imaging":
         run_imaging(args, world, rank, local)
+        return
+    if args.workload == "scale":
+        run_scale(args, world, rank, local)
         return
     if args.impl == "reference":
         run_reference(args, world, rank, local)
