@@ -99,7 +99,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, unsigned parity, unsigned
     return true;
 }
 
-__global__ void __launch_bounds__(kThreads, 2)
+// Three blocks per SM (80 registers): the few FP64 values the compiler keeps in local
+// memory are touched only between stages, and the extra warps hide the latency of the
+// broadcast shared-memory reads and of rsqrt.approx better than two blocks without spills.
+__global__ void __launch_bounds__(kThreads, 3)
 dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar[2];
@@ -152,31 +155,29 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
     if (tid == 0 && G > 0) issue(0);
 
     const double dt = a.dt, dt2 = a.dt / 2.0, dt6 = a.dt / 6.0;
-    double k1vx = 0, k1vy = 0, k1vz = 0, k2vx = 0, k2vy = 0, k2vz = 0;
-    double k3vx = 0, k3vy = 0, k3vz = 0, k4vx = 0, k4vy = 0, k4vz = 0;
-    double k2rx = 0, k2ry = 0, k2rz = 0, k3rx = 0, k3ry = 0, k3rz = 0;
-    double k4rx = 0, k4ry = 0, k4rz = 0;
+    // RK4 of src/gpu_functions.cu:627-943 with running sums, so that little FP64 state is
+    // live across the FP32 loop: stage s evaluates the acceleration at
+    //   x_s = x + r_{s-1} c_s,  r_s = v + k_{s-1} c_s   (c = 0, dt/2, dt/2, dt; r_0 = v),
+    // and the update is x += dt/6 sum w_s r_s, v += dt/6 sum w_s k_s with w = 1, 2, 2, 1.
+    double rpx = vx, rpy = vy, rpz = vz;      // r_{s-1}
+    double kpx = 0, kpy = 0, kpz = 0;         // k_{s-1}
+    double Ax = 0, Ay = 0, Az = 0;            // sum w_s r_s
+    double Bx = 0, By = 0, Bz = 0;            // sum w_s k_s
     int removed = 0, removed_stage = -1;
     int lost = 0;
     int g = 0;
 
 #pragma unroll 1
     for (int st = 0; st < 4; ++st) {
-        double xt, yt, zt, rx, ry, rz;
-        if (st == 0)      { xt = x; yt = y; zt = z; rx = vx; ry = vy; rz = vz; }
-        else if (st == 1) {
-            k2rx = vx + k1vx * dt2; k2ry = vy + k1vy * dt2; k2rz = vz + k1vz * dt2;
-            xt = x + vx * dt2; yt = y + vy * dt2; zt = z + vz * dt2;
-            rx = k2rx; ry = k2ry; rz = k2rz;
-        } else if (st == 2) {
-            k3rx = vx + k2vx * dt2; k3ry = vy + k2vy * dt2; k3rz = vz + k2vz * dt2;
-            xt = x + k2rx * dt2; yt = y + k2ry * dt2; zt = z + k2rz * dt2;
-            rx = k3rx; ry = k3ry; rz = k3rz;
-        } else {
-            k4rx = vx + k3vx * dt; k4ry = vy + k3vy * dt; k4rz = vz + k3vz * dt;
-            xt = x + k3rx * dt; yt = y + k3ry * dt; zt = z + k3rz * dt;
-            rx = k4rx; ry = k4ry; rz = k4rz;
+        double xt = x, yt = y, zt = z, rx = vx, ry = vy, rz = vz;
+        if (st > 0) {
+            const double c = st == 3 ? dt : dt2;
+            xt = x + rpx * c; yt = y + rpy * c; zt = z + rpz * c;
+            rx = vx + kpx * c; ry = vy + kpy * c; rz = vz + kpz * c;
         }
+        const double w = (st == 1 || st == 2) ? 2.0 : 1.0;
+        Ax += w * rx; Ay += w * ry; Az += w * rz;
+        rpx = rx; rpy = ry; rpz = rz;
         double kx = 0, ky = 0, kz = 0;
         if (alive) {
             const Body ps = ms.P[st * ms.cap + 0];
@@ -241,10 +242,8 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
             }
             kx += px; ky += py; kz += pz;
         }
-        if (st == 0)      { k1vx = kx; k1vy = ky; k1vz = kz; }
-        else if (st == 1) { k2vx = kx; k2vy = ky; k2vz = kz; }
-        else if (st == 2) { k3vx = kx; k3vy = ky; k3vz = kz; }
-        else              { k4vx = kx; k4vy = ky; k4vz = kz; }
+        Bx += w * kx; By += w * ky; Bz += w * kz;
+        kpx = kx; kpy = ky; kpz = kz;
     }
     lost = __syncthreads_or(lost);
     if (lost) {
@@ -263,12 +262,8 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
         return;
     }
     if (!alive) return;
-    x += dt6 * (vx + 2.0 * (k2rx + k3rx) + k4rx);
-    y += dt6 * (vy + 2.0 * (k2ry + k3ry) + k4ry);
-    z += dt6 * (vz + 2.0 * (k2rz + k3rz) + k4rz);
-    vx += dt6 * (k1vx + 2.0 * (k2vx + k3vx) + k4vx);
-    vy += dt6 * (k1vy + 2.0 * (k2vy + k3vy) + k4vy);
-    vz += dt6 * (k1vz + 2.0 * (k2vz + k3vz) + k4vz);
+    x += dt6 * Ax; y += dt6 * Ay; z += dt6 * Az;
+    vx += dt6 * Bx; vy += dt6 * By; vz += dt6 * Bz;
     s.x[t] = x; s.y[t] = y; s.z[t] = z;
     s.vx[t] = vx; s.vy[t] = vy; s.vz[t] = vz;
 }

@@ -57,7 +57,7 @@ struct __align__(16) BodyPair {
     float lx[2], ly[2], lz[2], pad[2];
 };
 
-constexpr int kPairSpan = 8;     // pair records per plain-FP32 partial sum (16 sources)
+constexpr int kPairSpan = 16;    // pair records per plain-FP32 partial sum (32 sources)
 
 // Pair records per stage for n_src FP32 sources (bodies n_exact..n_grav-1) in pairs,
 // padded with zero-mass records to a multiple of kPairSpan.
