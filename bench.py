@@ -693,6 +693,20 @@ def run_imaging(args, world, rank, local):
         "sed_rel_err_max": float(((Sm - S64).abs() / S64.abs()).max().item()),
         "image_speedup": out["fp64"]["image_ms"] / out["mixed"]["image_ms"],
         "sed_speedup": out["fp64"]["sed_ms"] / out["mixed"]["sed_ms"]}
+    # the dust-temperature table of the same optics (Grid::calculate_dust_temp): GPU vs the
+    # oracle on all host cores
+    import oracle.cpu as oc
+    eng.dust_temp(o["w"], o["in"], o["Qabs"], s.view["dist"], 60.0)
+    t0 = time.perf_counter()
+    Td_g, rmin_g, _ = eng.dust_temp(o["w"], o["in"], o["Qabs"], s.view["dist"], 60.0)
+    t_g = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Td_c, rmin_c, _ = oc.dust_temp(o["w"], o["in"], o["Qabs"], s.view["dist"], 60.0)
+    t_c = time.perf_counter() - t0
+    out["dust_temp"] = {"what": "Td table, %d bins x %d wavelengths x 1,999 temperatures" % o["Qabs"].shape,
+                        "gpu_ms": t_g * 1e3, "cpu_oracle_ms": t_c * 1e3, "cpu_cores": os.cpu_count(),
+                        "max_rel_diff": float(np.max(np.abs(Td_g / Td_c - 1.0))),
+                        "rmin_rel_diff": abs(rmin_g / rmin_c - 1.0)}
     line = {"metric": "imaging particle-wavelengths/s", "workload": "imaging", "n_particles": n,
             "n_img": n_img, "n_wav": len(o["w"]), "image": [s.view["xsize"], s.view["ysize"]],
             "results": out, "l2": "flushed between timed calls"}

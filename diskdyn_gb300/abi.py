@@ -87,6 +87,8 @@ SIGNATURES = [
     ("ddx_det_step", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_void_p, C.c_int,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                C.c_void_p]),
+    ("ddx_dust_temp", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p, C.c_void_p]),
     ("ddx_sync_status", C.c_int, [C.c_void_p, C.c_void_p]),
     ("ddx_debug_lose_tile_copy", C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong]),
     ("ddx_probe_fma_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -367,6 +367,15 @@ int ddx_det_step(ddx_ctx* c, const ddx_state* s, int n_grav, int n_step, const d
     return DDX_OK;
 }
 
+int ddx_dust_temp(ddx_ctx* c, int n_grid, int n_wav, const double* w, const double* in, const double* Qabs,
+                  double dist, double* Rmin_AU, double* Rmax_AU, double* Td, void* stream) {
+    if (!c || n_grid < 1 || n_wav < 2 || !w || !in || !Qabs || !Rmin_AU || !Rmax_AU || !Td) return DDX_ERR_ARG;
+    if (!(dist > 0.0) || !(*Rmax_AU > 0.0)) return DDX_ERR_ARG;
+    if (n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
+    cudaSetDevice(c->device);
+    return dust_temp_run(n_grid, n_wav, w, in, Qabs, dist, Rmin_AU, Rmax_AU, Td, (cudaStream_t)stream);
+}
+
 int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,
                         int ckpt_every, const ddx_phys* phys, const ddx_view* view, const int* wj, int n_img,
                         double* image, void* stream) {

@@ -156,4 +156,8 @@ struct DetStepScratch {
 int det_step_scan(DetStepScratch*& d, const ddx_state& s, int n_grav, cudaStream_t st,
                   std::vector<double>& rr, std::vector<double>& mi, double& m0);
 void det_step_free(DetStepScratch*& d);
+
+// ddx_optics_prep.cu: the dust-temperature table (host arrays in and out; synchronizes).
+int dust_temp_run(int n_grid, int n_wav, const double* w, const double* in, const double* Qabs, double dist,
+                  double* Rmin_AU, double* Rmax_AU, double* Td, cudaStream_t st);
 }  // namespace ddx

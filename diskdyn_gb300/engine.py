@@ -197,6 +197,20 @@ class Engine:
                                         C.c_void_p(_stream_handle(stream))), "ddx_det_step")
         return dt.value
 
+    def dust_temp(self, w, influx, Qabs, dist, Rmax_AU, stream=None):
+        """Grid::calculate_dust_temp on the GPU: (Td (n_grid, 100), Rmin, Rmax) in AU."""
+        w = np.ascontiguousarray(w, np.float64)
+        influx = np.ascontiguousarray(influx, np.float64)
+        Qabs = np.ascontiguousarray(Qabs, np.float64)
+        n_grid, n_wav = Qabs.shape
+        Td = np.zeros((n_grid, abi.DDX_NR))
+        rmin, rmax = C.c_double(0.0), C.c_double(float(Rmax_AU))
+        abi.check(self.lib.ddx_dust_temp(self.ctx, n_grid, n_wav, C.c_void_p(w.ctypes.data),
+                                         C.c_void_p(influx.ctypes.data), C.c_void_p(Qabs.ctypes.data), float(dist),
+                                         C.byref(rmin), C.byref(rmax), C.c_void_p(Td.ctypes.data),
+                                         C.c_void_p(_stream_handle(stream))), "ddx_dust_temp")
+        return Td, rmin.value, rmax.value
+
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
         bounded device-side wait since the last call, else 0."""

@@ -201,6 +201,18 @@ int ddx_det_step(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_step, const
                  int n_disks, const double *blob_a, const double *blob_ecc, const double *blob_sigma,
                  int n_blobs, double *dt, void *stream);
 
+/* Dust-temperature table; replaces Grid::calculate_dust_temp (src/grid.cu:754-834), which
+ * the reference runs on the host before the first step.  In: the optical tables w[n_wav]
+ * (m), in[n_wav], Qabs[n_grid][n_wav] and dist (m), host pointers, and *Rmax_AU = the
+ * largest configured radius (disks' Rout, blobs' a(1+e)+sigma, planets' distances; the
+ * reference's loop at src/grid.cu:759-765).  Out: Td[n_grid][DDX_NR] (host), the grain
+ * temperature on the log-radius grid from *Rmin_AU (the smallest sublimation radius at
+ * 2000 K) to *Rmax_AU (twice the input, as the reference sets it).  The Planck integrals run
+ * on the GPU, one thread per (bin, temperature).  Synchronises `stream`. */
+int ddx_dust_temp(ddx_ctx *ctx, int n_grid, int n_wav, const double *w, const double *in,
+                  const double *Qabs, double dist, double *Rmin_AU, double *Rmax_AU, double *Td,
+                  void *stream);
+
 /* Discrete adjoint of the trajectory and image (no counterpart in the reference).
  *
  * ddx_adjoint_forward integrates the initial state `s` (read only) for n_steps fixed-dt
