@@ -134,7 +134,7 @@ def measured_peaks():
 
 def run_ours(args, world, rank, local):
     import torch
-    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300 import abi, shard, synth
     from diskdyn_gb300.engine import DeviceState, Engine, make_phys, probe_fma_peak
 
     torch.cuda.set_device(local)
@@ -200,9 +200,9 @@ def run_ours(args, world, rank, local):
     step_ms = [e[0].elapsed_time(e[3]) for e in evs]
     dust_ms = [e[1].elapsed_time(e[2]) for e in evs]
     alive1 = int((st.N[ng:] != 0).sum().item())
-    t_total = allmax(sum(step_ms) / 1e3)
-    units = allsum((ng + 0.5 * (alive0 + alive1)) * args.steps)
-    value = units / t_total
+    # whole job: units of all ranks over the slowest rank's time (diskdyn_gb300.shard)
+    units, t_total, value = shard.job_rate((ng + 0.5 * (alive0 + alive1)) * args.steps, sum(step_ms) / 1e3,
+                                           device="cuda")
 
     # spatial-hash collision pass over the grains (the workload detects collisions every step)
     h_coll = 0.1
