@@ -49,7 +49,8 @@ def parse():
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale"], default="dusty_ring")
+    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar"], default="dusty_ring")
+    p.add_argument("--solar-steps", type=int, default=1000)
     p.add_argument("--scale-err-steps", type=int, default=60)
     p.add_argument("--adjoint-steps", type=int, default=2000)
     return p.parse_args()
@@ -602,6 +603,9 @@ def run_reference(args, world, rank, local):
         return
     import oracle.cpu as oc
     from diskdyn_gb300 import synth
+    if args.workload == "solar":
+        run_reference_solar(args, world)
+        return
     sysm = synth.dusty_ring(n_dust=args.n_dust, n_plsml=args.n_plsml)
     ng = sysm.n_grav
     n_sample = min(65536, sysm.n_dust)
@@ -631,6 +635,109 @@ def run_reference(args, world, rank, local):
                 "value": (ng + sysm.n_dust) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
                 "what": "the reference's own kernels compiled unmodified for sm_103a, one full step, CUDA events"}
     except Exception as e:  # the GPU leg is informative only
+        line["reference_cuda_gb300"] = {"unavailable": str(e)[:200]}
+    print(json.dumps(line), flush=True)
+
+
+def run_solar(args, world, rank, local):
+    """Plain FP64 solar-system-like run: 1 Msun star, 8 planets (1.7e-7 to 9.5e-4 Msun,
+    0.4-30 AU), 16,384 massless planetesimals at 30-50 AU, dt = 0.05 yr, 1,000 steps.  One
+    timed repetition is the whole 1,000-step run through ddx_evolve (4 kernels per step),
+    launched directly and replayed as a CUDA graph captured from the same call."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys
+
+    torch.cuda.set_device(local)
+    n_dust = args.n_dust if args.n_dust != 1048576 else 16384
+    sysm = synth.solar_like(n_dust=n_dust, seed=synth.SEED + 7919 * rank)
+    ng, n_steps = sysm.n_grav, args.solar_steps
+    eng = Engine(local)
+    eng.set_size_table(**sysm.size_table)
+    phys = make_phys(**sysm.phys)
+    st0 = DeviceState.from_numpy(sysm.state, device=f"cuda:{local}")
+    stream = torch.cuda.Stream()
+    out = {}
+    for prec, name in ((abi.DDX_PREC_FP64, "fp64"), (abi.DDX_PREC_MIXED, "mixed")):
+        st = st0.clone()
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                eng.evolve(st, ng, sysm.dt, 10, phys, prec, stream=stream)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(max(1, args.steps // 10)):
+            st = st0.clone()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.evolve(st, ng, sysm.dt, n_steps, phys, prec, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        res = {"ms_per_run": statistics.mean(ms), "body_steps_per_s": (ng + n_dust) * n_steps / (statistics.mean(ms) / 1e3)}
+        # the same 1,000 steps captured once into a CUDA graph and replayed
+        try:
+            st = st0.clone()
+            g = torch.cuda.CUDAGraph()
+            torch.cuda.synchronize()
+            with torch.cuda.graph(g, stream=stream):
+                eng.evolve(st, ng, sysm.dt, n_steps, phys, prec, stream=stream)
+            gms = []
+            for _ in range(max(1, args.steps // 10)):
+                st.copy_from_({f: getattr(st0, f) for f in ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id")})
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
+                    g.replay()
+                    e1.record(stream)
+                torch.cuda.synchronize()
+                gms.append(e0.elapsed_time(e1))
+            res["graph_ms_per_run"] = statistics.mean(gms)
+            res["graph_body_steps_per_s"] = (ng + n_dust) * n_steps / (statistics.mean(gms) / 1e3)
+        except Exception as e:
+            res["graph"] = {"unavailable": str(e)[:200]}
+        out[name] = res
+    best = max(out["fp64"].get("graph_body_steps_per_s", 0.0), out["fp64"]["body_steps_per_s"])
+    line = {"metric": METRIC, "value": best, "unit": UNIT, "n_gpus": 1, "steps": n_steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded Philox), solar-system-like configuration",
+            "config": {"workload": "solar", "n_grav": ng, "n_dust": n_dust, "dt_yr": sysm.dt, "precision": "fp64",
+                       "kernels_per_step": 4, "l2": "inputs below L2; a whole 1,000-step run per timed repetition"},
+            "results": out, "gpu_launches": 4 * n_steps}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_solar(args, world):
+    """Reference arm of the solar-system run: the oracle port on all host cores over the
+    whole 1,000-step run, and the reference's own CUDA kernels (sm_103a, its launch
+    sequence: about 12 launches per step) over the same run."""
+    import oracle.cpu as oc
+    from diskdyn_gb300 import synth
+    n_dust = args.n_dust if args.n_dust != 1048576 else 16384
+    sysm = synth.solar_like(n_dust=n_dust)
+    ng, n_steps = sysm.n_grav, args.solar_steps
+    oc.step(sysm.state, ng, sysm.dt, sysm.size_table, sysm.phys, 10)
+    t0 = time.perf_counter()
+    oc.step(sysm.state, ng, sysm.dt, sysm.size_table, sysm.phys, n_steps)
+    t = time.perf_counter() - t0
+    value = (ng + n_dust) * n_steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": n_steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox), solar-system-like configuration",
+            "config": {"workload": "solar", "n_grav": ng, "n_dust": n_dust, "dt_yr": sysm.dt, "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"the whole run: {n_steps} steps of {ng} massive bodies + {n_dust} planetesimals"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    try:
+        import oracle.refk as rk
+        if rk.available():
+            _, ms_step = rk.step(sysm.state, ng, sysm.dt, sysm.size_table, sysm.phys, n_steps, return_ms=True)
+            ms = ms_step * n_steps
+            line["reference_cuda_gb300"] = {
+                "value": (ng + n_dust) * n_steps / (ms / 1e3), "unit": UNIT, "ms_per_run": ms,
+                "what": "the reference's own kernels compiled unmodified for sm_103a, the whole run, CUDA events"}
+    except Exception as e:
         line["reference_cuda_gb300"] = {"unavailable": str(e)[:200]}
     print(json.dumps(line), flush=True)
 
@@ -722,6 +829,9 @@ def main():
         return
     if args.workload == "scale":
         run_scale(args, world, rank, local)
+        return
+    if args.workload == "solar" and args.impl == "ours":
+        run_solar(args, world, rank, local)
         return
     if args.impl == "reference":
         run_reference(args, world, rank, local)

@@ -108,7 +108,7 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
     __shared__ __align__(8) unsigned long long mbar[2];
     BodyPair* const tiles = reinterpret_cast<BodyPair*>(smem);
     const int tid = threadIdx.x;
-    const int i = blockIdx.x * kThreads + tid;
+    const int i = blockIdx.x * blockDim.x + tid;
     const int ng = a.n_grav;
     const int t = ng + i;
 
@@ -284,8 +284,9 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
-    const int blocks = (a.n_dust + kThreads - 1) / kThreads;
-    dust_rk4_mixed_kernel<<<blocks, kThreads, smem, st>>>(s, a, ms, bins);
+    const int threads = dust_block_threads(a.n_dust);   // 256 unless the grains are few
+    const int blocks = (a.n_dust + threads - 1) / threads;
+    dust_rk4_mixed_kernel<<<blocks, threads, smem, st>>>(s, a, ms, bins);
     return cudaGetLastError();
 }
 

@@ -157,6 +157,12 @@ int det_step_scan(DetStepScratch*& d, const ddx_state& s, int n_grav, cudaStream
                   std::vector<double>& rr, std::vector<double>& mi, double& m0);
 void det_step_free(DetStepScratch*& d);
 
+// Threads per block of the one-tracer-per-thread dust kernels: 256, halved (down to 64)
+// while the grid would cover fewer than two blocks per SM.  FP64 runs at 1/73 of the FP32
+// rate, so a few thousand grains on 256-thread blocks leave most SMs idle for tens of
+// microseconds; smaller blocks spread them over the whole GPU.
+int dust_block_threads(int n_dust);
+
 // ddx_optics_prep.cu: the dust-temperature table (host arrays in and out; synchronizes).
 int dust_temp_run(int n_grid, int n_wav, const double* w, const double* in, const double* Qabs, double dist,
                   double* Rmin_AU, double* Rmax_AU, double* Td, cudaStream_t st);

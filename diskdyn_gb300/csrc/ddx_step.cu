@@ -389,17 +389,33 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
     return cudaGetLastError();
 }
 
+int dust_block_threads(int n_dust) {
+    static int sm_count[128] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 128) return kDustThreads;
+    if (sm_count[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+        sm_count[dev] = n;
+    }
+    int threads = kDustThreads;
+    while (threads > 64 && (n_dust + threads - 1) / threads < 2 * sm_count[dev]) threads /= 2;
+    return threads;
+}
+
 cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                         const SizeBin* bins, int precision, cudaStream_t st) {
     if (a.n_dust <= 0) return cudaSuccess;
-    const int blocks = (a.n_dust + kDustThreads - 1) / kDustThreads;
+    const int threads = dust_block_threads(a.n_dust);
+    const int blocks = (a.n_dust + threads - 1) / threads;
     const size_t smem = (size_t)kDustTile * 32;
     if (precision == DDX_PREC_MIXED) {
         return launch_dust_mixed(s, a, ms, bins, st);
     } else if (a.mode == DDX_MODE_REFERENCE) {
-        dust_rk4_kernel<kDustFP64Exact><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
+        dust_rk4_kernel<kDustFP64Exact><<<blocks, threads, smem, st>>>(s, a, ms, bins);
     } else {
-        dust_rk4_kernel<kDustFP64><<<blocks, kDustThreads, smem, st>>>(s, a, ms, bins);
+        dust_rk4_kernel<kDustFP64><<<blocks, threads, smem, st>>>(s, a, ms, bins);
     }
     return cudaGetLastError();
 }
