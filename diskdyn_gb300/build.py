@@ -37,14 +37,21 @@ def _headers_mtime() -> float:
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 
+# Host-only sources (file formats): plain C++, no contraction, like the reference's host code.
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(ROOT / "include")]
+
+
 def _compile(src: Path, hmt: float, verbose: bool) -> Path:
     obj = OBJ / (src.stem + ".o")
     if obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, hmt):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    if src.suffix == ".cpp":
+        cmd = [shutil.which("g++") or "g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)]
+    else:
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"compile failed on {src.name}:\n{r.stdout}\n{r.stderr}")
     if verbose and r.stderr.strip():
         print(r.stderr)
     return obj
@@ -52,11 +59,11 @@ def _compile(src: Path, hmt: float, verbose: bool) -> Path:
 
 def build(verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
-    srcs = sorted(CSRC.glob("*.cu"))
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     hmt = _headers_mtime()
     # objects built with other flags are stale
     stamp = OBJ / "flags.txt"
-    flags = " ".join(ARCH + NVCC_FLAGS)
+    flags = " ".join(ARCH + NVCC_FLAGS + CXX_FLAGS)
     if not stamp.exists() or stamp.read_text() != flags:
         for o in OBJ.glob("*.o"):
             o.unlink()

@@ -165,6 +165,7 @@ const char* ddx_status_string(int status) {
         case DDX_ERR_RANGE: return "size beyond limit";
         case DDX_ERR_TIMEOUT: return "device-side wait timed out";
         case DDX_ERR_NONFINITE: return "non-finite value";
+        case DDX_ERR_IO: return "file input/output failed";
         default: return "unknown status";
     }
 }

@@ -32,6 +32,7 @@ extern "C" {
 #define DDX_ERR_RANGE       5   /* a size is beyond a documented limit */
 #define DDX_ERR_TIMEOUT     6   /* a bounded device-side wait gave up */
 #define DDX_ERR_NONFINITE   7   /* NaN/Inf found where a finite value is required */
+#define DDX_ERR_IO          8   /* a file could not be opened, read or written */
 
 /* Arithmetic of the force stage. */
 #define DDX_PREC_FP64   0   /* every operation in FP64, like the reference */

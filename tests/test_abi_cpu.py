@@ -7,9 +7,12 @@ from conftest import ROOT
 
 
 def header_functions():
-    txt = (ROOT / "include" / "diskdyn_gb300.h").read_text()
-    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(ddx_\w+)\s*\(", txt)))
+    names = set()
+    for h in ("diskdyn_gb300.h", "diskdyn_gb300_io.h"):
+        txt = (ROOT / "include" / h).read_text()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names |= set(re.findall(r"\b(ddx_\w+)\s*\(", txt))
+    return sorted(names)
 
 
 def test_header_declares_core_entry_points():
