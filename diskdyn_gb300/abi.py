@@ -53,6 +53,11 @@ class View(C.Structure):
 # (name, restype, argtypes) of every symbol include/diskdyn_gb300.h declares.
 SIGNATURES = [
     ("ddx_param_read", C.c_int, [C.c_char_p, C.c_void_p]),
+    ("ddx_dat_write", C.c_int, [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ddx_dat_read", C.c_int, [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ddx_sed_write", C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("ddx_fits_write", C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double,
+                                 C.c_double]),
     ("ddx_abi_version", C.c_int, []),
     ("ddx_status_string", C.c_char_p, [C.c_int]),
     ("ddx_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int]),

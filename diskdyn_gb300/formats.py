@@ -1,5 +1,6 @@
 """Python view of the reference-format file functions of libddx.so
-(include/diskdyn_gb300_io.h): the parameter-file parser."""
+(include/diskdyn_gb300_io.h): the parameter-file parser, the data (restart) file writer
+and reader, the SED file and FITS image writers."""
 from __future__ import annotations
 
 import ctypes as C
@@ -42,7 +43,28 @@ class Param(C.Structure):
                 ("rho", C.c_double), ("kqe", C.c_double), ("comp", C.c_char * STR),
                 ("n_disks", C.c_int), ("disks", Disk * MAX_DISKS),
                 ("n_blobs", C.c_int), ("blobs", Blob * MAX_BLOBS),
-                ("name_stub", C.c_char * STR), ("usage_code", C.c_int)]
+                ("name_stub", C.c_char * STR), ("usage_code", C.c_int),
+                ("amin", C.c_double), ("amax", C.c_double), ("mmin", C.c_double), ("mmax", C.c_double),
+                ("f", C.c_double), ("n_grid", C.c_int), ("n_wav", C.c_int), ("n_theta", C.c_int),
+                ("n_dust", C.c_int), ("seed", C.c_longlong)]
+
+
+class DatRun(C.Structure):
+    _fields_ = [("time", C.c_double), ("dt", C.c_double), ("tlastd", C.c_double), ("tlastf", C.c_double),
+                ("tlasts", C.c_double), ("Rmax", C.c_double), ("nR", C.c_int), ("n_mass", C.c_int),
+                ("n_dust", C.c_int), ("n_all", C.c_int)]
+
+
+class HostState(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("x", "y", "z", "vx", "vy", "vz", "N", "m", "id")] + [("cap", C.c_longlong)]
+
+
+STATE_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "N", "m", "id")
+
+
+def host_state(arrays: dict) -> HostState:
+    """HostState over numpy arrays (float64; id int32), which must stay alive."""
+    return HostState(*[arrays[k].ctypes.data for k in STATE_FIELDS], len(arrays["x"]))
 
 
 class ParamError(RuntimeError):
@@ -51,13 +73,21 @@ class ParamError(RuntimeError):
         self.status, self.usage_code = status, usage_code
 
 
-def read_param(path: str) -> dict:
-    """Parse a DiskDyn parameter file with ddx_param_read; the reference's fields and units."""
+def read_param_struct(path: str) -> Param:
     lib = abi.load()
     p = Param()
     st = lib.ddx_param_read(str(path).encode(), C.byref(p))
     if st != 0:
         raise ParamError(st, p.usage_code)
+    return p
+
+
+def read_param(path: str) -> dict:
+    """Parse a DiskDyn parameter file with ddx_param_read; the reference's fields and units."""
+    return param_dict(read_param_struct(path))
+
+
+def param_dict(p: Param) -> dict:
     d = {k: getattr(p, k) for k, _ in Param._fields_
          if k not in ("sptype", "specfile", "comp", "name_stub", "wavs", "planets", "disks", "blobs", "nwavs",
                       "n_planets", "n_disks", "n_blobs", "usage_code")}
@@ -68,3 +98,46 @@ def read_param(path: str) -> dict:
     d["disks"] = [{f: getattr(p.disks[k], f) for f, _ in Disk._fields_} for k in range(p.n_disks)]
     d["blobs"] = [{f: getattr(p.blobs[k], f) for f, _ in Blob._fields_} for k in range(p.n_blobs)]
     return d
+
+
+def write_dat(path, version: str, p: Param, run: DatRun, arrays: dict, beta) -> None:
+    """ddx_dat_write: the data file of state `arrays` (massive bodies first)."""
+    import numpy as np
+    beta = np.ascontiguousarray(beta, np.float32)
+    st = abi.load().ddx_dat_write(str(path).encode(), version.encode(), C.byref(p), C.byref(run),
+                                  C.byref(host_state(arrays)), C.c_void_p(beta.ctypes.data))
+    abi.check(st, "ddx_dat_write")
+
+
+def read_dat(path, version: str, nR: int = 100, Rmax: float = 0.0):
+    """ddx_dat_read: (param struct, run struct, state arrays) of a data file.  Rmax (AU,
+    the temperature table's outer radius) is not in the file and is passed through."""
+    import numpy as np
+    lib = abi.load()
+    p, run = Param(), DatRun(nR=nR, Rmax=Rmax)
+    st = lib.ddx_dat_read(str(path).encode(), version.encode(), C.byref(p), C.byref(run), None)
+    if st != 0:
+        raise ParamError(st, p.usage_code)
+    arrays = {k: np.zeros(run.n_all, np.int32 if k == "id" else np.float64) for k in STATE_FIELDS}
+    run.nR = nR
+    st = lib.ddx_dat_read(str(path).encode(), version.encode(), C.byref(p), C.byref(run),
+                          C.byref(host_state(arrays)))
+    if st != 0:
+        raise ParamError(st, p.usage_code)
+    return p, run, arrays
+
+
+def write_sed(path, version: str, w, influx, exc) -> None:
+    import numpy as np
+    w, influx, exc = (np.ascontiguousarray(a, np.float64) for a in (w, influx, exc))
+    abi.check(abi.load().ddx_sed_write(str(path).encode(), version.encode(), len(w), C.c_void_p(w.ctypes.data),
+                                       C.c_void_p(influx.ctypes.data), C.c_void_p(exc.ctypes.data)), "ddx_sed_write")
+
+
+def write_fits(path, version: str, image, wavelength_m: float, fov_AU: float, dist_m: float) -> None:
+    """ddx_fits_write of one x-major image (xsize, ysize), as ddx_image returns it."""
+    import numpy as np
+    F = np.ascontiguousarray(image, np.float64)
+    xs, ys = F.shape
+    abi.check(abi.load().ddx_fits_write(str(path).encode(), version.encode(), xs, ys, C.c_void_p(F.ctypes.data),
+                                        float(wavelength_m), float(fov_AU), float(dist_m)), "ddx_fits_write")

@@ -63,7 +63,63 @@ typedef struct {
     char name_stub[DDX_PARAM_STR];
     int usage_code;                /* on a rejected file: the reference's exit_with_usage
                                       code (src/error.cu), else 0 */
+    /* Set after the parameter file by the optics set-up (the reference's detminmax and
+     * optical-table read, src/read_in.cu:268-342, 419-505); written to and read from the
+     * data-file header.  Zero after ddx_param_read. */
+    double amin, amax, mmin, mmax, f;  /* dust size (m) and mass (kg) range, ln mass-bin step */
+    int n_grid, n_wav, n_theta, n_dust;
+    long long seed;
 } ddx_param;
+
+/* Run-time values of a data file (Grid members, src/ddyn.cuh): time, step and the times of
+ * the last outputs (yr), the radius-grid size and the outer radius of the temperature
+ * table (AU; bodies beyond it, or inside the star, are written commented out with "## ").
+ * n_mass counts the massive bodies after the star and planets. */
+typedef struct {
+    double time, dt, tlastd, tlastf, tlasts, Rmax;
+    int nR;
+    int n_mass, n_dust, n_all;
+} ddx_dat_run;
+
+/* Host state of every body, massive first, in the GPU state's units (mass * 4 pi^2 in
+ * Msun); cap = capacity of each array for ddx_dat_read. */
+typedef struct {
+    double *x, *y, *z, *vx, *vy, *vz, *N, *m;
+    int *id;
+    long long cap;
+} ddx_host_state;
+
+/* Data file in the reference's layout (Grid::writegrid, src/grid.cu:441-673): the header
+ * of configuration and run values, then the star and planets and every other body, one
+ * per line: x y z [AU] vx vy vz [AU/yr] N, m [kg], radius [m] and beta of its size bin,
+ * id.  beta[n_grid] is the size-bin table (bodies with id < 0 get 0).  The reference names
+ * the file <stub>_<time %.2f>.dat; the caller passes the path. */
+int ddx_dat_write(const char *path, const char *version, const ddx_param *p, const ddx_dat_run *run,
+                  const ddx_host_state *s, const float *beta);
+
+/* Reads a data file the way the reference's restart does (read_in_model,
+ * src/read_in.cu:736-1014, and Grid::read_in, src/grid.cu:205-310): the header into *p
+ * and *run, the bodies into *s, with the size bin of every body after the planets
+ * recomputed as round(ln(m / mmin) / f) (-1 beyond the grid).  With s == NULL or
+ * s->cap < run->n_all only the header is read (call again with room for run->n_all).
+ * run->nR and run->Rmax are inputs (the file does not hold Rmax; it comes from the
+ * temperature table).  Rejects a file written by another version (usage code 55) or with
+ * another nR (56). */
+int ddx_dat_read(const char *path, const char *version, ddx_param *p, ddx_dat_run *run, ddx_host_state *s);
+
+/* SED file (Grid::write_sed, src/grid.cu:675-691): wavelength [micron], stellar flux and
+ * excess flux [Jy] per table wavelength; w in m, in = the stellar flux table, exc = the
+ * SED of ddx_sed. */
+int ddx_sed_write(const char *path, const char *version, int n_wav, const double *w, const double *in,
+                  const double *exc);
+
+/* FITS image (Grid::write_image, src/fits.cu:9-85): a primary 2-D FP64 image of
+ * xsize x ysize pixels, image[y][x] = F[ysize*x + y] (F is x-major, as ddx_image writes
+ * it), with the keys WAVELENG [micron], FLUX (total, Jy), PIXELSCA [arcsec/px],
+ * VERSION, a HISTORY card and DATE.  The reference names the file
+ * <stub>_<wavelength %.2f>_<time %.3f>.fits. */
+int ddx_fits_write(const char *path, const char *version, int xsize, int ysize, const double *F,
+                   double wavelength_m, double fov_AU, double dist_m);
 
 /* Parses a DiskDyn parameter file the way read_in_param does (src/read_in.cu:508-733):
  * the same tokeniser, section order, unit conversions, star at planet 0, planets through

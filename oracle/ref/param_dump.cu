@@ -18,17 +18,38 @@ cudadata ccuda;
 cudaconf* prop;
 
 int read_in_param(char* param);
+int read_in_model(char* model, const char* ver);
 
 static void hexd(const char* key, double v, bool comma = true) { printf("\"%s\": \"%a\"%s", key, v, comma ? ", " : ""); }
 static void str(const char* key, const char* s, bool comma = true) {
     printf("\"%s\": \"%s\"%s", key, s ? s : "", comma ? ", " : "");
 }
 
+// param_dump <file.param>             : read_in_param
+// param_dump -m <file.dat> <version>   : read_in_model (the data-file header), plus the
+//                                        fields only a data file sets
 int main(int argc, char** argv) {
     if (argc < 2) return 2;
-    read_in_param(argv[1]);
+    const bool model = argc >= 4 && argv[1][0] == '-' && argv[1][1] == 'm';
+    if (model) read_in_model(argv[2], argv[3]);
+    else read_in_param(argv[1]);
     const configdata* c = &cconfig;
     printf("{");
+    if (model) {
+        hexd("amin", c->amin); hexd("amax", c->amax); hexd("mmin", c->mmin); hexd("mmax", c->mmax);
+        hexd("f", c->f);
+        printf("\"n_grid\": %d, \"n_wav\": %d, \"n_theta\": %d, \"n_dust\": %d, ", c->n_grid, c->n_wav, c->n_theta,
+               c->n_dust);
+        printf("\"disks_extra\": [");
+        for (int k = 0; k < c->n_disks; ++k)
+            printf("[\"%a\", \"%a\", \"%a\"]%s", c->disks[k].dmax, c->disks[k].dmmax, c->disks[k].C,
+                   k + 1 < c->n_disks ? ", " : "");
+        printf("], \"blobs_extra\": [");
+        for (int k = 0; k < c->n_blobs; ++k)
+            printf("[\"%a\", \"%a\", \"%a\"]%s", c->blobs[k].dmax, c->blobs[k].dmmax, c->blobs[k].C,
+                   k + 1 < c->n_blobs ? ", " : "");
+        printf("], ");
+    }
     printf("\"verb\": %d, \"gpuid\": %d, \"gl\": %d, ", c->verb, c->gpuid, c->gl);
     hexd("t_gl", c->t_gl); hexd("t_write", c->t_write); hexd("t_fits", c->t_fits); hexd("t_sed", c->t_sed);
     hexd("t_end", c->t_end);
