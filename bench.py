@@ -814,6 +814,22 @@ def run_imaging(args, world, rank, local):
                         "gpu_ms": t_g * 1e3, "cpu_oracle_ms": t_c * 1e3, "cpu_cores": os.cpu_count(),
                         "max_rel_diff": float(np.max(np.abs(Td_g / Td_c - 1.0))),
                         "rmin_rel_diff": abs(rmin_g / rmin_c - 1.0)}
+    # the size grid and its tables (interpolate_dust_to_grid + calculate_beta) of a table
+    # file of Mie size: 40 radii x 200 wavelengths x 181 angles onto 218 bins
+    w_m, in_m, tab = synth.mie_table()
+    grid = dict(n_grid=218, amin=1.3e-7, amax=float(tab["s"][-1]), dmax=float(tab["s"][-1]), kqe=3e-3, radQ=1,
+                SWQ=1, rho=3300.0, dist=7.7 * synth.PC, mstar=2.1 * 4 * np.pi ** 2, mloss=1e-13, vsw=5e5)
+    eng.dust_grid(w_m, in_m, tab, **grid)
+    t0 = time.perf_counter()
+    g_out = eng.dust_grid(w_m, in_m, tab, **grid)
+    t_g = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    c_out = oc.dust_grid(w_m, in_m, tab, **grid)
+    t_c = time.perf_counter() - t0
+    out["dust_grid"] = {"what": "218 bins from a 40 x 200 x 181 table, host arrays in and out",
+                        "gpu_ms": t_g * 1e3, "cpu_oracle_ms": t_c * 1e3, "cpu_cores": 1,
+                        "Qpfunc_max_rel_diff": float(np.max(np.abs(g_out["Qpfunc"] / c_out["Qpfunc"] - 1.0))),
+                        "beta_identical": bool(np.array_equal(g_out["beta"], c_out["beta"]))}
     line = {"metric": "imaging particle-wavelengths/s", "workload": "imaging", "n_particles": n,
             "n_img": n_img, "n_wav": len(o["w"]), "image": [s.view["xsize"], s.view["ysize"]],
             "results": out, "l2": "flushed between timed calls"}

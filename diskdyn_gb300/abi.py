@@ -22,7 +22,7 @@ DDX_NR = 100
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "device allocation failed",
           4: "required table not set", 5: "size beyond limit", 6: "device-side wait timed out",
-          7: "non-finite value"}
+          7: "non-finite value", 8: "file could not be opened, read or written"}
 
 
 class DDXError(RuntimeError):
@@ -50,6 +50,19 @@ class View(C.Structure):
                 ("xsize", C.c_int), ("ysize", C.c_int)]
 
 
+class OpticalTable(C.Structure):
+    """ddx_optical_table: host pointers to s[n_size], Qabs/Qsca[n_size][n_wav] and
+    Qpfunc[n_size][n_theta][n_wav]."""
+    _fields_ = [("n_size", C.c_int), ("n_wav", C.c_int), ("n_theta", C.c_int), ("s", C.c_void_p),
+                ("Qabs", C.c_void_p), ("Qsca", C.c_void_p), ("Qpfunc", C.c_void_p)]
+
+
+class GridSetup(C.Structure):
+    _fields_ = [("n_grid", C.c_int), ("amin", C.c_double), ("amax", C.c_double), ("dmax", C.c_double),
+                ("kqe", C.c_double), ("radQ", C.c_int), ("SWQ", C.c_int), ("rho", C.c_double),
+                ("dist", C.c_double), ("mstar", C.c_double), ("mloss", C.c_double), ("vsw", C.c_double)]
+
+
 # (name, restype, argtypes) of every symbol include/diskdyn_gb300.h declares.
 SIGNATURES = [
     ("ddx_param_read", C.c_int, [C.c_char_p, C.c_void_p]),
@@ -58,6 +71,12 @@ SIGNATURES = [
     ("ddx_sed_write", C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("ddx_fits_write", C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double,
                                  C.c_double]),
+    ("ddx_optical_read", C.c_int, [C.c_char_p, C.POINTER(OpticalTable), C.c_void_p, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]),
+    ("ddx_spec_read", C.c_int, [C.c_char_p, C.c_double, C.c_double, C.POINTER(C.c_int), C.c_void_p, C.c_void_p,
+                                C.c_int]),
+    ("ddx_stellar_grid", C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]),
     ("ddx_abi_version", C.c_int, []),
     ("ddx_status_string", C.c_char_p, [C.c_int]),
     ("ddx_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
@@ -95,6 +114,9 @@ SIGNATURES = [
                                C.c_void_p]),
     ("ddx_dust_temp", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p, C.c_void_p]),
+    ("ddx_dust_grid", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(OpticalTable),
+                                C.POINTER(GridSetup), C.POINTER(OpticalTable), C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
     ("ddx_sync_status", C.c_int, [C.c_void_p, C.c_void_p]),
     ("ddx_debug_lose_tile_copy", C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong]),
     ("ddx_probe_fma_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

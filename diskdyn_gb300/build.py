@@ -33,7 +33,7 @@ def nvcc() -> str:
 
 
 def _headers_mtime() -> float:
-    hs = list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    hs = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 

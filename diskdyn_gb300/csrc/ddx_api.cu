@@ -377,6 +377,21 @@ int ddx_dust_temp(ddx_ctx* c, int n_grid, int n_wav, const double* w, const doub
     return dust_temp_run(n_grid, n_wav, w, in, Qabs, dist, Rmin_AU, Rmax_AU, Td, (cudaStream_t)stream);
 }
 
+int ddx_dust_grid(ddx_ctx* c, int n_wav, const double* w, const double* in, const ddx_optical_table* file,
+                  const ddx_grid_setup* g, ddx_optical_table* grid, float* q, float* beta, float* betasw,
+                  double* Lum, double* betaswconst, void* stream) {
+    if (!c || !w || !in || !file || !g || !grid || !q || !beta || !betasw || !Lum || !betaswconst) return DDX_ERR_ARG;
+    if (!file->s || !file->Qabs || !file->Qsca || !file->Qpfunc) return DDX_ERR_ARG;
+    if (!grid->s || !grid->Qabs || !grid->Qsca || !grid->Qpfunc) return DDX_ERR_ARG;
+    if (n_wav < 2 || file->n_wav != n_wav || grid->n_wav != n_wav) return DDX_ERR_ARG;
+    if (file->n_theta < 1 || grid->n_theta != file->n_theta || (g->radQ == 1 && file->n_theta < 2)) return DDX_ERR_ARG;
+    if (file->n_size < 2 || g->n_grid < 2 || grid->n_size != g->n_grid) return DDX_ERR_ARG;
+    if (!(g->amin > 0.0) || !(g->amax > g->amin) || !(g->rho > 0.0) || !(g->mstar > 0.0)) return DDX_ERR_ARG;
+    if (g->n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
+    cudaSetDevice(c->device);
+    return dust_grid_run(n_wav, w, in, *file, *g, *grid, q, beta, betasw, Lum, betaswconst, (cudaStream_t)stream);
+}
+
 int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,
                         int ckpt_every, const ddx_phys* phys, const ddx_view* view, const int* wj, int n_img,
                         double* image, void* stream) {

@@ -166,4 +166,9 @@ int dust_block_threads(int n_dust);
 // ddx_optics_prep.cu: the dust-temperature table (host arrays in and out; synchronizes).
 int dust_temp_run(int n_grid, int n_wav, const double* w, const double* in, const double* Qabs, double dist,
                   double* Rmin_AU, double* Rmax_AU, double* Td, cudaStream_t st);
+// ddx_optics_prep.cu: the size grid and its optical, beta and beta_sw tables (host arrays
+// in and out, arguments checked by the caller; synchronizes).
+int dust_grid_run(int n_wav, const double* w, const double* in, const ddx_optical_table& file,
+                  const ddx_grid_setup& g, ddx_optical_table& grid, float* q, float* beta, float* betasw,
+                  double* Lum, double* betaswconst, cudaStream_t st);
 }  // namespace ddx

@@ -18,8 +18,11 @@
 
 #include "../../include/diskdyn_gb300.h"
 #include "../../include/diskdyn_gb300_io.h"
+#include "ddx_host.h"
 
 namespace {
+
+using ddx_host::split;
 
 constexpr double kPI = 3.14159265358979323846;
 constexpr double kGrav = 4.0 * kPI * kPI;
@@ -165,40 +168,8 @@ void write_header(FILE* fw, const char* ver, const ddx_param* c, const ddx_dat_r
 }
 
 // ---------------------------------------------------------------------------------------
-// data file reader: the reference's tokeniser and line numbering
+// data file reader: the reference's tokeniser (ddx_host::split) and line numbering
 // ---------------------------------------------------------------------------------------
-
-bool is_sep(int c) { return c == 64 || c == 32 || c == 13 || c == 10 || c == 9; }
-
-int split(char* buf, char** tok, int max) {
-    int n = 0;
-    bool in_tok = false, in_quote = false;
-    while (*buf && n < max) {
-        const bool sep = is_sep(*buf);
-        if (!sep && !in_tok) {
-            tok[n++] = buf;
-            in_tok = true;
-            in_quote = (*buf == '"');
-            ++buf;
-        } else if (in_tok && (!sep || in_quote)) {
-            if (*buf == '"') in_quote = !in_quote;
-            ++buf;
-        } else if (in_tok) {
-            *buf++ = 0;
-            in_tok = false;
-        } else {
-            ++buf;
-        }
-    }
-    tok[n] = nullptr;
-    for (int k = 0; k < n; ++k) {
-        char* w = tok[k];
-        for (char* r = tok[k]; *r; ++r)
-            if (*r != '"') *w++ = *r;
-        *w = 0;
-    }
-    return n;
-}
 
 void scan(const char* s, double& v) {
     if (!s) return;

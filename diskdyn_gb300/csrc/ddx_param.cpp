@@ -13,18 +13,11 @@
 
 #include "../../include/diskdyn_gb300.h"
 #include "../../include/diskdyn_gb300_io.h"
+#include "ddx_host.h"
+
+namespace ddx_host {
 
 namespace {
-
-// Constants of src/ddyn.cuh:17-38.
-constexpr double kPI = 3.14159265358979323846;
-constexpr double kGrav = 4.0 * kPI * kPI;
-constexpr double kAU = 1.49598e11;
-constexpr double kMSun = 1.98892e30;
-constexpr double kRSun = 695700000.0;
-constexpr double kYear = 3.1556926e7;
-constexpr double kPc = 3.08567758149137e16;
-constexpr double kMEarth = 5.97e24;
 
 // The reference's separator set: '@', space, CR, LF and tab.
 bool is_sep(int c) { return c == 64 || c == 32 || c == 13 || c == 10 || c == 9; }
@@ -37,9 +30,8 @@ void drop_quotes(char* s) {
     *w = 0;
 }
 
-// Splits buf into at most `max` tokens at separators outside double quotes.  Like the
-// reference, scanning stops once the max-th token has started, so that token runs to the
-// end of the line.
+}  // namespace
+
 int split(char* buf, char** tok, int max) {
     int n = 0;
     bool in_tok = false, in_quote = false;
@@ -64,6 +56,22 @@ int split(char* buf, char** tok, int max) {
     for (int k = 0; k < n; ++k) drop_quotes(tok[k]);
     return n;
 }
+
+}  // namespace ddx_host
+
+namespace {
+
+using ddx_host::split;
+
+// Constants of src/ddyn.cuh:17-38.
+constexpr double kPI = 3.14159265358979323846;
+constexpr double kGrav = 4.0 * kPI * kPI;
+constexpr double kAU = 1.49598e11;
+constexpr double kMSun = 1.98892e30;
+constexpr double kRSun = 695700000.0;
+constexpr double kYear = 3.1556926e7;
+constexpr double kPc = 3.08567758149137e16;
+constexpr double kMEarth = 5.97e24;
 
 // sscanf("%lg") / ("%d") / ("%ld") semantics: the target keeps its value when the token
 // does not start with a number.

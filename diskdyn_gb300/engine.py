@@ -211,6 +211,32 @@ class Engine:
                                          C.c_void_p(_stream_handle(stream))), "ddx_dust_temp")
         return Td, rmin.value, rmax.value
 
+    def dust_grid(self, w, influx, table: dict, n_grid: int, amin: float, amax: float, dmax: float, kqe: float,
+                  radQ: int, SWQ: int, rho: float, dist: float, mstar: float, mloss: float, vsw: float,
+                  stream=None) -> dict:
+        """interpolate_dust_to_grid + calculate_beta on the GPU.  `table` holds the optical
+        file's s, Qabs, Qsca, Qpfunc (formats.read_optical); returns the grid's s, q,
+        Qabs, Qsca, Qpfunc, beta, betasw, Lum and betaswconst."""
+        w = np.ascontiguousarray(w, np.float64)
+        influx = np.ascontiguousarray(influx, np.float64)
+        src = {k: np.ascontiguousarray(table[k], np.float64) for k in ("s", "Qabs", "Qsca", "Qpfunc")}
+        nd, nt, nw = src["Qpfunc"].shape
+        out = {"s": np.zeros(n_grid), "Qabs": np.zeros((n_grid, nw)), "Qsca": np.zeros((n_grid, nw)),
+               "Qpfunc": np.zeros((n_grid, nt, nw)), "q": np.zeros(n_grid, np.float32),
+               "beta": np.zeros(n_grid, np.float32), "betasw": np.zeros(n_grid, np.float32)}
+        ptr = lambda a: a.ctypes.data
+        ft = abi.OpticalTable(nd, nw, nt, *(ptr(src[k]) for k in ("s", "Qabs", "Qsca", "Qpfunc")))
+        gt = abi.OpticalTable(n_grid, nw, nt, *(ptr(out[k]) for k in ("s", "Qabs", "Qsca", "Qpfunc")))
+        gs = abi.GridSetup(int(n_grid), float(amin), float(amax), float(dmax), float(kqe), int(radQ), int(SWQ),
+                           float(rho), float(dist), float(mstar), float(mloss), float(vsw))
+        lum, bsc = C.c_double(), C.c_double()
+        abi.check(self.lib.ddx_dust_grid(self.ctx, nw, C.c_void_p(ptr(w)), C.c_void_p(ptr(influx)), C.byref(ft),
+                                         C.byref(gs), C.byref(gt), C.c_void_p(ptr(out["q"])),
+                                         C.c_void_p(ptr(out["beta"])), C.c_void_p(ptr(out["betasw"])), C.byref(lum),
+                                         C.byref(bsc), C.c_void_p(_stream_handle(stream))), "ddx_dust_grid")
+        out["Lum"], out["betaswconst"] = lum.value, bsc.value
+        return out
+
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
         bounded device-side wait since the last call, else 0."""

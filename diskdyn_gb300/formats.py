@@ -141,3 +141,47 @@ def write_fits(path, version: str, image, wavelength_m: float, fov_AU: float, di
     xs, ys = F.shape
     abi.check(abi.load().ddx_fits_write(str(path).encode(), version.encode(), xs, ys, C.c_void_p(F.ctypes.data),
                                         float(wavelength_m), float(fov_AU), float(dist_m)), "ddx_fits_write")
+
+
+def read_optical(path) -> dict:
+    """ddx_optical_read: the Mie table file as a dict of s (m), w (m), Qabs, Qsca
+    (n_size, n_wav), Qpfunc (n_size, n_theta, n_wav), dmin and dmax (m)."""
+    import numpy as np
+    lib = abi.load()
+    t = abi.OpticalTable()
+    dmin, dmax = C.c_double(), C.c_double()
+    abi.check(lib.ddx_optical_read(str(path).encode(), C.byref(t), None, C.byref(dmin), C.byref(dmax)),
+              "ddx_optical_read")
+    nd, nw, nt = t.n_size, t.n_wav, t.n_theta
+    d = {"s": np.zeros(nd), "w": np.zeros(nw), "Qabs": np.zeros((nd, nw)), "Qsca": np.zeros((nd, nw)),
+         "Qpfunc": np.zeros((nd, nt, nw))}
+    t.s, t.Qabs, t.Qsca, t.Qpfunc = (d[k].ctypes.data for k in ("s", "Qabs", "Qsca", "Qpfunc"))
+    abi.check(lib.ddx_optical_read(str(path).encode(), C.byref(t), C.c_void_p(d["w"].ctypes.data), C.byref(dmin),
+                                   C.byref(dmax)), "ddx_optical_read")
+    d["dmin"], d["dmax"] = dmin.value, dmax.value
+    return d
+
+
+def read_spec(path, rstar_AU: float, dist_m: float):
+    """ddx_spec_read: (wavelengths, fluxes scaled to the observer) of a spectrum file."""
+    import numpy as np
+    lib = abi.load()
+    n = C.c_int()
+    abi.check(lib.ddx_spec_read(str(path).encode(), rstar_AU, dist_m, C.byref(n), None, None, 0), "ddx_spec_read")
+    w, F = np.zeros(n.value), np.zeros(n.value)
+    abi.check(lib.ddx_spec_read(str(path).encode(), rstar_AU, dist_m, C.byref(n), C.c_void_p(w.ctypes.data),
+                                C.c_void_p(F.ctypes.data), n.value), "ddx_spec_read")
+    return w, F
+
+
+def stellar_grid(w, spec_w, spec_F, wavs=()):
+    """ddx_stellar_grid: (in[n_wav], wj[len(wavs)])."""
+    import numpy as np
+    w, spec_w, spec_F = (np.ascontiguousarray(a, np.float64) for a in (w, spec_w, spec_F))
+    wavs = np.ascontiguousarray(wavs, np.float64)
+    influx = np.zeros(w.size)
+    wj = np.zeros(max(wavs.size, 1), np.int32)
+    P = lambda a: C.c_void_p(a.ctypes.data)
+    abi.check(abi.load().ddx_stellar_grid(w.size, P(w), spec_w.size, P(spec_w), P(spec_F), wavs.size, P(wavs),
+                                          P(influx), P(wj)), "ddx_stellar_grid")
+    return influx, wj[:wavs.size]

@@ -274,6 +274,26 @@ def hg_optics(n_grid=64, n_theta=181, n_wav=200, wmin=0.5e-6, wmax=850e-6, Teff=
             "Rmin": Rmin, "Rmax": Rmax, "size": size, "g": gg}
 
 
+def mie_table(n_size=40, n_wav=200, n_theta=181, smin=1e-7, smax=1e-4, Teff=9000.0, Rstar=1.8 * RSun,
+              dist=7.7 * PC, seed=SEED):
+    """An optical table file's contents at the size a Mie run gives (n_size radii from smin
+    to smax, n_wav wavelengths from 0.1 um to 1 mm, n_theta angles): Q_abs and Q_sca smooth in
+    the size parameter x = 2 pi s / lambda, Henyey-Greenstein phase functions with g rising
+    with x, every value positive; with a blackbody star seen from `dist`.
+    Returns (w, in, {"s", "Qabs", "Qsca", "Qpfunc"})."""
+    rng = np.random.default_rng(seed)
+    s = smin * np.exp(np.log(smax / smin) * np.arange(n_size) / (n_size - 1))
+    w = 1e-7 * np.exp(np.log(1e4) * np.arange(n_wav) / (n_wav - 1))
+    x = 2 * PI * s[:, None] / w[None, :]
+    Qabs = x / (1 + x) * (1 + 0.1 * rng.random((n_size, n_wav))) + 1e-5
+    Qsca = 2 * x ** 4 / (1 + x ** 4) + 1e-8
+    mu = np.arange(n_theta) * 2.0 / (n_theta - 1) - 1.0
+    gg = (0.85 * x / (1 + x))[:, None, :]
+    Qp = Qsca[:, None, :] * (1 - gg ** 2) / (1 + gg ** 2 - 2 * gg * mu[None, :, None]) ** 1.5
+    influx = PI * planck(Teff, w) * (Rstar / dist) ** 2
+    return w, influx, {"s": s, "Qabs": Qabs, "Qsca": Qsca, "Qpfunc": Qp}
+
+
 def ring_imaging(s: System, xsize=512, ysize=512) -> System:
     """Attach optics and a view to a `dusty_ring` system: HG tables on its grains' size
     bins, grey grains at T = 278.3 L^(1/4) (r/AU)^(-1/2) K, a 7500 K star of 2 Rsun at

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define DDX_ABI_VERSION 2
+#define DDX_ABI_VERSION 3
 
 /* Status codes.  The reference exits the process instead (src/error.cu:75-91,
  * src/ddyn.cuh:400-408). */
@@ -212,6 +212,52 @@ int ddx_det_step(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_step, const
  * on the GPU, one thread per (bin, temperature).  Synchronises `stream`. */
 int ddx_dust_temp(ddx_ctx *ctx, int n_grid, int n_wav, const double *w, const double *in,
                   const double *Qabs, double dist, double *Rmin_AU, double *Rmax_AU, double *Td,
+                  void *stream);
+
+/* Optical tables of one grain composition on n_size grain radii, host pointers: the
+ * reference's cfg->s, Qabs, Qsca and Qpfunc (src/ddyn.cuh), as read from the Mie table
+ * file (ddx_optical_read) or resampled onto the mass grid (ddx_dust_grid). */
+typedef struct {
+    int n_size, n_wav, n_theta;
+    double *s;          /* [n_size] grain radius, m, increasing */
+    double *Qabs;       /* [n_size][n_wav] */
+    double *Qsca;       /* [n_size][n_wav] */
+    double *Qpfunc;     /* [n_size][n_theta][n_wav], n_theta angles uniform in cos(theta) */
+} ddx_optical_table;
+
+/* Inputs of the mass grid and of the radiation-pressure and wind-drag tables, in the
+ * reference's units (cconfig, src/ddyn.cuh). */
+typedef struct {
+    int n_grid;                 /* size bins (detminmax, src/read_in.cu:339) */
+    double amin, amax;          /* smallest and largest grain radius of the grid, m */
+    double dmax;                /* largest radius of the optical table file, m */
+    double kqe;                 /* q = kqe * a * 1e9 per bin */
+    int radQ, SWQ;              /* radiation pressure and stellar-wind drag on (1) or off */
+    double rho;                 /* grain density, kg/m^3 */
+    double dist;                /* distance, m */
+    double mstar;               /* star mass * 4 pi^2 (Msun): cfg->planets[0].m */
+    double mloss;               /* stellar mass-loss rate as the parameter file gives it */
+    double vsw;                 /* stellar-wind speed, m/s */
+} ddx_grid_setup;
+
+/* Size grid and per-bin tables; replaces interpolate_dust_to_grid and calculate_beta
+ * (src/functions.cu:243-300, 338-388), called from Grid::setup (src/grid.cu:74-76).
+ * In (host): the table file's optics `file` on w[n_wav] (m), the stellar flux in[n_wav] of
+ * ddx_stellar_grid and the grid set-up g.  Out (host, caller-allocated): `grid` with
+ * n_size = g->n_grid (s = the bin radii a_i = amin exp(i ln(amax/amin)/(n_grid-1)), the
+ * tables interpolated log-log between the two file sizes around a_i), q[n_grid],
+ * beta[n_grid], betasw[n_grid], *Lum (Lsun) and *betaswconst.  The bin radii, q, betasw, Lum
+ * and the size brackets are computed on the host with the reference's expressions and
+ * rounding; the table interpolation and the phase-function integrals for beta run on the
+ * GPU, with the reference's operation order (no contractions), so they differ from it
+ * only by the CUDA math library's log and exp.  A bin at or below s[0] is interpolated on
+ * the first file interval and one beyond the last size on the last interval (the reference
+ * reads outside its table there).  Returns DDX_ERR_RANGE when the last bin overshoots dmax
+ * by more than 1e-12 (the reference's exit code 54) or n_grid > DDX_MAX_SIZE_BINS.
+ * Synchronises `stream`. */
+int ddx_dust_grid(ddx_ctx *ctx, int n_wav, const double *w, const double *in,
+                  const ddx_optical_table *file, const ddx_grid_setup *g, ddx_optical_table *grid,
+                  float *q, float *beta, float *betasw, double *Lum, double *betaswconst,
                   void *stream);
 
 /* Discrete adjoint of the trajectory and image (no counterpart in the reference).

@@ -7,6 +7,8 @@
 #ifndef DISKDYN_GB300_IO_H
 #define DISKDYN_GB300_IO_H
 
+#include "diskdyn_gb300.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -129,6 +131,41 @@ int ddx_fits_write(const char *path, const char *version, int xsize, int ysize, 
  * reference reads past), DDX_ERR_IO (8) if the file cannot be opened (usage code 3), or
  * DDX_ERR_RANGE (5) beyond the fixed table sizes above. */
 int ddx_param_read(const char *path, ddx_param *p);
+
+/* Mie table file of a grain composition (add_optical_data, src/read_in.cu:419-505; the
+ * layout of the reference's table generator): a first line that is skipped, a header line
+ * "# n_wav n_theta n_size amin amax" (radii in micron), then per size a line "#s <radius>"
+ * (micron), n_wav lines "<wavelength> <Qabs> <Qsca>" (micron) and the n_theta * n_wav
+ * phase-function values ten per line.  Lines are read 254 characters at a time, as the
+ * reference reads them.  With t->s == NULL only the header is read: t->n_size, n_wav,
+ * n_theta, *dmin and *dmax (m).  Otherwise t's counts must be the file's, and t's arrays
+ * and w[n_wav] (m; taken from the first size) are filled.  The values are the reference's
+ * to the bit.  Returns DDX_ERR_IO if the file cannot be opened (the reference's exit code
+ * 39), DDX_ERR_ARG for counts that differ from the header or for data the reference would
+ * write outside its arrays (values before the first size line, more sizes or values than
+ * the header announces). */
+int ddx_optical_read(const char *path, ddx_optical_table *t, double *w, double *dmin, double *dmax);
+
+/* Stellar spectrum file (add_specfile, src/read_in.cu:377-417): lines "<wavelength> <flux>",
+ * '#' lines and lines without two numbers skipped; each flux scaled by
+ * (rstar_AU * AU)^2 / dist_m^2 as the reference scales it.  *nspec = the number of points;
+ * wvl and F (cap entries each) are filled when they are non-NULL and cap >= *nspec, else
+ * only the count is returned.  Returns DDX_ERR_IO if the file cannot be opened (exit code
+ * 39). */
+int ddx_spec_read(const char *path, double rstar_AU, double dist_m, int *nspec, double *wvl, double *F,
+                  int cap);
+
+/* Stellar flux on the table wavelengths and the image wavelength indices
+ * (interpolate_stellar_to_grid, src/functions.cu:302-336): in[j] log-log interpolated in
+ * the spectrum (spec_w, spec_F, nspec >= 2), 0 below its first wavelength or next to a zero
+ * flux, F_last (w_last / w)^4 beyond it; wj[k] = i - 1 for the first i with
+ * w[i] >= wavs[k] (at most n_wav - 2), as the reference sets it (so -1 for wavs[k] == w[0]).
+ * The reference's walk over the spectrum is kept step for step, so the values are its own
+ * to the bit; where it would read past the last spectrum point (a table wavelength equal to
+ * it) the walk stops there.  Returns DDX_ERR_RANGE if an image wavelength lies outside
+ * [w[0], w[n_wav-1]] (the reference's exit code 43). */
+int ddx_stellar_grid(int n_wav, const double *w, int nspec, const double *spec_w, const double *spec_F,
+                     int nwavs, const double *wavs, double *in, int *wj);
 
 #ifdef __cplusplus
 }

@@ -180,3 +180,45 @@ def collide(arrays: dict, i0: int, i1: int, h: float, method: str = "brute", cap
     out = np.zeros((max(total, 1), 2), np.int32)
     f(os_, i0, i1, float(h), _ptr(out), total)
     return out[:total]
+
+
+def stellar_grid(w, spec_w, spec_F, wavs=()):
+    """interpolate_stellar_to_grid (src/functions.cu:302-336): (in[n_wav], wj[len(wavs)]);
+    raises ValueError with the reference's usage code 43 for an image wavelength outside w."""
+    w, spec_w, spec_F = (np.ascontiguousarray(a, np.float64) for a in (w, spec_w, spec_F))
+    wavs = np.ascontiguousarray(wavs, np.float64)
+    influx = np.zeros(w.size)
+    wj = np.zeros(max(wavs.size, 1), np.int32)
+    f = lib().ora_stellar_grid
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    r = f(w.size, _ptr(w), spec_w.size, _ptr(spec_w), _ptr(spec_F), wavs.size, _ptr(wavs), _ptr(influx), _ptr(wj))
+    if r != 0:
+        raise ValueError(f"usage code {r}")
+    return influx, wj[:wavs.size]
+
+
+def dust_grid(w, influx, table: dict, n_grid, amin, amax, dmax, kqe, radQ, SWQ, rho, dist, mstar, mloss, vsw):
+    """interpolate_dust_to_grid + calculate_beta (src/functions.cu:243-300, 338-388) on the
+    optical file's s, Qabs, Qsca, Qpfunc; returns the grid's s, q, Qabs, Qsca, Qpfunc, beta,
+    betasw, Lum, betaswconst.  Raises ValueError with usage code 54 when the last bin
+    overshoots dmax."""
+    w, influx = (np.ascontiguousarray(a, np.float64) for a in (w, influx))
+    src = {k: np.ascontiguousarray(table[k], np.float64) for k in ("s", "Qabs", "Qsca", "Qpfunc")}
+    nd, nt, nw = src["Qpfunc"].shape
+    o = {"s": np.zeros(n_grid), "q": np.zeros(n_grid, np.float32), "Qabs": np.zeros((n_grid, nw)),
+         "Qsca": np.zeros((n_grid, nw)), "Qpfunc": np.zeros((n_grid, nt, nw)), "beta": np.zeros(n_grid, np.float32),
+         "betasw": np.zeros(n_grid, np.float32)}
+    lum, bsc = C.c_double(), C.c_double()
+    f = lib().ora_dust_grid
+    f.restype = C.c_int
+    f.argtypes = ([C.c_int] * 3 + [C.c_void_p] * 6 + [C.c_int] + [C.c_double] * 4 + [C.c_int] * 2 +
+                  [C.c_double] * 5 + [C.c_void_p] * 7 + [C.POINTER(C.c_double)] * 2)
+    r = f(nd, nw, nt, _ptr(src["s"]), _ptr(w), _ptr(src["Qabs"]), _ptr(src["Qsca"]), _ptr(src["Qpfunc"]),
+          _ptr(influx), int(n_grid), float(amin), float(amax), float(dmax), float(kqe), int(radQ), int(SWQ),
+          float(rho), float(dist), float(mstar), float(mloss), float(vsw),
+          *(_ptr(o[k]) for k in ("s", "q", "Qabs", "Qsca", "Qpfunc", "beta", "betasw")), C.byref(lum), C.byref(bsc))
+    if r != 0:
+        raise ValueError(f"usage code {r}")
+    o["Lum"], o["betaswconst"] = lum.value, bsc.value
+    return o

@@ -622,3 +622,114 @@ long long ora_collide_grid(ora_state s, int i0, int i1, double h, int *out, long
     free(cnt); free(own); free(cells);
     return tot;
 }
+
+/* ------------------------------------------------------------------------------------
+ * Stellar flux on the table wavelengths and the image wavelength indices:
+ * interpolate_stellar_to_grid, src/functions.cu:302-336.  sw, sF: the spectrum file's
+ * wavelengths and fluxes (nspec >= 2).  Returns 43, the reference's usage code, if an image
+ * wavelength lies outside w.  The reference walks the spectrum with an index that it steps
+ * back by one after each table wavelength; that walk is kept, with one guard: where it
+ * would read past the last spectrum point (a table wavelength equal to it) it stops there.
+ * wj[j] = i - 1 where i is the first index with w[i] >= wavs[j] (at most n_wav - 2), as in
+ * the reference, so it is -1 for wavs[j] == w[0].
+ * ------------------------------------------------------------------------------------ */
+int ora_stellar_grid(int n_wav, const double *w, int nspec, const double *sw, const double *sF, int nwavs,
+                     const double *wavs, double *in, int *wj) {
+    if (nspec < 2) return -1;
+    int ip = 0;
+    for (int j = 0; j < n_wav; j++) {
+        if (w[j] < sw[0]) {
+            in[j] = 0.0;
+        } else if (w[j] > sw[nspec - 1]) {
+            in[j] = sF[nspec - 1] * pow(sw[nspec - 1] / w[j], 4.0);
+        } else {
+            while (ip < nspec - 1 && sw[ip] <= w[j]) ip++;
+            int im = ip - 1;
+            if (sF[im] != 0 && sF[ip] != 0)
+                in[j] = exp(log(sF[im]) + log(w[j] / sw[im]) * log(sF[ip] / sF[im]) / log(sw[ip] / sw[im]));
+            else
+                in[j] = 0.0;
+            ip--;
+        }
+    }
+    for (int j = 0; j < nwavs; j++) {
+        int i = 0;
+        if (wavs[j] < w[0] || wavs[j] > w[n_wav - 1]) return 43;
+        while (w[i] < wavs[j] && i < n_wav - 2) i++;
+        wj[j] = i - 1;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Optical tables resampled onto the mass grid and the radiation-pressure and wind-drag
+ * tables: interpolate_dust_to_grid, src/functions.cu:243-300, and calculate_beta,
+ * :338-388 (Cd = 2, Grav = 4 pi^2, src/ddyn.cuh).  s, Qabs, Qsca, Qpfunc: the optical file's
+ * n_dust sizes; a, q, Qa, Qs, Qp, beta, betasw: the n_grid bins.  Returns 54 (the
+ * reference's usage code) when the last bin overshoots dmax by more than 1e-12.
+ * The size walk is the reference's, with two guards where it would read outside s: a bin
+ * at or below s[0] is interpolated on [s[0], s[1]] (the reference reads s[-1] there), and a
+ * bin above the last size on the last interval.
+ * ------------------------------------------------------------------------------------ */
+int ora_dust_grid(int n_dust, int n_wav, int n_theta, const double *s, const double *w, const double *Qabs,
+                  const double *Qsca, const double *Qpfunc, const double *in, int n_grid, double amin, double amax,
+                  double dmax, double kqe, int radQ, int SWQ, double rho, double dist, double mstar,
+                  double mloss, double vsw, double *a, float *q, double *Qa, double *Qs, double *Qp, float *beta,
+                  float *betasw, double *Lum, double *betaswconst) {
+    if (n_dust < 2 || n_grid < 2) return -1;
+    const double f = log(amax / amin) / ((double)n_grid - 1.0);
+    int ip = 0;
+    for (int i = 0; i < n_grid; i++) {
+        a[i] = amin * exp((double)i * f);
+        q[i] = kqe * a[i] * 1e9;
+        if (i == n_grid - 1 && (a[i] - dmax) > 1e-12) return 54;
+        if (i == n_grid - 1 && (a[i] - dmax) < 1e-12 && (a[i] - dmax) > 0) a[i] = dmax;
+        while (ip < n_dust - 1 && s[ip] < a[i]) ip++;
+        int im = ip - 1;
+        if (im < 0) { im = 0; ip = 1; }
+        for (int j = 0; j < n_wav; j++) {
+            const size_t m = (size_t)im * n_wav + j, p = (size_t)ip * n_wav + j, o = (size_t)i * n_wav + j;
+            Qa[o] = exp(log(Qabs[m]) + log(a[i] / s[im]) * log(Qabs[p] / Qabs[m]) / log(s[ip] / s[im]));
+            Qs[o] = exp(log(Qsca[m]) + log(a[i] / s[im]) * log(Qsca[p] / Qsca[m]) / log(s[ip] / s[im]));
+            for (int k = 0; k < n_theta; k++) {
+                const size_t pm = (size_t)n_wav * ((size_t)n_theta * im + k) + j;
+                const size_t pp = (size_t)n_wav * ((size_t)n_theta * ip + k) + j;
+                Qp[(size_t)n_wav * ((size_t)n_theta * i + k) + j] =
+                    exp(log(Qpfunc[pm]) + log(a[i] / s[im]) * log(Qpfunc[pp] / Qpfunc[pm]) / log(s[ip] / s[im]));
+            }
+        }
+        ip--;
+    }
+
+    *betaswconst = 3.0 * mloss * 2 * 1.98892e30 * 3.1556926e7 * vsw / 32.0 / ORA_PI / mstar / rho / ORA_AU / ORA_AU /
+                   ORA_AU;
+    double Star = 0.0;
+    for (int j = 0; j < n_wav - 1; j++) Star += 0.5 * (w[j + 1] - w[j]) * (in[j + 1] + in[j]);
+    *Lum = Star * 4.0 * ORA_PI * pow(dist, 2.0) / 3.827e26;
+    double *Qpr = (double *)malloc(sizeof(double) * n_wav);
+    for (int i = 0; i < n_grid; i++) {
+        if (radQ == 1) {
+            double Qsum = 0.0;
+            for (int j = 0; j < n_wav; j++) {
+                double g = 0.0, S = 0.0, costm = -1.0;
+                for (int k = 1; k < n_theta; k++) {
+                    const double costp = (double)k * 2.0 / (n_theta - 1.0) - 1.0;
+                    const double P0 = Qp[(size_t)n_wav * ((size_t)n_theta * i + k - 1) + j];
+                    const double P1 = Qp[(size_t)n_wav * ((size_t)n_theta * i + k) + j];
+                    S += 0.5 * (P0 + P1) * (costp - costm);
+                    g += 0.5 * (costm * P0 + costp * P1) * (costp - costm);
+                    costm = costp;
+                }
+                g /= S;
+                Qpr[j] = (Qa[(size_t)i * n_wav + j] + Qs[(size_t)i * n_wav + j] * (1.0 - g)) * in[j];
+            }
+            for (int j = 0; j < n_wav - 1; j++) Qsum += 0.5 * (w[j + 1] - w[j]) * (Qpr[j + 1] + Qpr[j]);
+            beta[i] = 0.57 * Qsum / Star * (*Lum / mstar * (4.0 * ORA_PI * ORA_PI)) / a[i] / 1e6 / rho / 1e-3;
+        } else {
+            beta[i] = 0.0;
+        }
+        betasw[i] = SWQ == 1 ? *betaswconst / a[i] : 0.0;
+    }
+    free(Qpr);
+    return 0;
+}

@@ -15,30 +15,43 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
 REFSRC = Path("/root/reference/src")
 EXE = OUT / "param_dump"
+OPTICS_EXE = OUT / "optics_dump"
 UNITS = ("read_in", "functions", "ran3", "error", "print", "getMemorySize")
 
 
-def build() -> Path | None:
+def _build(harness: str, exe: Path) -> Path | None:
     if not (REFSRC / "read_in.cu").exists():
-        return EXE if EXE.exists() else None
+        return exe if exe.exists() else None
     OUT.mkdir(exist_ok=True)
-    deps = [REFSRC / f"{u}.cu" for u in UNITS] + [REFSRC / "ddyn.cuh", HERE / "param_dump.cu"]
-    if EXE.exists() and EXE.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
-        return EXE
+    deps = [REFSRC / f"{u}.cu" for u in UNITS] + [REFSRC / "ddyn.cuh", HERE / harness]
+    if exe.exists() and exe.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return exe
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     flags = ["-O2", "-rdc=true", "-D_GNU_SOURCE", "-gencode", "arch=compute_103a,code=sm_103a", "-I", str(REFSRC)]
     objs = []
     for u in UNITS:
         o = OUT / f"ref_{u}.o"
-        r = subprocess.run([nvcc, *flags, "-c", str(REFSRC / f"{u}.cu"), "-o", str(o)], capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"reference {u}.cu failed to build:\n{r.stderr}")
+        if not (o.exists() and o.stat().st_mtime >= (REFSRC / f"{u}.cu").stat().st_mtime):
+            r = subprocess.run([nvcc, *flags, "-c", str(REFSRC / f"{u}.cu"), "-o", str(o)], capture_output=True,
+                               text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"reference {u}.cu failed to build:\n{r.stderr}")
         objs.append(str(o))
-    r = subprocess.run([nvcc, *flags, str(HERE / "param_dump.cu"), *objs, "-o", str(EXE)], capture_output=True,
-                       text=True)
+    r = subprocess.run([nvcc, *flags, str(HERE / harness), *objs, "-o", str(exe)], capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"param_dump failed to link:\n{r.stderr}")
-    return EXE
+        raise RuntimeError(f"{harness} failed to link:\n{r.stderr}")
+    return exe
+
+
+def build() -> Path | None:
+    """oracle/_ref/param_dump: read_in_param and read_in_model."""
+    return _build("param_dump.cu", EXE)
+
+
+def build_optics() -> Path | None:
+    """oracle/_ref/optics_dump: interpolate_stellar_to_grid, interpolate_dust_to_grid,
+    calculate_beta."""
+    return _build("optics_dump.cu", OPTICS_EXE)
 
 
 if __name__ == "__main__":

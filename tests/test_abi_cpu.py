@@ -37,7 +37,7 @@ def test_python_binding_covers_header(built_lib):
 def test_status_strings_and_version(built_lib):
     from diskdyn_gb300 import abi
     lib = abi.load()
-    assert lib.ddx_abi_version() == 2
+    assert lib.ddx_abi_version() == 3
     assert lib.ddx_status_string(0) == b"ok"
     assert lib.ddx_status_string(5) == b"size beyond limit"
     assert lib.ddx_status_string(99) == b"unknown status"
