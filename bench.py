@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar"], default="dusty_ring")
+    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar", "setup"], default="dusty_ring")
     p.add_argument("--solar-steps", type=int, default=1000)
     p.add_argument("--scale-err-steps", type=int, default=60)
     p.add_argument("--adjoint-steps", type=int, default=2000)
@@ -837,9 +837,93 @@ def run_imaging(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_setup(args, world, rank, local):
+    """Start-of-run set-up of a 16.8M-tracer A-star debris system (synth.setup_param_text,
+    the size of the largest single-GPU configuration): the size grid and its optical, beta
+    and beta_sw tables from a 40 x 200 x 181 Mie table (ddx_dust_grid), the temperature
+    table (ddx_dust_temp) and every body drawn into device memory (ddx_setup_device).
+    Against the host path the reference runs: the oracle's restatement of its table
+    set-up (one core; the temperature table on all cores) and its generator with ran3
+    (ddx_setup_host, the reference's bodies to the bit) on a 1/16 sample, scaled."""
+    import tempfile
+    import torch
+    import oracle.cpu as oc
+    from diskdyn_gb300 import formats, synth
+    from diskdyn_gb300.engine import Engine
+
+    torch.cuda.set_device(local)
+    eng = Engine(local)
+    w, influx, tab = synth.mie_table()
+    dmin, dmax = float(tab["s"][0]), float(tab["s"][-1])
+
+    def param(n_grains, n_grav):
+        with tempfile.TemporaryDirectory() as td:
+            pf = Path(td) / "system.param"
+            pf.write_text(synth.setup_param_text(n_grains=n_grains, n_gravitating=n_grav))
+            p = formats.read_param_struct(pf)
+        formats.param_grid(p, dmin, dmax)
+        return p
+
+    p = param(16777216, 4096)
+    grid = dict(n_grid=p.n_grid, amin=p.amin, amax=p.amax, dmax=dmax, kqe=p.kqe, radQ=p.radQ, SWQ=p.SWQ,
+                rho=p.rho, dist=p.dist, mstar=p.planets[0].m, mloss=p.mloss, vsw=p.vsw)
+
+    def gpu_setup():
+        g = eng.dust_grid(w, influx, tab, **grid)
+        td = eng.dust_temp(w, influx, g["Qabs"], p.dist, 300.0)
+        st, run = eng.setup_device(p, dmin, dmax, g["beta"], seed=20241203)
+        torch.cuda.synchronize()
+        return g, td, st, run
+
+    for _ in range(max(1, args.warmup)):
+        g, td, st, run = gpu_setup()
+        del st
+    reps = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        g, td, st, run = gpu_setup()
+        reps.append(time.perf_counter() - t0)
+        del st
+    # the generation alone, device-timed
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    st, run = eng.setup_device(p, dmin, dmax, g["beta"], seed=20241203)
+    e1.record()
+    torch.cuda.synchronize()
+    gen_ms = e0.elapsed_time(e1)
+    finite = bool(torch.isfinite(st.x).all().item() and torch.isfinite(st.vz).all().item())
+    n_all = run.n_all
+    del st
+    # host path: table set-up (oracle, one core), temperature table (oracle, all cores),
+    # generation with ran3 on a 1/16 sample
+    t0 = time.perf_counter()
+    c = oc.dust_grid(w, influx, tab, **grid)
+    t_grid = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oc.dust_temp(w, influx, c["Qabs"], p.dist, 300.0)
+    t_temp = time.perf_counter() - t0
+    ps = param(16777216 // 16, 4096 // 16)
+    t0 = time.perf_counter()
+    hs, hrun = formats.setup_host(ps, dmin, dmax, c["beta"])
+    t_gen = (time.perf_counter() - t0) * n_all / hrun.n_all
+    line = {"metric": "set-up time (s)", "workload": "setup", "n_all": n_all, "n_mass": run.n_mass,
+            "n_grid": p.n_grid, "table": "40 sizes x 200 wavelengths x 181 angles",
+            "gpu_s": float(np.median(reps)), "gpu_generation_ms": gen_ms,
+            "gpu_bodies_per_s": n_all / (gen_ms * 1e-3), "state_finite": finite,
+            "host_s": t_grid + t_temp + t_gen,
+            "host_parts_s": {"dust_grid_1core": t_grid, "dust_temp_all_cores": t_temp, "ran3_generation": t_gen},
+            "host_sample": f"generation timed on {hrun.n_all} bodies and scaled to {n_all}",
+            "cpu_cores": os.cpu_count(), "higher_is_better": False}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
+    if args.workload == "setup":
+        run_setup(args, world, rank, local)
+        return
     if args.workload == "imaging":
         run_imaging(args, world, rank, local)
         return

@@ -77,6 +77,12 @@ SIGNATURES = [
                                 C.c_int]),
     ("ddx_stellar_grid", C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                    C.c_void_p, C.c_void_p]),
+    ("ddx_param_grid", C.c_int, [C.c_void_p, C.c_double, C.c_double]),
+    ("ddx_setup_count", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p]),
+    ("ddx_setup_host", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_longlong, C.c_void_p,
+                                 C.c_void_p]),
+    ("ddx_setup_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_ulonglong,
+                                   C.POINTER(State), C.c_longlong, C.c_void_p, C.c_void_p]),
     ("ddx_abi_version", C.c_int, []),
     ("ddx_status_string", C.c_char_p, [C.c_int]),
     ("ddx_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int]),

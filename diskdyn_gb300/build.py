@@ -42,7 +42,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(ROOT /
 
 
 def _compile(src: Path, hmt: float, verbose: bool) -> Path:
-    obj = OBJ / (src.stem + ".o")
+    obj = OBJ / (src.name + ".o")     # x.cu and x.cpp may share a stem
     if obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, hmt):
         return obj
     if src.suffix == ".cpp":

@@ -392,6 +392,13 @@ int ddx_dust_grid(ddx_ctx* c, int n_wav, const double* w, const double* in, cons
     return dust_grid_run(n_wav, w, in, *file, *g, *grid, q, beta, betasw, Lum, betaswconst, (cudaStream_t)stream);
 }
 
+int ddx_setup_device(ddx_ctx* c, const ddx_param* p, double dmin, double dmax, const float* beta,
+                     unsigned long long seed, const ddx_state* s, long long cap, ddx_dat_run* run, void* stream) {
+    if (!c || !p || !beta || !run || !state_ok(s)) return DDX_ERR_ARG;
+    cudaSetDevice(c->device);
+    return setup_device_run(p, dmin, dmax, beta, seed, *s, cap, run, (cudaStream_t)stream);
+}
+
 int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,
                         int ckpt_every, const ddx_phys* phys, const ddx_view* view, const int* wj, int n_img,
                         double* image, void* stream) {

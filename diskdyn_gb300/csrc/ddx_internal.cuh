@@ -7,6 +7,7 @@
 #include <stdint.h>
 #include <vector>
 #include "../../include/diskdyn_gb300.h"
+#include "../../include/diskdyn_gb300_io.h"
 
 namespace ddx {
 
@@ -171,4 +172,8 @@ int dust_temp_run(int n_grid, int n_wav, const double* w, const double* in, cons
 int dust_grid_run(int n_wav, const double* w, const double* in, const ddx_optical_table& file,
                   const ddx_grid_setup& g, ddx_optical_table& grid, float* q, float* beta, float* betasw,
                   double* Lum, double* betaswconst, cudaStream_t st);
+// ddx_setup.cu: the initial system drawn on the GPU (arguments other than the state
+// checked by the caller; synchronizes).
+int setup_device_run(const ddx_param* p, double dmin, double dmax, const float* beta, unsigned long long seed,
+                     const ddx_state& s, long long cap, ddx_dat_run* run, cudaStream_t st);
 }  // namespace ddx

@@ -105,6 +105,10 @@ void copy_str(char* dst, const char* src) {
     dst[DDX_PARAM_STR - 1] = 0;
 }
 
+}  // namespace
+
+namespace ddx_host {
+
 // Orbital elements to Cartesian state about a central mass, both masses times 4 pi^2
 // (src/functions.cu:6-46), expression for expression.
 void coe2rv(double M, double m, double a, double e, double i, double w, double o, double nu, double* x,
@@ -128,6 +132,12 @@ void coe2rv(double M, double m, double a, double e, double i, double w, double o
           vze * (-cos(o) * sin(i));
     *vz = vxe * sin(w) * sin(i) + vye * cos(w) * sin(i) + vze * cos(i);
 }
+
+}  // namespace ddx_host
+
+namespace {
+
+using ddx_host::coe2rv;
 
 // Shifts the bodies to the centre of mass and gives the star the balancing momentum
 // (src/read_in.cu:344-375).

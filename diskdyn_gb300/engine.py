@@ -237,6 +237,22 @@ class Engine:
         out["Lum"], out["betaswconst"] = lum.value, bsc.value
         return out
 
+    def setup_device(self, p, dmin: float, dmax: float, beta, seed: int, stream=None) -> tuple:
+        """ddx_setup_device: the initial system of parameter struct p (after
+        formats.param_grid) drawn on this GPU; returns (DeviceState, run counts)."""
+        from . import formats
+        run = formats.setup_count(p, dmin, dmax)
+        dev = torch.device("cuda", self.device)
+        ts = {f: torch.empty(run.n_all, dtype=torch.int32 if f == "id" else torch.float64, device=dev)
+              for f in STATE_FIELDS}
+        st = DeviceState(**ts)
+        beta = np.ascontiguousarray(beta, np.float32)
+        abi.check(self.lib.ddx_setup_device(self.ctx, C.byref(p), float(dmin), float(dmax),
+                                            C.c_void_p(beta.ctypes.data), int(seed) & (2 ** 64 - 1),
+                                            C.byref(st._abi), run.n_all, C.byref(run),
+                                            C.c_void_p(_stream_handle(stream))), "ddx_setup_device")
+        return st, run
+
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
         bounded device-side wait since the last call, else 0."""

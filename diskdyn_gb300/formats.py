@@ -185,3 +185,27 @@ def stellar_grid(w, spec_w, spec_F, wavs=()):
     abi.check(abi.load().ddx_stellar_grid(w.size, P(w), spec_w.size, P(spec_w), P(spec_F), wavs.size, P(wavs),
                                           P(influx), P(wj)), "ddx_stellar_grid")
     return influx, wj[:wavs.size]
+
+
+def param_grid(p: Param, dmin: float, dmax: float) -> None:
+    """ddx_param_grid on a parsed parameter file, in place: grain ranges clipped to the
+    optical table's [dmin, dmax] (m), the mass grid and the number constants."""
+    abi.check(abi.load().ddx_param_grid(C.byref(p), float(dmin), float(dmax)), "ddx_param_grid")
+
+
+def setup_count(p: Param, dmin: float, dmax: float) -> DatRun:
+    run = DatRun()
+    abi.check(abi.load().ddx_setup_count(C.byref(p), float(dmin), float(dmax), C.byref(run)), "ddx_setup_count")
+    return run
+
+
+def setup_host(p: Param, dmin: float, dmax: float, beta, seed: int = -2):
+    """ddx_setup_host: (state arrays, run counts) of Grid::setup's bodies with the
+    reference's generator."""
+    import numpy as np
+    run = setup_count(p, dmin, dmax)
+    arrays = {k: np.zeros(run.n_all, np.int32 if k == "id" else np.float64) for k in STATE_FIELDS}
+    beta = np.ascontiguousarray(beta, np.float32)
+    abi.check(abi.load().ddx_setup_host(C.byref(p), float(dmin), float(dmax), C.c_void_p(beta.ctypes.data), int(seed),
+                                        C.byref(host_state(arrays)), C.byref(run)), "ddx_setup_host")
+    return arrays, run

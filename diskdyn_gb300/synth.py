@@ -294,6 +294,23 @@ def mie_table(n_size=40, n_wav=200, n_theta=181, smin=1e-7, smax=1e-4, Teff=9000
     return w, influx, {"s": s, "Qabs": Qabs, "Qsca": Qsca, "Qpfunc": Qp}
 
 
+def setup_param_text(n_grains: int = 16777216, n_gravitating: int = 4096) -> str:
+    """A parameter file (the reference's format) of an A-star debris system whose set-up
+    makes about n_grains grain tracers and n_gravitating gravitating bodies: a planet, a
+    narrow belt (Fomalhaut-like, 70% of both), a wide halo disk and a collisional blob."""
+    ng = [int(n_gravitating * f) for f in (0.7, 0.3)]
+    # tracers per mass bin x bins: the set-up rounds Nsmall / Ngrid, so ask per disk
+    ns = [int(n_grains * f) for f in (0.7, 0.25, 0.05)]
+    return "\n".join([
+        "# A-star debris system for set-up timing", "1", "0", "no 100", "1000.0 100.0 500.0", "2000", "300",
+        "1.92 A3V 8590 1.84 1.0 25.0 1.0e-13 500.0", "7.7 400.0 0.0 65.6 0.0 1024 1024", "0.55 24.0 70.0",
+        "Library", "yes yes no", "begin_planets", "0.0 115.0 0.12 0.0 0.0 0.0 3.0e-6", "end_planets",
+        "3.3 optical/astrosil.dat 27.5", "begin_disks",
+        f"130.0 145.0 0.03 0.1 10.0 0.3 3.65 3.0 0.0 {ng[0]} {ns[0]}",
+        f"30.0 200.0 0.15 0.05 1.0 0.3 3.5 0.3 -1.0 {ng[1]} {ns[1]}", "end_disks", "begin_blobs",
+        f"140.0 0.1 1.0 30.0 45.0 90.0 1.0 0.5 3.65 0.01 0 {ns[2]} Collision 5.0", "end_blobs", "synthetic", ""])
+
+
 def ring_imaging(s: System, xsize=512, ysize=512) -> System:
     """Attach optics and a view to a `dusty_ring` system: HG tables on its grains' size
     bins, grey grains at T = 278.3 L^(1/4) (r/AU)^(-1/2) K, a 7500 K star of 2 Rsun at

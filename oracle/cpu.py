@@ -222,3 +222,60 @@ def dust_grid(w, influx, table: dict, n_grid, amin, amax, dmax, kqe, radQ, SWQ, 
         raise ValueError(f"usage code {r}")
     o["Lum"], o["betaswconst"] = lum.value, bsc.value
     return o
+
+
+class ODisk(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("Rin", "Rout", "sigmae", "gammas", "dhdr")]
+
+
+class OBlob(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("a", "ecc", "inc", "w", "o", "nu", "sigma", "vkepp")] + [("collcloud", C.c_int)]
+
+
+def setup_populations(p, dmin: float, dmax: float):
+    """Grid::setup's body order (src/grid.cu:79-190) after the planets, as (kind, index)
+    per body: kind 0 = disk, 1 = blob; the gravitating bodies of every disk then blob, then
+    round(Nsmall / Ngrid) grains per mass bin of every disk then blob.  p is a parsed
+    parameter struct after the grid set-up (fields mmin, f, disks, blobs)."""
+    import math
+    kind, idx = [], []
+    for k, n, pops in ((0, p.n_disks, p.disks), (1, p.n_blobs, p.blobs)):
+        for j in range(n):
+            kind += [k] * pops[j].Ngrav
+            idx += [j] * pops[j].Ngrav
+    for k, n, pops in ((0, p.n_disks, p.disks), (1, p.n_blobs, p.blobs)):
+        for j in range(n):
+            mmax = p.mmin * math.exp(round(math.log(pops[j].dmmax / p.mmin) / p.f) * p.f)
+            mmin = p.mmin * math.exp(round(math.log(pops[j].mmin / p.mmin) / p.f) * p.f)
+            ngrid = int(round(math.log(mmax / mmin) / math.log(1.1) + 1))
+            npg = int(round(pops[j].Nsmall / ngrid))
+            kind += [k] * (ngrid * npg)
+            idx += [j] * (ngrid * npg)
+    return np.asarray(kind, np.int32), np.asarray(idx, np.int32)
+
+
+def setup_philox(p, kind, idx, m, beta, seed: int, first: int):
+    """The GPU set-up's counter-based orbit draws for bodies first.. (oracle restatement):
+    returns (n, 6) states x y z vx vy vz and the number of bodies whose rejections ran out."""
+    disks = (ODisk * max(p.n_disks, 1))(*[ODisk(d.Rin, d.Rout, d.sigmae, d.gammas, d.dhdr)
+                                          for d in list(p.disks)[:p.n_disks]])
+    blobs = (OBlob * max(p.n_blobs, 1))(*[OBlob(b.a, b.ecc, b.inc, b.w, b.o, b.nu, b.sigma, b.vkepp, b.collcloud)
+                                          for b in list(p.blobs)[:p.n_blobs]])
+    kind, idx = (np.ascontiguousarray(a, np.int32) for a in (kind, idx))
+    m, beta = (np.ascontiguousarray(a, np.float64) for a in (m, beta))
+    out = np.zeros((len(kind), 6))
+    f = lib().ora_setup_philox
+    f.restype = C.c_longlong
+    f.argtypes = [C.c_longlong, C.c_longlong] + [C.c_void_p] * 4 + [C.c_void_p, C.c_void_p, C.c_double,
+                                                                    C.c_ulonglong, C.c_void_p]
+    bad = f(len(kind), int(first), _ptr(kind), _ptr(idx), _ptr(m), _ptr(beta), C.cast(disks, C.c_void_p),
+            C.cast(blobs, C.c_void_p), float(p.planets[0].m), int(seed) & (2 ** 64 - 1), _ptr(out))
+    return out, bad
+
+
+def philox4x32_10(ctr, key):
+    f = lib().ora_philox4x32_10
+    f.argtypes = [C.c_uint32 * 4, C.c_uint32 * 2, C.c_uint32 * 4]
+    o = (C.c_uint32 * 4)()
+    f((C.c_uint32 * 4)(*ctr), (C.c_uint32 * 2)(*key), o)
+    return tuple(o)

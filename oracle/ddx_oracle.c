@@ -733,3 +733,106 @@ int ora_dust_grid(int n_dust, int n_wav, int n_theta, const double *s, const dou
     free(Qpr);
     return 0;
 }
+
+/* ------------------------------------------------------------------------------------
+ * Counter-based set-up draws (the GPU generator of the initial system), restated: the
+ * Philox4x32-10 bijection of Salmon, Moraes, Dror and Shaw ("Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11), then the orbit draws of genorb_disk / genorb_blob
+ * (src/functions.cu:157-232) and coe2rv (:6-46) in the reference's expression order, with
+ * libm.  Body i's uniforms come from counters (draw, i lo, i hi, 0x53455455) under the key
+ * (seed lo, seed hi), two per counter, each 53 bits mapped to (0, 1].
+ * ------------------------------------------------------------------------------------ */
+#include <stdint.h>
+
+void ora_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; r++) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n1 = (uint32_t)p1;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1, n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+typedef struct { uint32_t k[2], lo, hi, draw; } ora_stream;
+
+static void ora_pair(ora_stream *s, double *u1, double *u2) {
+    uint32_t c[4] = {s->draw++, s->lo, s->hi, 0x53455455u}, o[4];
+    ora_philox4x32_10(c, s->k, o);
+    *u1 = (double)((((uint64_t)(o[0] >> 5)) << 26 | (o[1] >> 6)) + 1) * 0x1.0p-53;
+    *u2 = (double)((((uint64_t)(o[2] >> 5)) << 26 | (o[3] >> 6)) + 1) * 0x1.0p-53;
+}
+
+#define ORA_PI2 6.28318530717958623200
+
+static double ora_gauss(double u1, double u2) { return sqrt(-2.0 * log(u1)) * cos(ORA_PI2 * u2); }
+
+static void ora_coe2rv(double M, double m, double a, double e, double i, double w, double o, double nu, double *s,
+                       double beta) {
+    double p = a * (1.0 - e * e), mu = (M + m) * (1.0 - beta);
+    double xe = p * cos(nu) / (1.0 + e * cos(nu)), ye = p * sin(nu) / (1.0 + e * cos(nu));
+    double vxe = -sqrt(mu / p) * sin(nu), vye = sqrt(mu / p) * (e + cos(nu));
+    s[0] = xe * (cos(o) * cos(w) - sin(o) * sin(w) * cos(i)) + ye * (-cos(o) * sin(w) - sin(o) * cos(w) * cos(i));
+    s[1] = xe * (sin(o) * cos(w) + cos(o) * sin(w) * cos(i)) + ye * (-sin(o) * sin(w) + cos(o) * cos(w) * cos(i));
+    s[2] = xe * sin(w) * sin(i) + ye * cos(w) * sin(i);
+    s[3] = vxe * (cos(o) * cos(w) - sin(o) * sin(w) * cos(i)) + vye * (-cos(o) * sin(w) - sin(o) * cos(w) * cos(i));
+    s[4] = vxe * (sin(o) * cos(w) + cos(o) * sin(w) * cos(i)) + vye * (-sin(o) * sin(w) + cos(o) * cos(w) * cos(i));
+    s[5] = vxe * sin(w) * sin(i) + vye * cos(w) * sin(i);
+}
+
+typedef struct { double Rin, Rout, sigmae, gammas, dhdr; } ora_disk;
+typedef struct { double a, ecc, inc, w, o, nu, sigma, vkepp; int collcloud; } ora_blob;
+
+/* Bodies first .. first+n-1: kind 0 = disk j[k], 1 = blob j[k]; out[n][6] = x y z vx vy vz.
+ * Returns the number of bodies whose rejection draws ran out (1,024 tries). */
+long long ora_setup_philox(long long n, long long first, const int *kind, const int *j, const double *m,
+                           const double *beta, const ora_disk *disks, const ora_blob *blobs, double M,
+                           unsigned long long seed, double *out) {
+    long long bad = 0;
+    for (long long k = 0; k < n; k++) {
+        const long long i = first + k;
+        ora_stream rs = {{(uint32_t)seed, (uint32_t)(seed >> 32)}, (uint32_t)i, (uint32_t)((unsigned long long)i >> 32), 0};
+        double *s = out + 6 * k, u1, u2;
+        int ok = 0;
+        if (kind[k] == 0) {
+            const ora_disk *d = &disks[j[k]];
+            double e = 0.0;
+            for (int t = 0; t < 1024 && !ok; t++) {
+                ora_pair(&rs, &u1, &u2);
+                e = fabs(ora_gauss(u1, u2) * d->sigmae);
+                ok = e < 1.0;
+            }
+            double amin = d->Rin / (1.0 - e), amax = d->Rout / (1.0 + e), g = 2.0 + d->gammas;
+            double ua, unu, ui1, ui2, uw, uo;
+            ora_pair(&rs, &ua, &unu);
+            ora_pair(&rs, &ui1, &ui2);
+            ora_pair(&rs, &uw, &uo);
+            double a = pow(ua * (pow(amax, g) - pow(amin, g)) + pow(amin, g), 1.0 / g);
+            double inc = fabs(ora_gauss(ui1, ui2) * d->dhdr);
+            ora_coe2rv(M, m[k], a, e, inc, ORA_PI2 * uw, ORA_PI2 * uo, ORA_PI2 * unu, s, beta[k]);
+        } else {
+            const ora_blob *b = &blobs[j[k]];
+            double a = 0.0;
+            for (int t = 0; t < 1024 && !ok; t++) {
+                ora_pair(&rs, &u1, &u2);
+                a = b->a + ora_gauss(u1, u2) * b->sigma;
+                ok = a > 0.0;
+            }
+            ora_pair(&rs, &u1, &u2);
+            double nu = b->nu + ora_gauss(u1, u2) * b->sigma / a;
+            ora_coe2rv(M, m[k], a, b->ecc, b->inc, b->w, b->o, nu, s, beta[k]);
+            if (b->collcloud == 0) {
+                ora_pair(&rs, &u1, &u2);
+                double voff = b->vkepp * 0.01 * sqrt(s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+                double ct = -1.0 + 2.0 * u1, st = sqrt(1.0 - ct * ct), gam = ORA_PI2 * u2;
+                s[3] += voff * st * cos(gam);
+                s[4] += voff * st * sin(gam);
+                s[5] += voff * ct;
+            }
+        }
+        if (!ok) bad++;
+    }
+    return bad;
+}

@@ -54,5 +54,10 @@ def build_optics() -> Path | None:
     return _build("optics_dump.cu", OPTICS_EXE)
 
 
+def build_setup() -> Path | None:
+    """oracle/_ref/setup_dump: the start-of-run set-up and Grid::setup's body generation."""
+    return _build("setup_dump.cu", OUT / "setup_dump")
+
+
 if __name__ == "__main__":
     print(build())
