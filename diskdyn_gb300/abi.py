@@ -63,6 +63,26 @@ class GridSetup(C.Structure):
                 ("dist", C.c_double), ("mstar", C.c_double), ("mloss", C.c_double), ("vsw", C.c_double)]
 
 
+class Cadence(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("t_write", "t_fits", "t_sed", "t_end", "time", "tlastd", "tlastf",
+                                          "tlasts", "model_dt")] + [("initial_outputs", C.c_int)]
+
+
+class HostStateView(C.Structure):
+    _fields_ = [(k, C.POINTER(C.c_double)) for k in ("x", "y", "z", "vx", "vy", "vz", "N", "m")] + \
+               [("id", C.POINTER(C.c_int)), ("cap", C.c_longlong)]
+
+
+class Output(C.Structure):
+    _fields_ = [("kind", C.c_int), ("time", C.c_double), ("model_dt", C.c_double), ("tlastd", C.c_double),
+                ("tlastf", C.c_double), ("tlasts", C.c_double), ("data", C.POINTER(C.c_double)),
+                ("n", C.c_longlong), ("state", C.POINTER(HostStateView))]
+
+
+OUTPUT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(Output))
+DDX_OUT_IMAGES, DDX_OUT_SED, DDX_OUT_STATE = 1, 2, 3
+
+
 # (name, restype, argtypes) of every symbol include/diskdyn_gb300.h declares.
 SIGNATURES = [
     ("ddx_param_read", C.c_int, [C.c_char_p, C.c_void_p]),
@@ -83,6 +103,11 @@ SIGNATURES = [
                                  C.c_void_p]),
     ("ddx_setup_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_ulonglong,
                                    C.POINTER(State), C.c_longlong, C.c_void_p, C.c_void_p]),
+    ("ddx_schedule", C.c_int, [C.POINTER(Cadence), C.c_double, C.c_longlong, C.c_void_p, C.c_void_p,
+                               C.POINTER(C.c_longlong)]),
+    ("ddx_run", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double, C.POINTER(Phys), C.c_int,
+                          C.c_int, C.POINTER(View), C.c_void_p, C.c_int, C.POINTER(Cadence), OUTPUT_FN, C.c_void_p,
+                          C.c_void_p]),
     ("ddx_abi_version", C.c_int, []),
     ("ddx_status_string", C.c_char_p, [C.c_int]),
     ("ddx_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int]),

@@ -392,6 +392,15 @@ int ddx_dust_grid(ddx_ctx* c, int n_wav, const double* w, const double* in, cons
     return dust_grid_run(n_wav, w, in, *file, *g, *grid, q, beta, betasw, Lum, betaswconst, (cudaStream_t)stream);
 }
 
+}  // extern "C"
+
+namespace ddx {
+int ctx_device(const ddx_ctx* c) { return c->device; }
+int ctx_optics_n_wav(const ddx_ctx* c) { return c->optics_set ? c->od.n_wav : 0; }
+}  // namespace ddx
+
+extern "C" {
+
 int ddx_setup_device(ddx_ctx* c, const ddx_param* p, double dmin, double dmax, const float* beta,
                      unsigned long long seed, const ddx_state* s, long long cap, ddx_dat_run* run, void* stream) {
     if (!c || !p || !beta || !run || !state_ok(s)) return DDX_ERR_ARG;

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/diskdyn_gb300_io.h"
+#include "../../include/diskdyn_gb300_run.h"
 
 namespace ddx_host {
 
@@ -47,5 +48,18 @@ int split(char* buf, char** tok, int max);
 // src/functions.cu:6-46), expression for expression: a in AU, angles in radians.
 void coe2rv(double M, double m, double a, double e, double i, double w, double o, double nu, double* x,
             double* y, double* z, double* vx, double* vy, double* vz, double beta);
+
+// Grid::evolve's clock (src/grid.cu:344-437): the step size dt cut to end on the next
+// output time or on t_end, and the outputs due after each step.
+struct Clock {
+    ddx_cadence c;
+    double dt = 0.0, dttmp = 0.0, time = 0.0;
+    void start(const ddx_cadence& cad, double dt_);
+    bool running() const { return time < c.t_end; }
+    // Advances the clock by the current step and returns the outputs now due as a mask of
+    // 1 << DDX_OUT_SED, 1 << DDX_OUT_IMAGES, 1 << DDX_OUT_STATE, in that order of writing,
+    // with the last-output times updated the way the reference updates them.
+    int advance();
+};
 
 }  // namespace ddx_host

@@ -172,6 +172,9 @@ int dust_temp_run(int n_grid, int n_wav, const double* w, const double* in, cons
 int dust_grid_run(int n_wav, const double* w, const double* in, const ddx_optical_table& file,
                   const ddx_grid_setup& g, ddx_optical_table& grid, float* q, float* beta, float* betasw,
                   double* Lum, double* betaswconst, cudaStream_t st);
+// ddx_api.cu: context facts for the run driver (ddx_run.cu).
+int ctx_device(const ddx_ctx* c);
+int ctx_optics_n_wav(const ddx_ctx* c);   // 0 when the optics are not set
 // ddx_setup.cu: the initial system drawn on the GPU (arguments other than the state
 // checked by the caller; synchronizes).
 int setup_device_run(const ddx_param* p, double dmin, double dmax, const float* beta, unsigned long long seed,

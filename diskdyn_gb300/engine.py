@@ -253,6 +253,43 @@ class Engine:
                                             C.c_void_p(_stream_handle(stream))), "ddx_setup_device")
         return st, run
 
+    def run(self, st: DeviceState, n_grav: int, dt: float, phys: abi.Phys, view: abi.View, wj, cadence: dict,
+            on_output, precision: int = abi.DDX_PREC_MIXED, mode: int = abi.DDX_MODE_FIXED, stream=None) -> dict:
+        """ddx_run: Grid::evolve with its output cadence.  cadence holds t_write, t_fits,
+        t_sed, t_end, time, tlastd, tlastf, tlasts, model_dt, initial_outputs; on_output(out)
+        gets a dict per output (kind, time, the run values, and `data` (numpy copy) or
+        `state` (dict of numpy copies)) and returns True to stop.  Returns the clock reached."""
+        wj_a, pwj = _host(wj, np.int32)
+        cad = abi.Cadence(**{k: float(cadence.get(k, 0.0)) for k in ("t_write", "t_fits", "t_sed", "t_end", "time",
+                                                                      "tlastd", "tlastf", "tlasts", "model_dt")},
+                          initial_outputs=int(cadence.get("initial_outputs", 0)))
+        errors = []
+
+        def cb(_user, o):
+            try:
+                o = o.contents
+                d = {"kind": o.kind, "time": o.time, "model_dt": o.model_dt, "tlastd": o.tlastd,
+                     "tlastf": o.tlastf, "tlasts": o.tlasts}
+                if o.kind == abi.DDX_OUT_STATE:
+                    hs = o.state.contents
+                    n = hs.cap
+                    d["state"] = {f: np.ctypeslib.as_array(getattr(hs, f), shape=(n,)).copy() for f in STATE_FIELDS}
+                else:
+                    d["data"] = np.ctypeslib.as_array(o.data, shape=(o.n,)).copy()
+                return 1 if on_output(d) else 0
+            except Exception as e:   # surfaced after the call
+                errors.append(e)
+                return 1
+
+        fn = abi.OUTPUT_FN(cb)
+        r = self.lib.ddx_run(self.ctx, C.byref(st._abi), n_grav, st.n_all - n_grav, float(dt), C.byref(phys),
+                             precision, mode, C.byref(view), pwj, len(wj_a), C.byref(cad), fn, None,
+                             C.c_void_p(_stream_handle(stream)))
+        if errors:
+            raise errors[0]
+        abi.check(r, "ddx_run")
+        return {k: getattr(cad, k) for k in ("time", "tlastd", "tlastf", "tlasts")}
+
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
         bounded device-side wait since the last call, else 0."""

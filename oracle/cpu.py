@@ -279,3 +279,47 @@ def philox4x32_10(ctr, key):
     o = (C.c_uint32 * 4)()
     f((C.c_uint32 * 4)(*ctr), (C.c_uint32 * 2)(*key), o)
     return tuple(o)
+
+
+def cadence(cad: dict, dt: float):
+    """Grid::evolve's step sizes and output triggers (src/grid.cu:375-434) restated: a list
+    of (step size, outputs after it), outputs a tuple of "sed", "images", "state" in the
+    order the reference writes them."""
+    time = cad.get("time", 0.0)
+    tlastd, tlastf, tlasts = cad.get("tlastd", 0.0), cad.get("tlastf", 0.0), cad.get("tlasts", 0.0)
+    t_write, t_fits, t_sed, t_end = cad["t_write"], cad["t_fits"], cad["t_sed"], cad["t_end"]
+
+    def clip(dttmp):
+        if time + dttmp > tlastd + t_write:
+            dttmp = t_write + tlastd - time
+        if time + dttmp > tlastf + t_fits:
+            dttmp = t_fits + tlastf - time
+        if time + dttmp > tlasts + t_sed:
+            dttmp = t_sed + tlasts - time
+        if time + dttmp > t_end:
+            dttmp = t_end - time
+        return dttmp
+
+    dttmp = clip(dt)
+    out = []
+    while True:
+        h = dttmp
+        time += dttmp
+        due = []
+        if time >= tlasts + t_sed or time >= t_end:
+            due.append("sed")
+            tlasts = time
+            dttmp = dt
+        if time >= tlastf + t_fits or time >= t_end:
+            due.append("images")
+            tlastf = time
+            dttmp = dt
+        if time >= tlastd + t_write or time >= t_end:
+            due.append("state")
+            tlastd = time
+            dttmp = dt
+        dttmp = clip(dttmp)
+        out.append((h, tuple(due)))
+        if not time < t_end:
+            break
+    return out

@@ -8,7 +8,7 @@ from conftest import ROOT
 
 def header_functions():
     names = set()
-    for h in ("diskdyn_gb300.h", "diskdyn_gb300_io.h", "diskdyn_gb300_setup.h"):
+    for h in ("diskdyn_gb300.h", "diskdyn_gb300_io.h", "diskdyn_gb300_setup.h", "diskdyn_gb300_run.h"):
         txt = (ROOT / "include" / h).read_text()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
         names |= set(re.findall(r"\b(ddx_\w+)\s*\(", txt))
