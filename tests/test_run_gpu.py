@@ -102,6 +102,7 @@ def test_run_writes_the_reference_files(tmp_path):
     s, eng = setup(n_dust=1500)
     dt = s.dt
     p = formats.read_param_struct(Path(__file__).parent / "golden" / "setup" / "disks_blobs.param")
+    formats.param_grid(p, 1e-7, 1e-4)                       # the data-file header's grid
     cad = dict(t_write=10 * dt, t_fits=5 * dt, t_sed=10 * dt, t_end=10 * dt, initial_outputs=1)
     view = make_view(**s.view)
     o = s.optics
