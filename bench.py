@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar", "setup"], default="dusty_ring")
+    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar", "setup", "cadence"], default="dusty_ring")
     p.add_argument("--solar-steps", type=int, default=1000)
     p.add_argument("--scale-err-steps", type=int, default=60)
     p.add_argument("--adjoint-steps", type=int, default=2000)
@@ -918,11 +918,80 @@ def run_setup(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_cadence(args, world, rank, local):
+    """A whole run with outputs (ddx_run): the dusty ring with 256 planetesimals and 262,144
+    grains, mixed precision, 200 steps; SED (200 wavelengths) every 5 steps, two 512x512
+    images every 10, the state every 50.  Against the same run made call by call with a
+    host synchronisation and a host copy at every output, as the reference's evolve loop
+    makes them (there per wavelength)."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys, make_view
+
+    torch.cuda.set_device(local)
+    s = synth.dusty_ring(n_dust=262144, n_plsml=256, seed=synth.SEED + rank, n_steps=300)
+    synth.ring_imaging(s, 512, 512)
+    eng = Engine(local)
+    eng.set_size_table(**s.size_table)
+    o = s.optics
+    eng.set_optics(o["w"], o["in"], o["Qabs"], o["Qsca"], o["Qpfunc"], o["Td"], o["Rmin"], o["Rmax"])
+    phys, view, wj, ng, dt = make_phys(**s.phys), make_view(**s.view), s.image_wj, s.n_grav, s.dt
+    n_steps = 200
+    cad = dict(t_write=50 * dt, t_fits=10 * dt, t_sed=5 * dt, t_end=n_steps * dt)
+    MIX = abi.DDX_PREC_MIXED
+    counts = {}
+
+    def on(out):
+        counts[out["kind"]] = counts.get(out["kind"], 0) + 1
+        return False
+
+    def fused():
+        st = DeviceState.from_numpy(s.state)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.run(st, ng, dt, phys, view, wj, cad, on, precision=MIX)
+        return time.perf_counter() - t0
+
+    def call_by_call():
+        from diskdyn_gb300 import run as runmod
+        st = DeviceState.from_numpy(s.state)
+        h, m = runmod.schedule(cad, dt)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(len(h)):
+            eng.step(st, ng, float(h[k]), phys, MIX)
+            if m[k] & (1 << abi.DDX_OUT_SED):
+                eng.sed(st, ng, view, precision=MIX).cpu()
+            if m[k] & (1 << abi.DDX_OUT_IMAGES):
+                eng.image(st, ng, view, wj, precision=MIX).cpu()
+            if m[k] & (1 << abi.DDX_OUT_STATE):
+                for f in ("x", "y", "z", "vx", "vy", "vz", "N", "m", "id"):
+                    getattr(st, f).cpu()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    fused(), call_by_call()
+    counts.clear()
+    t_f = min(fused() for _ in range(3))
+    per_run = {k: v // 3 for k, v in counts.items()}
+    t_c = min(call_by_call() for _ in range(3))
+    line = {"metric": "run time with outputs (s)", "workload": "cadence", "n_grav": ng, "n_dust": s.n_dust,
+            "steps": n_steps, "precision": "mixed",
+            "outputs_per_run": {"sed": per_run.get(abi.DDX_OUT_SED, 0), "images": per_run.get(abi.DDX_OUT_IMAGES, 0),
+                                "state": per_run.get(abi.DDX_OUT_STATE, 0)},
+            "ddx_run_s": t_f, "call_by_call_synchronous_s": t_c, "speedup": t_c / t_f, "higher_is_better": False}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
     if args.workload == "setup":
         run_setup(args, world, rank, local)
+        return
+    if args.workload == "cadence":
+        run_cadence(args, world, rank, local)
         return
     if args.workload == "imaging":
         run_imaging(args, world, rank, local)
