@@ -219,8 +219,9 @@ def run_ours(args, world, rank, local):
         coll_ms.append((time.perf_counter() - t1) * 1e3)
     collide = {"h_AU": h_coll, "pairs": eng.last_pair_count, "ms_per_call": statistics.median(coll_ms),
                "bodies_per_s": nd / (statistics.median(coll_ms) / 1e3),
-               "what": "ddx_collide over the grains: hash keys, radix sort, cell ranges, count, scan, "
-                       "write; host wall time, including the count read-back"}
+               "what": "one ddx_collide call over the grains (output buffer sized from the previous call): "
+                       "hash keys on 2h cells, radix sort, cell ranges, octant count, scan, write; host wall "
+                       "time, including the count read-back"}
     step_plus_coll_ms = t_total * 1e3 / args.steps + collide["ms_per_call"]
     collide["body_steps_per_s_with_collisions"] = (ng + alive1) / (step_plus_coll_ms / 1e3)
 

@@ -3,14 +3,16 @@
 // (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2, every operation rounded on its own (no FMA
 // contraction), so the result is identical to a CPU brute force with the same expression.
 //
-//  1. keys   : cell = floor(x / cs) per axis with cs = h (1 + 1e-9), clamped to +-(2^20 - 2)
-//              (clamping only merges far cells); the 63-bit cell id is hashed (the 64-bit
-//              finaliser of MurmurHash3) into T = 2^k >= 2n buckets;
+//  1. keys   : cell = floor(x / cs) per axis with cs = 2h (1 + 1e-9), clamped to
+//              +-(2^20 - 2) (clamping only merges far cells); the 63-bit cell id is hashed
+//              (the 64-bit finaliser of MurmurHash3) into T = 2^k >= 2n buckets;
 //  2. sort   : stable radix sort of (bucket, local index) (ddx_sort.cu);
 //  3. ranges : first/last sorted position of every bucket;
-//  4. count  : every tracer visits the buckets of its 27 neighbour cells, keeps the entries
-//              whose cell id is that neighbour (hash collisions are filtered), j > i, and
-//              applies the distance test;
+//  4. count  : every tracer visits the buckets of the 8 cells of its octant: per axis its
+//              own cell and the neighbour on the side of the cell's half it lies in (a
+//              partner closer than h cannot be further, because the cell is 2h wide); on a
+//              clamped axis both neighbours.  It keeps the entries whose cell id is that
+//              cell (hash collisions are filtered), j > i, and applies the distance test;
 //  5. scan   : exclusive scan of the counts gives each tracer its output slot;
 //  6. write  : the same walk writes (i, j) and sorts the tracer's segment by j, so the list
 //              is ordered by (i, j).
@@ -47,6 +49,20 @@ __device__ __forceinline__ long long cell_coord(double x, double inv) {
     c = fmin(fmax(c, (double)-kCellLim), (double)kCellLim);
     return (long long)c;
 }
+// Neighbour offsets [lo, hi] along one axis: the cell itself and the neighbour on the side
+// of the half the tracer lies in; both neighbours on a clamped axis.  With cells 2h (1 +
+// 1e-9) wide, the rounding of x / cs (below 1e-9 of a cell for |cell| < 2^20) cannot put a
+// partner within h outside these cells.
+__device__ __forceinline__ void octant(double x, double inv, long long c, int& lo, int& hi) {
+    if (c <= -kCellLim || c >= kCellLim) {
+        lo = -1;
+        hi = 1;
+        return;
+    }
+    const double f = x * inv - (double)c;
+    lo = f < 0.5 ? -1 : 0;
+    hi = f < 0.5 ? 0 : 1;
+}
 
 __global__ void keys_kernel(ddx_state s, int i0, int n, double inv, uint32_t mask, uint32_t sentinel,
                             uint32_t* keys, uint32_t* vals, unsigned long long* cellid) {
@@ -76,7 +92,7 @@ __global__ void ranges_kernel(const uint32_t* __restrict__ keys, int n, uint32_t
 }
 
 template <bool WRITE>
-__global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, uint32_t mask, uint32_t sentinel,
+__global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, uint32_t mask, uint32_t sentinel,
                              const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                              const unsigned long long* __restrict__ cellid, const uint32_t* __restrict__ start,
                              const uint32_t* __restrict__ end, uint32_t* __restrict__ count,
@@ -92,11 +108,15 @@ __global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, uint32_t mas
     const double xi = s.x[i], yi = s.y[i], zi = s.z[i];
     long long cx, cy, cz;
     unpack_cell(cellid[p], cx, cy, cz);
+    int lx, hx, ly, hy, lz, hz;
+    octant(xi, inv, cx, lx, hx);
+    octant(yi, inv, cy, ly, hy);
+    octant(zi, inv, cz, lz, hz);
     const long long base = WRITE ? (long long)offs[p] : 0;
     uint32_t c = 0;
-    for (int dx = -1; dx <= 1; ++dx)
-        for (int dy = -1; dy <= 1; ++dy)
-            for (int dz = -1; dz <= 1; ++dz) {
+    for (int dx = lx; dx <= hx; ++dx)
+        for (int dy = ly; dy <= hy; ++dy)
+            for (int dz = lz; dz <= hz; ++dz) {
                 const unsigned long long nid = pack_cell(cx + dx, cy + dy, cz + dz);
                 const uint32_t b = bucket_of(nid, mask);
                 const uint32_t r1 = end[b];
@@ -176,7 +196,7 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
         cs = nc;
     }
     const uint32_t mask = T - 1, sentinel = T;
-    const double cell = h * (1.0 + 1e-9);
+    const double cell = 2.0 * h * (1.0 + 1e-9);
     const double inv = 1.0 / cell;
     const double h2 = h * h;
     const int thr = 256, blk = (n + thr - 1) / thr;
@@ -185,12 +205,12 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
     cudaMemsetAsync(cs->start, 0, 4ull * T, st);
     cudaMemsetAsync(cs->end, 0, 4ull * T, st);
     ranges_kernel<<<blk, thr, 0, st>>>(cs->keys, n, sentinel, cs->start, cs->end);
-    pairs_kernel<false><<<blk, thr, 0, st>>>(s, i0, n, h2, mask, sentinel, cs->keys, cs->vals, cs->cellid,
+    pairs_kernel<false><<<blk, thr, 0, st>>>(s, i0, n, h2, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid,
                                              cs->start, cs->end, cs->count, nullptr, nullptr, 0);
     uint32_t* scan_temp = cs->temp + sort_temp_words(cs->n_cap);
     if (exclusive_scan(cs->count, cs->offs, n, scan_temp, cs->total, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (pairs && cap > 0)
-        pairs_kernel<true><<<blk, thr, 0, st>>>(s, i0, n, h2, mask, sentinel, cs->keys, cs->vals, cs->cellid,
+        pairs_kernel<true><<<blk, thr, 0, st>>>(s, i0, n, h2, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid,
                                                 cs->start, cs->end, nullptr, cs->offs, pairs, cap);
     if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
     uint32_t tot = 0;

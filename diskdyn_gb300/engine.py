@@ -167,16 +167,20 @@ class Engine:
                 stream=None) -> torch.Tensor:
         """Collision pairs (m, 2) int32 on the device, ordered by (i, j): live tracers
         i < j of [i0, i1) with squared separation < h^2.  With cap=None the buffer is
-        sized from a first counting call."""
+        sized from the previous call's count (twice it, at least 4,096 pairs) and the call
+        is repeated with room for all pairs when that was too small."""
         n = C.c_longlong(0)
         sh = C.c_void_p(_stream_handle(stream))
-        if cap is None:
-            abi.check(self.lib.ddx_collide(self.ctx, C.byref(st._abi), i0, i1, float(h), None, 0,
-                                           C.byref(n), sh), "ddx_collide")
+        fixed = cap is not None
+        if not fixed:
+            cap = max(4096, 2 * getattr(self, "last_pair_count", 0))
+        while True:
+            out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=st.x.device)
+            abi.check(self.lib.ddx_collide(self.ctx, C.byref(st._abi), i0, i1, float(h),
+                                           C.c_void_p(out.data_ptr()), cap, C.byref(n), sh), "ddx_collide")
+            if fixed or n.value <= cap:
+                break
             cap = n.value
-        out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=st.x.device)
-        abi.check(self.lib.ddx_collide(self.ctx, C.byref(st._abi), i0, i1, float(h),
-                                       C.c_void_p(out.data_ptr()), cap, C.byref(n), sh), "ddx_collide")
         self.last_pair_count = n.value
         return out[:min(cap, n.value)]
 
