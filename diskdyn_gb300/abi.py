@@ -103,6 +103,8 @@ SIGNATURES = [
                                  C.c_void_p]),
     ("ddx_setup_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_ulonglong,
                                    C.POINTER(State), C.c_longlong, C.c_void_p, C.c_void_p]),
+    ("ddx_step_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double,
+                                C.POINTER(Phys), C.c_int, C.c_int, C.c_void_p]),
     ("ddx_schedule", C.c_int, [C.POINTER(Cadence), C.c_double, C.c_longlong, C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_longlong)]),
     ("ddx_run", C.c_int, [C.c_void_p, C.POINTER(State), C.c_int, C.c_int, C.c_double, C.POINTER(Phys), C.c_int,

@@ -5,6 +5,7 @@
 #include <vector>
 #include "ddx_internal.cuh"
 #include "ddx_flux.cuh"
+#include "../../include/diskdyn_gb300_run.h"
 
 using namespace ddx;
 
@@ -35,6 +36,9 @@ struct ddx_ctx {
     CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
     AdjointScratch* adjoint = nullptr;          // trajectory checkpoints of the last adjoint forward
     DetStepScratch* detstep = nullptr;          // body scan of ddx_det_step
+    // ddx_step_host: copy streams (host to device, device to host) and their events
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_comp = nullptr, ev_out = nullptr;
 };
 
 namespace {
@@ -124,17 +128,76 @@ __global__ void star_only_reference_kernel(ddx_state s, MassiveScratch ms) {
     }
 }
 
-int enqueue_step(ddx_ctx* c, const ddx_state& s, StepArgs a, int precision, cudaStream_t st) {
-    take_injection(c, a);
+// The massive set's whole step: stage positions P1..P4 for the dust and the RK4
+// combination of the massive bodies (the dust reads only the stage positions).
+int enqueue_massive(ddx_ctx* c, const ddx_state& s, const StepArgs& a, int precision, cudaStream_t st) {
     if (a.n_grav == 1 && a.mode == DDX_MODE_REFERENCE) {
         star_only_reference_kernel<<<1, 32, 0, st>>>(s, c->ms);
-        if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
-        return cuda_status(launch_dust(s, a, c->ms, c->bins, precision, st));
+        return cuda_status(cudaGetLastError());
     }
     if (launch_massive_prepare(s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (launch_massive_pass1(s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (launch_massive_pass2(s, a, c->ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
+    return DDX_OK;
+}
+
+int enqueue_step(ddx_ctx* c, const ddx_state& s, StepArgs a, int precision, cudaStream_t st) {
+    take_injection(c, a);
+    const int r = enqueue_massive(c, s, a, precision, st);
+    if (r) return r;
     return cuda_status(launch_dust(s, a, c->ms, c->bins, precision, st));
+}
+
+// Tracers per dust launch of ddx_step_host: one wave of the mixed kernel (3 resident blocks
+// of 256 on every SM), so every chunk fills the GPU once and the copies of the neighbouring
+// chunks overlap it.
+int dust_chunk(int n_dust) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
+    const int wave = sms * 3 * 256;
+    return n_dust > 2 * wave ? wave : n_dust;
+}
+
+ddx_state shifted(const ddx_state& s, long long o) {
+    return ddx_state{s.x + o, s.y + o, s.z + o, s.vx + o, s.vy + o, s.vz + o, s.m + o, s.N + o, s.id + o};
+}
+
+// Copies of bodies [o, o + n) between a host state and the device state.
+bool h2d_range(const ddx_state& d, const ddx_host_state& h, long long o, long long n, cudaStream_t st) {
+    if (n <= 0) return true;
+    double* const dd[8] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.m, d.N};
+    const double* const hh[8] = {h.x, h.y, h.z, h.vx, h.vy, h.vz, h.m, h.N};
+    for (int f = 0; f < 8; ++f)
+        if (cudaMemcpyAsync(dd[f] + o, hh[f] + o, sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return false;
+    return cudaMemcpyAsync(d.id + o, h.id + o, sizeof(int) * n, cudaMemcpyHostToDevice, st) == cudaSuccess;
+}
+bool d2h_range(const ddx_host_state& h, const ddx_state& d, long long o, long long n, cudaStream_t st) {
+    if (n <= 0) return true;
+    double* const hh[7] = {h.x, h.y, h.z, h.vx, h.vy, h.vz, h.N};
+    const double* const dd[7] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.N};
+    for (int f = 0; f < 7; ++f)
+        if (cudaMemcpyAsync(hh[f] + o, dd[f] + o, sizeof(double) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            return false;
+    return true;
+}
+
+bool host_state_ok(const ddx_host_state* h, long long n) {
+    return h && h->x && h->y && h->z && h->vx && h->vy && h->vz && h->N && h->m && h->id && h->cap >= n;
+}
+
+int ensure_pipeline(ddx_ctx* c) {
+    if (c->s_in) return DDX_OK;
+    if (cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_comp, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return DDX_ERR_CUDA;
+    }
+    return DDX_OK;
 }
 
 void free_optics(ddx_ctx* c) {
@@ -203,6 +266,11 @@ int ddx_destroy(ddx_ctx* c) {
     collide_free(c->collide);
     adjoint_free(c->adjoint);
     det_step_free(c->detstep);
+    if (c->s_in) cudaStreamDestroy(c->s_in);
+    if (c->s_out) cudaStreamDestroy(c->s_out);
+    if (c->ev_in) cudaEventDestroy(c->ev_in);
+    if (c->ev_comp) cudaEventDestroy(c->ev_comp);
+    if (c->ev_out) cudaEventDestroy(c->ev_out);
     delete c;
     return DDX_OK;
 }
@@ -273,6 +341,45 @@ int ddx_set_optics(ddx_ctx* c, int n_grid, int n_wav, int n_theta, const double*
 int ddx_step(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
              const ddx_phys* phys, int precision, int mode, void* stream) {
     return ddx_evolve(c, s, n_grav, n_dust, dt, 1, phys, precision, mode, stream);
+}
+
+int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, const ddx_state* s, int n_grav,
+                  int n_dust, double dt, const ddx_phys* phys, int precision, int mode, void* stream) {
+    if (!c || !state_ok(s) || n_grav < 1 || n_dust < 0) return DDX_ERR_ARG;
+    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    const long long n_all = (long long)n_grav + n_dust;
+    if (!host_state_ok(in, n_all) || !host_state_ok(out, n_all)) return DDX_ERR_ARG;
+    if (!c->bins) return DDX_ERR_STATE;
+    StepArgs a;
+    int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
+    if (r) return r;
+    cudaSetDevice(c->device);
+    if ((r = ensure_massive(c, n_grav)) || (r = ensure_pipeline(c))) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    take_injection(c, a);
+    // the massive bodies: in, step, out (small)
+    if (!h2d_range(*s, *in, 0, n_grav, st)) return DDX_ERR_CUDA;
+    if ((r = enqueue_massive(c, *s, a, precision, st))) return r;
+    if (!d2h_range(*out, *s, 0, n_grav, st)) return DDX_ERR_CUDA;
+    // the dust, chunk by chunk: copy-in stream -> compute stream -> copy-out stream.  The
+    // reference mode's stage-4 write lands at the chunk's own index, so it runs unchunked.
+    const int chunk = a.mode == DDX_MODE_REFERENCE ? n_dust : dust_chunk(n_dust);
+    for (int o = 0; o < n_dust; o += chunk) {
+        const int len = chunk < n_dust - o ? chunk : n_dust - o;
+        if (!h2d_range(*s, *in, n_grav + o, len, c->s_in) || cudaEventRecord(c->ev_in, c->s_in) != cudaSuccess ||
+            cudaStreamWaitEvent(st, c->ev_in, 0) != cudaSuccess)
+            return DDX_ERR_CUDA;
+        StepArgs ac = a;
+        ac.n_dust = len;
+        if (o > 0) ac.lose_tile = -1;
+        if (launch_dust(shifted(*s, o), ac, c->ms, c->bins, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
+        if (cudaEventRecord(c->ev_comp, st) != cudaSuccess || cudaStreamWaitEvent(c->s_out, c->ev_comp, 0) != cudaSuccess ||
+            !d2h_range(*out, *s, n_grav + o, len, c->s_out))
+            return DDX_ERR_CUDA;
+    }
+    if (cudaEventRecord(c->ev_out, c->s_out) != cudaSuccess || cudaStreamWaitEvent(st, c->ev_out, 0) != cudaSuccess)
+        return DDX_ERR_CUDA;
+    return cuda_status(cudaStreamSynchronize(st));
 }
 
 int ddx_evolve(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,

@@ -257,6 +257,21 @@ class Engine:
                                             C.c_void_p(_stream_handle(stream))), "ddx_setup_device")
         return st, run
 
+    def step_host(self, st: DeviceState, host_in: dict, host_out: dict, n_grav: int, dt: float, phys: abi.Phys,
+                  precision: int = abi.DDX_PREC_MIXED, mode: int = abi.DDX_MODE_FIXED, stream=None) -> None:
+        """ddx_step_host: one step of the state in host_in (CPU tensors or arrays, page-locked
+        for overlap), staged through the device state st, results into host_out."""
+        from .formats import HostState
+
+        def hs(d):
+            ptr = lambda t: t.data_ptr() if isinstance(t, torch.Tensor) else t.ctypes.data
+            return HostState(*[ptr(d[f]) for f in ("x", "y", "z", "vx", "vy", "vz", "N", "m", "id")], st.n_all)
+
+        hin, hout = hs(host_in), hs(host_out)
+        abi.check(self.lib.ddx_step_host(self.ctx, C.byref(hin), C.byref(hout), C.byref(st._abi), n_grav,
+                                         st.n_all - n_grav, float(dt), C.byref(phys), precision, mode,
+                                         C.c_void_p(_stream_handle(stream))), "ddx_step_host")
+
     def run(self, st: DeviceState, n_grav: int, dt: float, phys: abi.Phys, view: abi.View, wj, cadence: dict,
             on_output, precision: int = abi.DDX_PREC_MIXED, mode: int = abi.DDX_MODE_FIXED, stream=None) -> dict:
         """ddx_run: Grid::evolve with its output cadence.  cadence holds t_write, t_fits,

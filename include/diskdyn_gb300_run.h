@@ -60,6 +60,17 @@ int ddx_run(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
             int precision, int mode, const ddx_view *view, const int *wj, int nwavs, ddx_cadence *cad,
             ddx_output_fn fn, void *user, void *stream);
 
+/* One ddx_step of a system held in host memory: in (host, n_grav + n_dust bodies) is copied
+ * to the device state s, stepped, and the updated positions, velocities and grain numbers
+ * come back into out (m and id are not changed by a step and are not copied back).  The
+ * massive bodies go first; the dust then streams through in chunks of one wave of the dust
+ * kernel, the copy in of chunk k+1 and the copy out of chunk k-1 on their own streams
+ * overlapping chunk k's compute (the reference mode runs the dust in one chunk).  Overlap
+ * needs page-locked host memory.  in and out may be the same arrays.  Synchronises
+ * `stream`. */
+int ddx_step_host(ddx_ctx *ctx, const ddx_host_state *in, ddx_host_state *out, const ddx_state *s, int n_grav,
+                  int n_dust, double dt, const ddx_phys *phys, int precision, int mode, void *stream);
+
 /* The steps and outputs ddx_run makes for this cadence and dt, on the host without a GPU:
  * step_dt[k] is step k's size and outputs[k] the outputs due after it, a mask of
  * 1 << DDX_OUT_SED, 1 << DDX_OUT_IMAGES and 1 << DDX_OUT_STATE (the images are skipped by
