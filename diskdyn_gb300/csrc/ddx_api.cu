@@ -148,15 +148,17 @@ int enqueue_step(ddx_ctx* c, const ddx_state& s, StepArgs a, int precision, cuda
     return cuda_status(launch_dust(s, a, c->ms, c->bins, precision, st));
 }
 
-// Tracers per dust launch of ddx_step_host: one wave of the mixed kernel (3 resident blocks
-// of 256 on every SM), so every chunk fills the GPU once and the copies of the neighbouring
-// chunks overlap it.
-int dust_chunk(int n_dust) {
+// Dust chunks of ddx_step_host: one wave of the mixed kernel (3 resident blocks of 256 on
+// every SM) first and last, the rest in one launch between them.  The first chunk's copy in
+// and the last chunk's copy out are all that is not overlapped; every extra launch costs
+// the spread of its blocks' finishing times, so there are no more than three.
+std::vector<int> dust_chunks(int n_dust) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
     const int wave = sms * 3 * 256;
-    return n_dust > 2 * wave ? wave : n_dust;
+    if (n_dust < 4 * wave) return {n_dust};
+    return {wave, n_dust - 2 * wave, wave};
 }
 
 ddx_state shifted(const ddx_state& s, long long o) {
@@ -363,9 +365,10 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
     if (!d2h_range(*out, *s, 0, n_grav, st)) return DDX_ERR_CUDA;
     // the dust, chunk by chunk: copy-in stream -> compute stream -> copy-out stream.  The
     // reference mode's stage-4 write lands at the chunk's own index, so it runs unchunked.
-    const int chunk = a.mode == DDX_MODE_REFERENCE ? n_dust : dust_chunk(n_dust);
-    for (int o = 0; o < n_dust; o += chunk) {
-        const int len = chunk < n_dust - o ? chunk : n_dust - o;
+    const std::vector<int> chunks = a.mode == DDX_MODE_REFERENCE ? std::vector<int>{n_dust} : dust_chunks(n_dust);
+    int o = 0;
+    for (const int len : chunks) {
+        if (len <= 0) continue;
         if (!h2d_range(*s, *in, n_grav + o, len, c->s_in) || cudaEventRecord(c->ev_in, c->s_in) != cudaSuccess ||
             cudaStreamWaitEvent(st, c->ev_in, 0) != cudaSuccess)
             return DDX_ERR_CUDA;
@@ -376,6 +379,7 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
         if (cudaEventRecord(c->ev_comp, st) != cudaSuccess || cudaStreamWaitEvent(c->s_out, c->ev_comp, 0) != cudaSuccess ||
             !d2h_range(*out, *s, n_grav + o, len, c->s_out))
             return DDX_ERR_CUDA;
+        o += len;
     }
     if (cudaEventRecord(c->ev_out, c->s_out) != cudaSuccess || cudaStreamWaitEvent(st, c->ev_out, 0) != cudaSuccess)
         return DDX_ERR_CUDA;

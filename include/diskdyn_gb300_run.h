@@ -63,9 +63,10 @@ int ddx_run(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
 /* One ddx_step of a system held in host memory: in (host, n_grav + n_dust bodies) is copied
  * to the device state s, stepped, and the updated positions, velocities and grain numbers
  * come back into out (m and id are not changed by a step and are not copied back).  The
- * massive bodies go first; the dust then streams through in chunks of one wave of the dust
- * kernel, the copy in of chunk k+1 and the copy out of chunk k-1 on their own streams
- * overlapping chunk k's compute (the reference mode runs the dust in one chunk).  Overlap
+ * massive bodies go first; the dust then goes through in up to three chunks (one wave of the
+ * dust kernel, the bulk, one wave), the copy in of chunk k+1 and the copy out of chunk k-1
+ * on their own streams overlapping chunk k's compute (the reference mode, and fewer than
+ * four waves of grains, run the dust in one chunk).  Overlap
  * needs page-locked host memory.  in and out may be the same arrays.  Synchronises
  * `stream`. */
 int ddx_step_host(ddx_ctx *ctx, const ddx_host_state *in, ddx_host_state *out, const ddx_state *s, int n_grav,

@@ -1,5 +1,5 @@
 """ddx_step_host: one step of a system in host memory, the dust streamed through the GPU in
-chunks of one kernel wave with the copies on their own streams.  Each tracer's step does
+up to three chunks with the copies on their own streams.  Each tracer's step does
 not depend on the others, so the result must equal ddx_step on the device bit for bit,
 whatever the chunking; the reference mode runs unchunked."""
 import numpy as np
@@ -22,7 +22,7 @@ def pinned(arrays):
                                        (abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED),
                                        (abi.DDX_PREC_MIXED, abi.DDX_MODE_REFERENCE)])
 def test_host_step_equals_device_step(prec, mode):
-    n_dust = 300000 if prec == abi.DDX_PREC_MIXED else 40000     # mixed: three chunks of unequal size
+    n_dust = 500000 if prec == abi.DDX_PREC_MIXED else 40000     # mixed: three chunks of unequal size
     s = synth.dusty_ring(n_dust=n_dust, n_plsml=64, seed=12)
     eng = Engine(0)
     eng.set_size_table(**s.size_table)
