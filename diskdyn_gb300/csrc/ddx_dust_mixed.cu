@@ -18,52 +18,13 @@
 //    context's status word, waits (bounded) for its own copies, leaves its tracers
 //    untouched and exits.
 #include "ddx_internal.cuh"
+#include "ddx_f32x2.cuh"
 
 namespace ddx {
 namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTilePairs = 512;                 // pair records per tile (32 KiB)
-
-typedef unsigned long long f2;   // two FP32 lanes of one f32x2 instruction
-
-__device__ __forceinline__ f2 f2_dup(float a) {
-    f2 r; asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a)); return r;
-}
-__device__ __forceinline__ void f2_split(f2 v, float& lo, float& hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 f2_join(float lo, float hi) {
-    f2 r; asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi)); return r;
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-    f2 r; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 r; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 r; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b)); return r;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 r; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c)); return r;
-}
-__device__ __forceinline__ float rsqrt_approx(float x) {
-    float r; asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r;
-}
-__device__ __forceinline__ void kahan2(f2& S, f2& C, f2 v) {
-    const f2 y = sub2(v, C);
-    const f2 t = add2(S, y);
-    C = sub2(sub2(t, S), y);
-    S = t;
-}
-// Compensated sum of both lanes of (S, C), in FP64.
-__device__ __forceinline__ double f2_total(f2 S, f2 C) {
-    float s0, s1, c0, c1;
-    f2_split(S, s0, s1);
-    f2_split(C, c0, c1);
-    return ((double)s0 - (double)c0) + ((double)s1 - (double)c1);
-}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);

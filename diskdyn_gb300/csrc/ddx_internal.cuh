@@ -81,6 +81,9 @@ struct MassiveScratch {
     int      *status; // device status word: DDX_STATUS_* bits set by kernels
     int       cap;
     int       pcap;   // pair records per stage, >= pair_count(cap)
+    double   *part;   // [slices][6][cap] per-slice sums of the mixed passes (null: one warp
+                      // per target instead)
+    long long part_words;
 };
 
 // Bits of the device status word.
@@ -136,6 +139,10 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
                                  int precision, cudaStream_t st);
 cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                         const SizeBin* bins, int precision, cudaStream_t st);
+// Source slices of the mixed massive passes for n_grav bodies (about two blocks per SM),
+// and the doubles of MassiveScratch::part they need.
+int massive_slices(int n_grav, int n_exact);
+long long massive_part_words(int n_grav, int cap);
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                               const SizeBin* bins, cudaStream_t st);
 

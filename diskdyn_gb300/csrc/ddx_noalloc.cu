@@ -99,6 +99,8 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     ms.status = reinterpret_cast<int*>(base + kOffStatus);
     ms.cap = kCap;
     ms.pcap = kPcap;
+    ms.part = nullptr;          // no room for slice sums: one warp per target
+    ms.part_words = 0;
     SizeBin* bins = reinterpret_cast<SizeBin*>(base + kOffBins);
 
     StepArgs a;

@@ -15,6 +15,7 @@
 // per step with CAS atomics; here it is prepare + pass1 + pass2 + dust, deterministic, with
 // no atomics.
 #include "ddx_internal.cuh"
+#include "ddx_f32x2.cuh"
 
 namespace ddx {
 
@@ -166,13 +167,8 @@ __device__ __forceinline__ void store_stage_pos(MassiveScratch& ms, int stage, i
 
 // Pass 1: A1 at P1, A2 at P2; then R2, P3, R3, P4 for the target
 // (src/gpu_functions.cu:219-230, 350-362, 482-493).
-template <int PREC>
-__global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= a.n_grav) return;  // warp-uniform
-    double acc[6];
-    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 0, 1, acc);
-    if ((threadIdx.x & 31) != 0) return;
+__device__ __forceinline__ void pass1_update(const ddx_state& s, const StepArgs& a, MassiveScratch& ms, int i,
+                                             const double acc[6], int prec) {
     const int c = ms.cap;
     double* A = ms.A;
     double* R = ms.R;
@@ -186,19 +182,24 @@ __global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     const double k4x = x + k3rx * a.dt, k4y = y + k3ry * a.dt, k4z = z + k3rz * a.dt;
     R[(0 * 3 + 0) * c + i] = k2rx; R[(0 * 3 + 1) * c + i] = k2ry; R[(0 * 3 + 2) * c + i] = k2rz;
     R[(1 * 3 + 0) * c + i] = k3rx; R[(1 * 3 + 1) * c + i] = k3ry; R[(1 * 3 + 2) * c + i] = k3rz;
-    store_stage_pos(ms, 2, i, k3x, k3y, k3z, m, PREC, a.n_exact);
-    store_stage_pos(ms, 3, i, k4x, k4y, k4z, m, PREC, a.n_exact);
+    store_stage_pos(ms, 2, i, k3x, k3y, k3z, m, prec, a.n_exact);
+    store_stage_pos(ms, 3, i, k4x, k4y, k4z, m, prec, a.n_exact);
+}
+
+template <int PREC>
+__global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.n_grav) return;  // warp-uniform
+    double acc[6];
+    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 0, 1, acc);
+    if ((threadIdx.x & 31) != 0) return;
+    pass1_update(s, a, ms, i, acc, PREC);
 }
 
 // Pass 2: A3 at P3, A4 at P4; R4; final combination (src/gpu_functions.cu:613-625).
 // Reads only stage records of other bodies, so updating x, v of the target is safe.
-template <int PREC>
-__global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= a.n_grav) return;
-    double acc[6];
-    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 2, 3, acc);
-    if ((threadIdx.x & 31) != 0) return;
+__device__ __forceinline__ void pass2_update(const ddx_state& s, const StepArgs& a, MassiveScratch& ms, int i,
+                                             const double acc[6]) {
     const int c = ms.cap;
     double* A = ms.A;
     const double* R = ms.R;
@@ -213,6 +214,139 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     s.vx[i] += dt * (A[(0 * 3 + 0) * c + i] + 2.0 * A[(1 * 3 + 0) * c + i] + 2.0 * acc[0] + acc[3]);
     s.vy[i] += dt * (A[(0 * 3 + 1) * c + i] + 2.0 * A[(1 * 3 + 1) * c + i] + 2.0 * acc[1] + acc[4]);
     s.vz[i] += dt * (A[(0 * 3 + 2) * c + i] + 2.0 * A[(1 * 3 + 2) * c + i] + 2.0 * acc[2] + acc[5]);
+}
+
+template <int PREC>
+__global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.n_grav) return;
+    double acc[6];
+    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 2, 3, acc);
+    if ((threadIdx.x & 31) != 0) return;
+    pass2_update(s, a, ms, i, acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// Mixed massive passes over source slices
+// ---------------------------------------------------------------------------------------
+// A few thousand targets leave most of the GPU idle when one warp serves one target, so
+// the FP32 pulls of the planetesimals are split over source slices: block (target group of
+// kSliceThreads, slice k) stages the slice's pair records of the pass's two stages in
+// shared memory, every thread (one target) reads each record at once (broadcast) and
+// works on both sources of a record with one f32x2 instruction, in plain sums over spans
+// of kPairSpan records with a Kahan sum across spans (the dust kernel's scheme).  A
+// target's own slot gives RR = 0 and is masked.  The star (target 0) takes the
+// planetesimals' pulls in FP64.  massive_gather_kernel then adds the slices in slice order
+// (deterministic), adds the FP64 pulls of bodies 0..n_exact-1 and applies the pass's
+// update.
+constexpr int kSliceThreads = 256;
+constexpr int kSliceTile = 256;       // pair records per stage staged at once (16 KiB)
+
+__device__ __forceinline__ void pair_f2(const BodyPair& r, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH, f2 ZL, f2& px,
+                                        f2& py, f2& pz) {
+    const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r.hx);   // hx, hy
+    const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r.hz);   // hz, m
+    const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r.lx);   // lx, ly
+    const f2 lz = *reinterpret_cast<const f2*>(r.lz);
+    const f2 dX = add2(sub2(q0.x, XH), sub2(q2.x, XL));
+    const f2 dY = add2(sub2(q0.y, YH), sub2(q2.y, YL));
+    const f2 dZ = add2(sub2(q1.x, ZH), sub2(lz, ZL));
+    const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+    float r0, r1;
+    f2_split(RR, r0, r1);
+    const f2 ri = f2_join(r0 > 0.f ? rsqrt_approx(r0) : 0.f, r1 > 0.f ? rsqrt_approx(r1) : 0.f);
+    const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
+    px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+}
+
+__global__ void __launch_bounds__(kSliceThreads)
+massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, double* __restrict__ part) {
+    __shared__ __align__(16) BodyPair tile[2][kSliceTile];
+    const int i = blockIdx.x * kSliceThreads + threadIdx.x;
+    const int k = blockIdx.y;
+    const int sb = sa + 1;
+    const int n_src = a.n_grav - a.n_exact;
+    const int npairs = pair_count(n_src);
+    const int r0 = k * per, r1 = min(r0 + per, npairs);
+    const bool active = i < a.n_grav;
+    const int c = ms.cap;
+    float4 ha = make_float4(0.f, 0.f, 0.f, 0.f), la = ha, hb = ha, lb = ha;
+    Body pa = make_body(0.0, 0.0, 0.0, 0.0), pb = pa;
+    if (active) {
+        ha = ms.Phi[sa * c + i]; la = ms.Plo[sa * c + i];
+        hb = ms.Phi[sb * c + i]; lb = ms.Plo[sb * c + i];
+        pa = ms.P[sa * c + i]; pb = ms.P[sb * c + i];
+    }
+    const f2 XHa = f2_dup(ha.x), XLa = f2_dup(la.x), YHa = f2_dup(ha.y), YLa = f2_dup(la.y);
+    const f2 ZHa = f2_dup(ha.z), ZLa = f2_dup(la.z);
+    const f2 XHb = f2_dup(hb.x), XLb = f2_dup(lb.x), YHb = f2_dup(hb.y), YLb = f2_dup(lb.y);
+    const f2 ZHb = f2_dup(hb.z), ZLb = f2_dup(lb.z);
+    f2 SA[3] = {0, 0, 0}, CA[3] = {0, 0, 0}, SB[3] = {0, 0, 0}, CB[3] = {0, 0, 0};
+    double dA[3] = {0.0, 0.0, 0.0}, dB[3] = {0.0, 0.0, 0.0};
+    for (int t0 = r0; t0 < r1; t0 += kSliceTile) {
+        const int cnt = min(kSliceTile, r1 - t0);          // a multiple of kPairSpan
+        __syncthreads();                                   // the previous tile is consumed
+        const uint4* ga = reinterpret_cast<const uint4*>(ms.PP + (size_t)sa * ms.pcap + t0);
+        const uint4* gb = reinterpret_cast<const uint4*>(ms.PP + (size_t)sb * ms.pcap + t0);
+        uint4* ta = reinterpret_cast<uint4*>(tile[0]);
+        uint4* tb = reinterpret_cast<uint4*>(tile[1]);
+        for (int w = threadIdx.x; w < cnt * 4; w += kSliceThreads) {
+            ta[w] = ga[w];
+            tb[w] = gb[w];
+        }
+        __syncthreads();
+        if (!active) continue;
+        if (i == 0) {
+            // the star: the planetesimals of this tile in FP64
+            const int q1 = min(2 * (t0 + cnt), n_src);
+            for (int q = 2 * t0; q < q1; ++q) {
+                const int j = a.n_exact + q;
+                pair64(pa, ms.P[sa * c + j], dA[0], dA[1], dA[2]);
+                pair64(pb, ms.P[sb * c + j], dB[0], dB[1], dB[2]);
+            }
+            continue;
+        }
+        for (int u0 = 0; u0 < cnt; u0 += kPairSpan) {
+            f2 ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+#pragma unroll 4
+            for (int u = 0; u < kPairSpan; ++u) {
+                pair_f2(tile[0][u0 + u], XHa, XLa, YHa, YLa, ZHa, ZLa, ax, ay, az);
+                pair_f2(tile[1][u0 + u], XHb, XLb, YHb, YLb, ZHb, ZLb, bx, by, bz);
+            }
+            kahan2(SA[0], CA[0], ax); kahan2(SA[1], CA[1], ay); kahan2(SA[2], CA[2], az);
+            kahan2(SB[0], CB[0], bx); kahan2(SB[1], CB[1], by); kahan2(SB[2], CB[2], bz);
+        }
+    }
+    if (!active) return;
+    double* o = part + (size_t)k * 6 * c + i;
+    if (i == 0) {
+        o[0] = dA[0]; o[c] = dA[1]; o[2 * c] = dA[2];
+        o[3 * c] = dB[0]; o[4 * c] = dB[1]; o[5 * c] = dB[2];
+    } else {
+        o[0] = f2_total(SA[0], CA[0]); o[c] = f2_total(SA[1], CA[1]); o[2 * c] = f2_total(SA[2], CA[2]);
+        o[3 * c] = f2_total(SB[0], CB[0]); o[4 * c] = f2_total(SB[1], CB[1]); o[5 * c] = f2_total(SB[2], CB[2]);
+    }
+}
+
+template <int PASS>
+__global__ void massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int slices,
+                                      const double* __restrict__ part) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n_grav) return;
+    const int c = ms.cap;
+    const int sa = PASS == 1 ? 0 : 2, sb = sa + 1;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < slices; ++k)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) acc[q] += part[((size_t)k * 6 + q) * c + i];
+    const Body pa = ms.P[sa * c + i], pb = ms.P[sb * c + i];
+    for (int j = 0; j < a.n_exact && j < a.n_grav; ++j) {
+        if (j == i) continue;
+        pair64(pa, ms.P[sa * c + j], acc[0], acc[1], acc[2]);
+        pair64(pb, ms.P[sb * c + j], acc[3], acc[4], acc[5]);
+    }
+    if (PASS == 1) pass1_update(s, a, ms, i, acc, DDX_PREC_MIXED);
+    else pass2_update(s, a, ms, i, acc);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -371,8 +505,54 @@ cudaError_t launch_massive_prepare(const ddx_state& s, const StepArgs& a, Massiv
     return cudaGetLastError();
 }
 
+namespace {
+int sm_count() {
+    static int cached[128] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 128) return 152;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+// The sliced mixed pass: slice sums, then their gather with the pass's update.
+template <int PASS>
+cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch& ms, cudaStream_t st) {
+    const int S = massive_slices(a.n_grav, a.n_exact);
+    const int spans = pair_count(a.n_grav - a.n_exact) / kPairSpan;
+    const int per = (spans + S - 1) / S * kPairSpan;
+    const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads, S);
+    massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, ms.part);
+    massive_gather_kernel<PASS><<<(a.n_grav + 127) / 128, 128, 0, st>>>(s, a, ms, S, ms.part);
+    return cudaGetLastError();
+}
+}  // namespace
+
+int massive_slices(int n_grav, int n_exact) {
+    const int groups = (n_grav + kSliceThreads - 1) / kSliceThreads;
+    const int spans = pair_count(n_grav - n_exact) / kPairSpan;
+    int S = (2 * sm_count() + groups - 1) / groups;
+    if (S > 32) S = 32;
+    if (S > spans) S = spans;
+    return S < 1 ? 1 : S;
+}
+
+long long massive_part_words(int n_grav, int cap) {
+    const int groups = (n_grav + kSliceThreads - 1) / kSliceThreads;
+    long long S = (2 * sm_count() + groups - 1) / groups;
+    if (S > 32) S = 32;
+    return (S < 1 ? 1 : S) * 6LL * cap;
+}
+
 cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                  int precision, cudaStream_t st) {
+    if (precision == DDX_PREC_MIXED && ms.part &&
+        ms.part_words >= (long long)massive_slices(a.n_grav, a.n_exact) * 6 * ms.cap)
+        return launch_sliced<1>(s, a, ms, st);
     const int threads = 128;  // 4 targets per block
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
     if (precision == DDX_PREC_MIXED) massive_pass1_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
@@ -382,6 +562,9 @@ cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveS
 
 cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                  int precision, cudaStream_t st) {
+    if (precision == DDX_PREC_MIXED && ms.part &&
+        ms.part_words >= (long long)massive_slices(a.n_grav, a.n_exact) * 6 * ms.cap)
+        return launch_sliced<2>(s, a, ms, st);
     const int threads = 128;
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
     if (precision == DDX_PREC_MIXED) massive_pass2_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
