@@ -69,20 +69,7 @@ void free_massive(MassiveScratch& ms) {
 }
 
 int ensure_massive(ddx_ctx* c, int n_grav) {
-    if (c->ms.cap >= n_grav && c->ms.P) {
-        // the slice sums of the mixed passes, grown when this system needs more slices
-        const long long need = massive_part_words(n_grav, c->ms.cap);
-        if (c->ms.part_words >= need) return DDX_OK;
-        double* p = nullptr;
-        if (dalloc(&p, (size_t)need) != cudaSuccess) {
-            cudaGetLastError();
-            return DDX_OK;          // the passes fall back to one warp per target
-        }
-        cudaFree(c->ms.part);
-        c->ms.part = p;
-        c->ms.part_words = need;
-        return DDX_OK;
-    }
+    if (c->ms.cap >= n_grav && c->ms.P) return DDX_OK;
     free_massive(c->ms);
     int cap = 64;
     while (cap < n_grav) cap *= 2;
@@ -90,7 +77,7 @@ int ensure_massive(ddx_ctx* c, int n_grav) {
     ms.cap = cap;
     ms.pcap = pair_count(cap) + kPairSpan;
     ms.status = c->status;
-    ms.part_words = massive_part_words(n_grav, cap);
+    ms.part_words = massive_part_words(cap);
     if (dalloc(&ms.P, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.Phi, (size_t)4 * cap) != cudaSuccess ||
         dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.PP, (size_t)4 * ms.pcap) != cudaSuccess ||
         dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess || dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess ||

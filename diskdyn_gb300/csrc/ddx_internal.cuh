@@ -81,8 +81,8 @@ struct MassiveScratch {
     int      *status; // device status word: DDX_STATUS_* bits set by kernels
     int       cap;
     int       pcap;   // pair records per stage, >= pair_count(cap)
-    double   *part;   // [slices][6][cap] per-slice sums of the mixed passes (null: one warp
-                      // per target instead)
+    double   *part;   // [slices][6][n_grav rounded to 256] per-slice sums of the mixed passes
+                      // (null: one warp per target instead)
     long long part_words;
 };
 
@@ -140,9 +140,9 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
 cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                         const SizeBin* bins, int precision, cudaStream_t st);
 // Source slices of the mixed massive passes for n_grav bodies (about two blocks per SM),
-// and the doubles of MassiveScratch::part they need.
+// and the doubles of MassiveScratch::part that cover every system of up to cap bodies.
 int massive_slices(int n_grav, int n_exact);
-long long massive_part_words(int n_grav, int cap);
+long long massive_part_words(int cap);
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                               const SizeBin* bins, cudaStream_t st);
 

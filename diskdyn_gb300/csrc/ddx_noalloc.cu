@@ -31,7 +31,10 @@ constexpr size_t kOffA = kOffPP + align256(sizeof(BodyPair) * 4 * kPcap);
 constexpr size_t kOffR = kOffA + align256(sizeof(double) * 12 * kCap);
 constexpr size_t kOffBins = kOffR + align256(sizeof(double) * 9 * kCap);
 constexpr size_t kOffStatus = kOffBins + align256(sizeof(SizeBin) * DDX_MAX_SIZE_BINS);
-constexpr size_t kBytes = kOffStatus + 256;
+// slice sums of the mixed passes: massive_part_words(kCap) for up to 160 SMs
+constexpr long long kPartWords = 6LL * 256 * (2LL * 160 + (kCap + 255) / 256);
+constexpr size_t kOffPart = kOffStatus + 256;
+constexpr size_t kBytes = kOffPart + align256(sizeof(double) * kPartWords);
 
 static __device__ __align__(256) unsigned char g_step_scratch[kBytes];
 
@@ -99,8 +102,8 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     ms.status = reinterpret_cast<int*>(base + kOffStatus);
     ms.cap = kCap;
     ms.pcap = kPcap;
-    ms.part = nullptr;          // no room for slice sums: one warp per target
-    ms.part_words = 0;
+    ms.part = reinterpret_cast<double*>(base + kOffPart);
+    ms.part_words = kPartWords;   // the passes check it against the device's SM count
     SizeBin* bins = reinterpret_cast<SizeBin*>(base + kOffBins);
 
     StepArgs a;

@@ -260,7 +260,7 @@ __device__ __forceinline__ void pair_f2(const BodyPair& r, f2 XH, f2 XL, f2 YH, 
 }
 
 __global__ void __launch_bounds__(kSliceThreads)
-massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, double* __restrict__ part) {
+massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, double* __restrict__ part) {
     __shared__ __align__(16) BodyPair tile[2][kSliceTile];
     const int i = blockIdx.x * kSliceThreads + threadIdx.x;
     const int k = blockIdx.y;
@@ -318,18 +318,18 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, double* __r
         }
     }
     if (!active) return;
-    double* o = part + (size_t)k * 6 * c + i;
+    double* o = part + (size_t)k * 6 * np + i;
     if (i == 0) {
-        o[0] = dA[0]; o[c] = dA[1]; o[2 * c] = dA[2];
-        o[3 * c] = dB[0]; o[4 * c] = dB[1]; o[5 * c] = dB[2];
+        o[0] = dA[0]; o[np] = dA[1]; o[2 * np] = dA[2];
+        o[3 * np] = dB[0]; o[4 * np] = dB[1]; o[5 * np] = dB[2];
     } else {
-        o[0] = f2_total(SA[0], CA[0]); o[c] = f2_total(SA[1], CA[1]); o[2 * c] = f2_total(SA[2], CA[2]);
-        o[3 * c] = f2_total(SB[0], CB[0]); o[4 * c] = f2_total(SB[1], CB[1]); o[5 * c] = f2_total(SB[2], CB[2]);
+        o[0] = f2_total(SA[0], CA[0]); o[np] = f2_total(SA[1], CA[1]); o[2 * np] = f2_total(SA[2], CA[2]);
+        o[3 * np] = f2_total(SB[0], CB[0]); o[4 * np] = f2_total(SB[1], CB[1]); o[5 * np] = f2_total(SB[2], CB[2]);
     }
 }
 
 template <int PASS>
-__global__ void massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int slices,
+__global__ void massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int slices, int np,
                                       const double* __restrict__ part) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n_grav) return;
@@ -338,7 +338,7 @@ __global__ void massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int k = 0; k < slices; ++k)
 #pragma unroll
-        for (int q = 0; q < 6; ++q) acc[q] += part[((size_t)k * 6 + q) * c + i];
+        for (int q = 0; q < 6; ++q) acc[q] += part[((size_t)k * 6 + q) * np + i];
     const Body pa = ms.P[sa * c + i], pb = ms.P[sb * c + i];
     for (int j = 0; j < a.n_exact && j < a.n_grav; ++j) {
         if (j == i) continue;
@@ -520,14 +520,22 @@ int sm_count() {
 }
 
 // The sliced mixed pass: slice sums, then their gather with the pass's update.
+// Slice sums are stored [slice][component][np] with np = n_grav rounded up to a block.
+int slice_stride(int n_grav) { return (n_grav + kSliceThreads - 1) / kSliceThreads * kSliceThreads; }
+
+bool sliced_fits(const StepArgs& a, const MassiveScratch& ms) {
+    return ms.part && ms.part_words >= (long long)massive_slices(a.n_grav, a.n_exact) * 6 * slice_stride(a.n_grav);
+}
+
 template <int PASS>
 cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch& ms, cudaStream_t st) {
     const int S = massive_slices(a.n_grav, a.n_exact);
     const int spans = pair_count(a.n_grav - a.n_exact) / kPairSpan;
     const int per = (spans + S - 1) / S * kPairSpan;
+    const int np = slice_stride(a.n_grav);
     const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads, S);
-    massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, ms.part);
-    massive_gather_kernel<PASS><<<(a.n_grav + 127) / 128, 128, 0, st>>>(s, a, ms, S, ms.part);
+    massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
+    massive_gather_kernel<PASS><<<(a.n_grav + 127) / 128, 128, 0, st>>>(s, a, ms, S, np, ms.part);
     return cudaGetLastError();
 }
 }  // namespace
@@ -541,18 +549,16 @@ int massive_slices(int n_grav, int n_exact) {
     return S < 1 ? 1 : S;
 }
 
-long long massive_part_words(int n_grav, int cap) {
-    const int groups = (n_grav + kSliceThreads - 1) / kSliceThreads;
-    long long S = (2 * sm_count() + groups - 1) / groups;
-    if (S > 32) S = 32;
-    return (S < 1 ? 1 : S) * 6LL * cap;
+// S * np <= (2 SMs / groups + 1) * groups * kSliceThreads, which grows with the groups, so
+// the bound at the capacity covers every smaller system.
+long long massive_part_words(int cap) {
+    const long long groups = (cap + kSliceThreads - 1) / kSliceThreads;
+    return 6LL * kSliceThreads * (2LL * sm_count() + groups);
 }
 
 cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                  int precision, cudaStream_t st) {
-    if (precision == DDX_PREC_MIXED && ms.part &&
-        ms.part_words >= (long long)massive_slices(a.n_grav, a.n_exact) * 6 * ms.cap)
-        return launch_sliced<1>(s, a, ms, st);
+    if (precision == DDX_PREC_MIXED && sliced_fits(a, ms)) return launch_sliced<1>(s, a, ms, st);
     const int threads = 128;  // 4 targets per block
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
     if (precision == DDX_PREC_MIXED) massive_pass1_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
@@ -562,9 +568,7 @@ cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveS
 
 cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                  int precision, cudaStream_t st) {
-    if (precision == DDX_PREC_MIXED && ms.part &&
-        ms.part_words >= (long long)massive_slices(a.n_grav, a.n_exact) * 6 * ms.cap)
-        return launch_sliced<2>(s, a, ms, st);
+    if (precision == DDX_PREC_MIXED && sliced_fits(a, ms)) return launch_sliced<2>(s, a, ms, st);
     const int threads = 128;
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
     if (precision == DDX_PREC_MIXED) massive_pass2_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
