@@ -313,7 +313,7 @@ def run_ours(args, world, rank, local):
                      "fp64_peak_tflops": fp64_peak, "traffic": None,
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 6 * args.steps,      # prepare, 2 x (slice sums + gather), dust
         "clocks": clk.summary(),
     }
     if rank == 0 and args.adjoint_steps > 0:

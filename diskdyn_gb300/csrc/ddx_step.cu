@@ -236,7 +236,8 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
 // works on both sources of a record with one f32x2 instruction, in plain sums over spans
 // of kPairSpan records with a Kahan sum across spans (the dust kernel's scheme).  A
 // target's own slot gives RR = 0 and is masked.  The star (target 0) takes the
-// planetesimals' pulls in FP64.  massive_gather_kernel then adds the slices in slice order
+// planetesimals' pulls in FP64, in an extra row of blocks that spread each slice over a
+// whole block (a fixed-order tree sum).  massive_gather_kernel then adds the slices in slice order
 // (deterministic), adds the FP64 pulls of bodies 0..n_exact-1 and applies the pass's
 // update.
 constexpr int kSliceThreads = 256;
@@ -259,30 +260,57 @@ __device__ __forceinline__ void pair_f2(const BodyPair& r, f2 XH, f2 XL, f2 YH, 
     px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
 }
 
+// Deterministic block sum of v (fixed tree order); the result in thread 0.
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kSliceThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
 __global__ void __launch_bounds__(kSliceThreads)
 massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, double* __restrict__ part) {
     __shared__ __align__(16) BodyPair tile[2][kSliceTile];
-    const int i = blockIdx.x * kSliceThreads + threadIdx.x;
     const int k = blockIdx.y;
     const int sb = sa + 1;
     const int n_src = a.n_grav - a.n_exact;
     const int npairs = pair_count(n_src);
     const int r0 = k * per, r1 = min(r0 + per, npairs);
-    const bool active = i < a.n_grav;
     const int c = ms.cap;
+    if (blockIdx.x == gridDim.x - 1) {
+        // the star's row: the whole block takes the slice's planetesimals in FP64
+        const Body pa = ms.P[sa * c], pb = ms.P[sb * c];
+        double d[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        const int q1 = min(2 * r1, n_src);
+        for (int q = 2 * r0 + threadIdx.x; q < q1; q += kSliceThreads) {
+            pair64(pa, ms.P[sa * c + a.n_exact + q], d[0], d[1], d[2]);
+            pair64(pb, ms.P[sb * c + a.n_exact + q], d[3], d[4], d[5]);
+        }
+        double* red = reinterpret_cast<double*>(&tile[0][0]);     // 2 KiB of the tile space
+        double* o = part + (size_t)k * 6 * np;
+        for (int q = 0; q < 6; ++q) {
+            const double t = block_sum(d[q], red);
+            if (threadIdx.x == 0) o[(size_t)q * np] = t;
+        }
+        return;
+    }
+    const int i = blockIdx.x * kSliceThreads + threadIdx.x;
+    const bool active = i > 0 && i < a.n_grav;                   // the star has its own row
     float4 ha = make_float4(0.f, 0.f, 0.f, 0.f), la = ha, hb = ha, lb = ha;
-    Body pa = make_body(0.0, 0.0, 0.0, 0.0), pb = pa;
     if (active) {
         ha = ms.Phi[sa * c + i]; la = ms.Plo[sa * c + i];
         hb = ms.Phi[sb * c + i]; lb = ms.Plo[sb * c + i];
-        pa = ms.P[sa * c + i]; pb = ms.P[sb * c + i];
     }
     const f2 XHa = f2_dup(ha.x), XLa = f2_dup(la.x), YHa = f2_dup(ha.y), YLa = f2_dup(la.y);
     const f2 ZHa = f2_dup(ha.z), ZLa = f2_dup(la.z);
     const f2 XHb = f2_dup(hb.x), XLb = f2_dup(lb.x), YHb = f2_dup(hb.y), YLb = f2_dup(lb.y);
     const f2 ZHb = f2_dup(hb.z), ZLb = f2_dup(lb.z);
     f2 SA[3] = {0, 0, 0}, CA[3] = {0, 0, 0}, SB[3] = {0, 0, 0}, CB[3] = {0, 0, 0};
-    double dA[3] = {0.0, 0.0, 0.0}, dB[3] = {0.0, 0.0, 0.0};
     for (int t0 = r0; t0 < r1; t0 += kSliceTile) {
         const int cnt = min(kSliceTile, r1 - t0);          // a multiple of kPairSpan
         __syncthreads();                                   // the previous tile is consumed
@@ -296,16 +324,6 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, dou
         }
         __syncthreads();
         if (!active) continue;
-        if (i == 0) {
-            // the star: the planetesimals of this tile in FP64
-            const int q1 = min(2 * (t0 + cnt), n_src);
-            for (int q = 2 * t0; q < q1; ++q) {
-                const int j = a.n_exact + q;
-                pair64(pa, ms.P[sa * c + j], dA[0], dA[1], dA[2]);
-                pair64(pb, ms.P[sb * c + j], dB[0], dB[1], dB[2]);
-            }
-            continue;
-        }
         for (int u0 = 0; u0 < cnt; u0 += kPairSpan) {
             f2 ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
 #pragma unroll 4
@@ -319,13 +337,8 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, dou
     }
     if (!active) return;
     double* o = part + (size_t)k * 6 * np + i;
-    if (i == 0) {
-        o[0] = dA[0]; o[np] = dA[1]; o[2 * np] = dA[2];
-        o[3 * np] = dB[0]; o[4 * np] = dB[1]; o[5 * np] = dB[2];
-    } else {
-        o[0] = f2_total(SA[0], CA[0]); o[np] = f2_total(SA[1], CA[1]); o[2 * np] = f2_total(SA[2], CA[2]);
-        o[3 * np] = f2_total(SB[0], CB[0]); o[4 * np] = f2_total(SB[1], CB[1]); o[5 * np] = f2_total(SB[2], CB[2]);
-    }
+    o[0] = f2_total(SA[0], CA[0]); o[np] = f2_total(SA[1], CA[1]); o[2 * np] = f2_total(SA[2], CA[2]);
+    o[3 * np] = f2_total(SB[0], CB[0]); o[4 * np] = f2_total(SB[1], CB[1]); o[5 * np] = f2_total(SB[2], CB[2]);
 }
 
 template <int PASS>
@@ -533,7 +546,7 @@ cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch&
     const int spans = pair_count(a.n_grav - a.n_exact) / kPairSpan;
     const int per = (spans + S - 1) / S * kPairSpan;
     const int np = slice_stride(a.n_grav);
-    const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads, S);
+    const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
     massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
     massive_gather_kernel<PASS><<<(a.n_grav + 127) / 128, 128, 0, st>>>(s, a, ms, S, np, ms.part);
     return cudaGetLastError();
