@@ -139,7 +139,7 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
                                  int precision, cudaStream_t st);
 cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                         const SizeBin* bins, int precision, cudaStream_t st);
-// Source slices of the mixed massive passes for n_grav bodies (about two blocks per SM),
+// Source slices of the mixed massive passes for n_grav bodies (about four blocks per SM),
 // and the doubles of MassiveScratch::part that cover every system of up to cap bodies.
 int massive_slices(int n_grav, int n_exact);
 long long massive_part_words(int cap);

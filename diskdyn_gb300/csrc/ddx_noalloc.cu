@@ -32,7 +32,7 @@ constexpr size_t kOffR = kOffA + align256(sizeof(double) * 12 * kCap);
 constexpr size_t kOffBins = kOffR + align256(sizeof(double) * 9 * kCap);
 constexpr size_t kOffStatus = kOffBins + align256(sizeof(SizeBin) * DDX_MAX_SIZE_BINS);
 // slice sums of the mixed passes: massive_part_words(kCap) for up to 160 SMs
-constexpr long long kPartWords = 6LL * 256 * (2LL * 160 + (kCap + 255) / 256);
+constexpr long long kPartWords = 6LL * 256 * (4LL * 160 + (kCap + 255) / 256);
 constexpr size_t kOffPart = kOffStatus + 256;
 constexpr size_t kBytes = kOffPart + align256(sizeof(double) * kPartWords);
 

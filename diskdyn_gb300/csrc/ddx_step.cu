@@ -242,6 +242,8 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
 // update.
 constexpr int kSliceThreads = 256;
 constexpr int kSliceTile = 256;       // pair records per stage staged at once (16 KiB)
+constexpr int kSliceBlocksPerSM = 4;  // slices are chosen to give about this many blocks per SM
+constexpr int kMaxSlices = 64;
 
 __device__ __forceinline__ void pair_f2(const BodyPair& r, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH, f2 ZL, f2& px,
                                         f2& py, f2& pz) {
@@ -548,7 +550,8 @@ cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch&
     const int np = slice_stride(a.n_grav);
     const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
     massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
-    massive_gather_kernel<PASS><<<(a.n_grav + 127) / 128, 128, 0, st>>>(s, a, ms, S, np, ms.part);
+    // one warp per block: the gather's FP64 work spreads over as many SMs as there are warps
+    massive_gather_kernel<PASS><<<(a.n_grav + 31) / 32, 32, 0, st>>>(s, a, ms, S, np, ms.part);
     return cudaGetLastError();
 }
 }  // namespace
@@ -556,8 +559,8 @@ cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch&
 int massive_slices(int n_grav, int n_exact) {
     const int groups = (n_grav + kSliceThreads - 1) / kSliceThreads;
     const int spans = pair_count(n_grav - n_exact) / kPairSpan;
-    int S = (2 * sm_count() + groups - 1) / groups;
-    if (S > 32) S = 32;
+    int S = (kSliceBlocksPerSM * sm_count() + groups - 1) / groups;
+    if (S > kMaxSlices) S = kMaxSlices;
     if (S > spans) S = spans;
     return S < 1 ? 1 : S;
 }
@@ -566,7 +569,7 @@ int massive_slices(int n_grav, int n_exact) {
 // the bound at the capacity covers every smaller system.
 long long massive_part_words(int cap) {
     const long long groups = (cap + kSliceThreads - 1) / kSliceThreads;
-    return 6LL * kSliceThreads * (2LL * sm_count() + groups);
+    return 6LL * kSliceThreads * ((long long)kSliceBlocksPerSM * sm_count() + groups);
 }
 
 cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,

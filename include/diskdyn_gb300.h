@@ -145,7 +145,7 @@ int ddx_evolve(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double 
  * Some callers cannot call cudaMalloc, for example a host inside a framework whose pool
  * allocator owns all device memory, or a loop that must keep a fixed device footprint.
  * This entry point needs no context.  Its scratch is one file-scope __device__ array of
- * fixed size (about 8.5 MiB), which every GPU that loads the library holds until the
+ * fixed size (about 12 MiB), which every GPU that loads the library holds until the
  * process exits.  It takes at most DDX_NOALLOC_MAX_GRAV massive bodies and
  * DDX_MAX_SIZE_BINS size bins and answers DDX_ERR_RANGE beyond that.  beta, betasw and q
  * are device pointers with n_grid entries; everything else is as for ddx_step.
