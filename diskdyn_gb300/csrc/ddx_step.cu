@@ -237,9 +237,9 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
 // of kPairSpan records with a Kahan sum across spans (the dust kernel's scheme).  A
 // target's own slot gives RR = 0 and is masked.  The star (target 0) takes the
 // planetesimals' pulls in FP64, in an extra row of blocks that spread each slice over a
-// whole block (a fixed-order tree sum).  massive_gather_kernel then adds the slices in slice order
-// (deterministic), adds the FP64 pulls of bodies 0..n_exact-1 and applies the pass's
-// update.
+// whole block (a fixed-order tree sum).  massive_gather_kernel then adds the slices (one
+// warp per target, a fixed lane order: deterministic), adds the FP64 pulls of bodies
+// 0..n_exact-1 and applies the pass's update.
 constexpr int kSliceThreads = 256;
 constexpr int kSliceTile = 256;       // pair records per stage staged at once (16 KiB)
 constexpr int kSliceBlocksPerSM = 4;  // slices are chosen to give about this many blocks per SM
@@ -343,17 +343,23 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, dou
     o[3 * np] = f2_total(SB[0], CB[0]); o[4 * np] = f2_total(SB[1], CB[1]); o[5 * np] = f2_total(SB[2], CB[2]);
 }
 
+// One warp per target: the lanes take the slices (lane, lane + 32, ...), a fixed butterfly
+// adds the lanes (the same order on every run), lane 0 finishes the target.
 template <int PASS>
 __global__ void massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int slices, int np,
                                       const double* __restrict__ part) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n_grav) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= a.n_grav) return;   // warp-uniform
     const int c = ms.cap;
     const int sa = PASS == 1 ? 0 : 2, sb = sa + 1;
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int k = 0; k < slices; ++k)
+    for (int k = lane; k < slices; k += 32)
 #pragma unroll
         for (int q = 0; q < 6; ++q) acc[q] += part[((size_t)k * 6 + q) * np + i];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q] = warp_sum(acc[q]);
+    if (lane != 0) return;
     const Body pa = ms.P[sa * c + i], pb = ms.P[sb * c + i];
     for (int j = 0; j < a.n_exact && j < a.n_grav; ++j) {
         if (j == i) continue;
@@ -550,8 +556,7 @@ cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch&
     const int np = slice_stride(a.n_grav);
     const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
     massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
-    // one warp per block: the gather's FP64 work spreads over as many SMs as there are warps
-    massive_gather_kernel<PASS><<<(a.n_grav + 31) / 32, 32, 0, st>>>(s, a, ms, S, np, ms.part);
+    massive_gather_kernel<PASS><<<(a.n_grav * 32 + 127) / 128, 128, 0, st>>>(s, a, ms, S, np, ms.part);
     return cudaGetLastError();
 }
 }  // namespace
