@@ -237,9 +237,9 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
 // of kPairSpan records with a Kahan sum across spans (the dust kernel's scheme).  A
 // target's own slot gives RR = 0 and is masked.  The star (target 0) takes the
 // planetesimals' pulls in FP64, in an extra row of blocks that spread each slice over a
-// whole block (a fixed-order tree sum).  massive_gather_kernel then adds the slices (one
-// warp per target, a fixed lane order: deterministic), adds the FP64 pulls of bodies
-// 0..n_exact-1 and applies the pass's update.
+// whole block (a fixed-order tree sum).  massive_gather_kernel then adds the slices (a
+// fixed lane order: deterministic), adds the FP64 pulls of bodies 0..n_exact-1 and applies
+// the pass's update.
 constexpr int kSliceThreads = 256;
 constexpr int kSliceTile = 256;       // pair records per stage staged at once (16 KiB)
 constexpr int kSliceBlocksPerSM = 4;  // slices are chosen to give about this many blocks per SM
@@ -343,23 +343,43 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, dou
     o[3 * np] = f2_total(SB[0], CB[0]); o[4 * np] = f2_total(SB[1], CB[1]); o[5 * np] = f2_total(SB[2], CB[2]);
 }
 
-// One warp per target: the lanes take the slices (lane, lane + 32, ...), a fixed butterfly
-// adds the lanes (the same order on every run), lane 0 finishes the target.
+// 32 targets per block of 8 warps.  Each warp adds the slices of 4 targets (the lanes take
+// slices lane, lane + 32, ..., a fixed butterfly adds the lanes: the same order on every
+// run); then warp 0 finishes the 32 targets, one per lane, so the FP64 update runs on full
+// warps.
+constexpr int kGatherTargets = 32;
+constexpr int kGatherThreads = 256;
+
 template <int PASS>
-__global__ void massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int slices, int np,
-                                      const double* __restrict__ part) {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= a.n_grav) return;   // warp-uniform
+__global__ void __launch_bounds__(kGatherThreads)
+massive_gather_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int slices, int np,
+                      const double* __restrict__ part) {
+    __shared__ double sums[kGatherTargets][6];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = blockIdx.x * kGatherTargets;
+    constexpr int per_warp = kGatherTargets / (kGatherThreads / 32);
+    for (int t = warp * per_warp; t < (warp + 1) * per_warp; ++t) {
+        const int it = i0 + t;
+        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (it < a.n_grav)
+            for (int k = lane; k < slices; k += 32)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) acc[q] += part[((size_t)k * 6 + q) * np + it];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const double v = warp_sum(acc[q]);
+            if (lane == 0) sums[t][q] = v;
+        }
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    const int i = i0 + lane;
+    if (i >= a.n_grav) return;
     const int c = ms.cap;
     const int sa = PASS == 1 ? 0 : 2, sb = sa + 1;
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int k = lane; k < slices; k += 32)
+    double acc[6];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) acc[q] += part[((size_t)k * 6 + q) * np + i];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) acc[q] = warp_sum(acc[q]);
-    if (lane != 0) return;
+    for (int q = 0; q < 6; ++q) acc[q] = sums[lane][q];
     const Body pa = ms.P[sa * c + i], pb = ms.P[sb * c + i];
     for (int j = 0; j < a.n_exact && j < a.n_grav; ++j) {
         if (j == i) continue;
@@ -556,7 +576,8 @@ cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch&
     const int np = slice_stride(a.n_grav);
     const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
     massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
-    massive_gather_kernel<PASS><<<(a.n_grav * 32 + 127) / 128, 128, 0, st>>>(s, a, ms, S, np, ms.part);
+    massive_gather_kernel<PASS><<<(a.n_grav + kGatherTargets - 1) / kGatherTargets, kGatherThreads, 0, st>>>(
+        s, a, ms, S, np, ms.part);
     return cudaGetLastError();
 }
 }  // namespace
