@@ -570,12 +570,14 @@ bool sliced_fits(const StepArgs& a, const MassiveScratch& ms) {
 
 template <int PASS>
 cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch& ms, cudaStream_t st) {
-    const int S = massive_slices(a.n_grav, a.n_exact);
     const int spans = pair_count(a.n_grav - a.n_exact) / kPairSpan;
-    const int per = (spans + S - 1) / S * kPairSpan;
+    const int S = spans > 0 ? massive_slices(a.n_grav, a.n_exact) : 0;    // no planetesimals: no slices
     const int np = slice_stride(a.n_grav);
-    const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
-    massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
+    if (S > 0) {
+        const int per = (spans + S - 1) / S * kPairSpan;
+        const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
+        massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
+    }
     massive_gather_kernel<PASS><<<(a.n_grav + kGatherTargets - 1) / kGatherTargets, kGatherThreads, 0, st>>>(
         s, a, ms, S, np, ms.part);
     return cudaGetLastError();
