@@ -36,6 +36,8 @@ struct ddx_ctx {
     CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
     AdjointScratch* adjoint = nullptr;          // trajectory checkpoints of the last adjoint forward
     DetStepScratch* detstep = nullptr;          // body scan of ddx_det_step
+    float* img32 = nullptr;                     // FP32 interleaved sums of the mixed images
+    size_t img32_words = 0;
     // ddx_step_host: copy streams (host to device, device to host) and their events
     cudaStream_t s_in = nullptr, s_out = nullptr;
     cudaEvent_t ev_in = nullptr, ev_comp = nullptr, ev_out = nullptr;
@@ -267,7 +269,7 @@ int ddx_destroy(ddx_ctx* c) {
     free_massive(c->ms);
     free_optics(c);
     cudaFree(c->bins); cudaFree(c->size_d); cudaFree(c->vc); cudaFree(c->od_dev);
-    cudaFree(c->sed_partial); cudaFree(c->counters); cudaFree(c->status);
+    cudaFree(c->sed_partial); cudaFree(c->counters); cudaFree(c->status); cudaFree(c->img32);
     collide_free(c->collide);
     adjoint_free(c->adjoint);
     det_step_free(c->detstep);
@@ -584,9 +586,21 @@ int ddx_image(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_
         il.wj[k] = wj[k];
     }
     cudaSetDevice(c->device);
-    if (precision == DDX_PREC_MIXED)
-        return cuda_status(launch_image_mixed(*s, n_grav, n_dust, *view, c->od, il, c->vc, c->photo, Fd,
+    if (precision == DDX_PREC_MIXED) {
+        const size_t need = (size_t)view->xsize * view->ysize * image_k4(n_img);
+        if (need > c->img32_words) {
+            cudaFree(c->img32);
+            c->img32 = nullptr;
+            c->img32_words = 0;
+            if (dalloc(&c->img32, need) != cudaSuccess) {
+                cudaGetLastError();
+                return DDX_ERR_NOMEM;
+            }
+            c->img32_words = need;
+        }
+        return cuda_status(launch_image_mixed(*s, n_grav, n_dust, *view, c->od, il, c->vc, c->photo, Fd, c->img32,
                                               c->counters, (cudaStream_t)stream));
+    }
     return cuda_status(launch_image(*s, n_grav, n_dust, *view, c->od, il, c->vc, Fd, c->counters,
                                     (cudaStream_t)stream));
 }

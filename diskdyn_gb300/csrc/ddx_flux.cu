@@ -602,10 +602,16 @@ __global__ void photo_prepare_kernel(OpticsDev o, const ViewConst* __restrict__ 
     }
 }
 
-// Images, mixed precision: one thread per tracer, every image wavelength in one pass.
+// Images, mixed precision: one thread per tracer, every image wavelength in one pass.  The
+// sums go to an FP32 buffer interleaved by wavelength, Fi[pixel][K4] (K4 = n_img rounded up
+// to 4), in the wavelengths' scaled domain (2^esh), as 16-byte vector atomics: one request
+// adds four wavelengths of a tracer, a quarter of the requests of one FP64 atomic per
+// wavelength, and FP32 atomics do not issue through the FP64 pipe.
+// image_convert_kernel then writes the FP64 x-major images.
 __global__ void __launch_bounds__(256)
 image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ vcp, View32 v32, OpticsDev o,
-                   ImageList il, PhotoConst pc, double* __restrict__ Fd, unsigned long long* __restrict__ counters) {
+                   ImageList il, PhotoConst pc, float* __restrict__ Fi, int K4,
+                   unsigned long long* __restrict__ counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_dust) return;
     const int t = n_grav + i;
@@ -634,13 +640,35 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
     }
     Tracer32 tr;
     tracer32_photometry(R, scatter_cos32(y1, zf, R, R * R, v32), id, d2f_trunc(s.N[t]), v32, o, tr);
-    const size_t npix = (size_t)v32.xsize * v32.ysize;
     const size_t pix = (size_t)v32.ysize * xim + yim;
     const float2* lq2 = o.lQp32p + ((size_t)tr.id * (o.n_theta - 1) + tr.cm) * o.n_wav;
     const float2* A = pc.A + (size_t)tr.id * pc.n_lam;
-    for (int k = 0; k < il.n; ++k) {
-        const float F = flux32(tr, lq2, A, k, il.wj[k], pc.C2[k]);
-        if (F != 0.0f) atomicAdd(&Fd[k * npix + pix], f2d_scaled(F, -pc.esh[k]));
+    float* row = Fi + pix * K4;
+    for (int g = 0; g < il.n; g += 4) {
+        float f[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = g + u;
+            f[u] = k < il.n ? flux32(tr, lq2, A, k, il.wj[k], pc.C2[k]) : 0.0f;
+        }
+        if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f || f[3] != 0.0f)
+            atomicAdd(reinterpret_cast<float4*>(row + g), make_float4(f[0], f[1], f[2], f[3]));
+    }
+}
+
+// One thread per pixel: the interleaved FP32 sums to the FP64 x-major images,
+// Fd[k][pixel] = Fi[pixel][k] 2^-esh[k] (an exact power-of-two scaling).
+__global__ void image_convert_kernel(const float* __restrict__ Fi, int K4, int n_img, size_t npix,
+                                     const int* __restrict__ esh, double* __restrict__ Fd) {
+    const size_t pix = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    const float4* row = reinterpret_cast<const float4*>(Fi + pix * K4);
+    for (int g = 0; g < n_img; g += 4) {
+        const float4 v = row[g >> 2];
+        const float f[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (g + u < n_img) Fd[(size_t)(g + u) * npix + pix] = f2d_scaled(f[u], -esh[g + u]);
     }
 }
 
@@ -748,17 +776,19 @@ cudaError_t launch_photo_prepare(const OpticsDev& o, const ViewConst* vc, const 
 
 cudaError_t launch_image_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
                                const OpticsDev& o, const ImageList& il, ViewConst* vc, PhotoConst pc,
-                               double* Fd, unsigned long long* counters, cudaStream_t st) {
+                               double* Fd, float* Fi, unsigned long long* counters, cudaStream_t st) {
     view_setup_kernel<<<1, 32, 0, st>>>(vc, view, o.n_theta);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     pc.n_lam = il.n;
     if ((e = launch_photo_prepare(o, vc, &il, pc, st)) != cudaSuccess) return e;
     const size_t npix = (size_t)view.xsize * view.ysize;
-    if ((e = cudaMemsetAsync(Fd, 0, sizeof(double) * npix * il.n, st)) != cudaSuccess) return e;
-    if (n_dust <= 0) return cudaSuccess;
-    image_mixed_kernel<<<(n_dust + 255) / 256, 256, 0, st>>>(s, n_grav, n_dust, vc, make_view32(view, o), o, il,
-                                                             pc, Fd, counters);
+    const int K4 = image_k4(il.n);
+    if ((e = cudaMemsetAsync(Fi, 0, sizeof(float) * npix * K4, st)) != cudaSuccess) return e;
+    if (n_dust > 0)
+        image_mixed_kernel<<<(n_dust + 255) / 256, 256, 0, st>>>(s, n_grav, n_dust, vc, make_view32(view, o), o, il,
+                                                                 pc, Fi, K4, counters);
+    image_convert_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(Fi, K4, il.n, npix, pc.esh, Fd);
     return cudaGetLastError();
 }
 

@@ -45,9 +45,11 @@ struct PhotoConst {
 
 cudaError_t launch_photo_prepare(const OpticsDev& o, const ViewConst* vc, const ImageList* il,
                                  PhotoConst pc, cudaStream_t st);
+// Mixed images: Fi is an FP32 scratch of npix * image_k4(n_img) floats (256-byte aligned).
+inline int image_k4(int n_img) { return (n_img + 3) / 4 * 4; }
 cudaError_t launch_image_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
                                const OpticsDev& o, const ImageList& il, ViewConst* vc, PhotoConst pc,
-                               double* Fd, unsigned long long* counters, cudaStream_t st);
+                               double* Fd, float* Fi, unsigned long long* counters, cudaStream_t st);
 cudaError_t launch_sed_mixed(const ddx_state& s, int n_grav, int n_dust, const ddx_view& view,
                              const OpticsDev& o, ViewConst* vc, PhotoConst pc, double* partial, int mode,
                              double* Fsed, cudaStream_t st);
