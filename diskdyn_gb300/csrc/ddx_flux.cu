@@ -545,21 +545,25 @@ __device__ __forceinline__ void tracer32_photometry(float R, float cossc, int id
     t.id = id;
 }
 
-// Scaled flux of tracer t at wavelength slot j (table wavelength J).  lq2: the tracer's
-// row of base-2 log phase-function pairs (bin, cos bracket cm): lq2[J] = (log2 P(cm),
-// log2 P(cm+1)); A: its bin's row of (At, As).  One 8-byte load each.
-__device__ __forceinline__ float flux32(const Tracer32& t, const float2* lq2, const float2* A, int j, int J,
-                                        float C2j) {
+// Scaled flux of tracer t at one wavelength: l = (log2 P(cm), log2 P(cm+1)) from the
+// tracer's row of base-2 log phase-function pairs (bin, cos bracket cm), a = (At, As) of its
+// bin at the wavelength, C2j = h c / (lambda k).
+__device__ __forceinline__ float flux32_row(const Tracer32& t, float2 l, float2 a, float C2j) {
     const float x = C2j * t.rT;
     const float e = expf(x);
     // exp(x) - 1 loses digits for small x: Taylor series there (error < x^8/8! < 1e-7 rel)
     const float ser = x * (1.0f + x * (0.5f + x * (1.0f / 6 + x * (1.0f / 24 + x * (1.0f / 120 + x * (1.0f / 720 + x * (1.0f / 5040)))))));
     const float em1 = x < 0.5f ? ser : e - 1.0f;
     const float pl = rcp_approx(em1);     // 0 once the exponential overflows
-    const float2 l = lq2[J];
     const float P = ex2_approx(l.x + (l.y - l.x) * t.wt);
-    const float2 a = A[j];
     return t.n * fmaf(a.x, pl, a.y * P * t.invR2);
+}
+
+// The same at wavelength slot j (table wavelength J) from the rows: lq2[J] and A[j], one
+// 8-byte load each.
+__device__ __forceinline__ float flux32(const Tracer32& t, const float2* lq2, const float2* A, int j, int J,
+                                        float C2j) {
+    return flux32_row(t, lq2[J], A[j], C2j);
 }
 
 }  // namespace
@@ -644,15 +648,25 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
     const float2* lq2 = o.lQp32p + ((size_t)tr.id * (o.n_theta - 1) + tr.cm) * o.n_wav;
     const float2* A = pc.A + (size_t)tr.id * pc.n_lam;
     float* row = Fi + pix * K4;
-    for (int g = 0; g < il.n; g += 4) {
-        float f[4];
+    // eight wavelengths at a time, their table loads issued together before the arithmetic
+    for (int g = 0; g < il.n; g += 8) {
+        float2 lv[8], av[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 8; ++u) {
             const int k = g + u;
-            f[u] = k < il.n ? flux32(tr, lq2, A, k, il.wj[k], pc.C2[k]) : 0.0f;
+            lv[u] = k < il.n ? lq2[il.wj[k]] : make_float2(0.f, 0.f);
+            av[u] = k < il.n ? A[k] : make_float2(0.f, 0.f);
         }
-        if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f || f[3] != 0.0f)
-            atomicAdd(reinterpret_cast<float4*>(row + g), make_float4(f[0], f[1], f[2], f[3]));
+        float f[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int k = g + u;
+            f[u] = k < il.n ? flux32_row(tr, lv[u], av[u], pc.C2[k]) : 0.0f;
+        }
+#pragma unroll
+        for (int h = 0; h < 8; h += 4)
+            if (g + h < il.n && (f[h] != 0.0f || f[h + 1] != 0.0f || f[h + 2] != 0.0f || f[h + 3] != 0.0f))
+                atomicAdd(reinterpret_cast<float4*>(row + g + h), make_float4(f[h], f[h + 1], f[h + 2], f[h + 3]));
     }
 }
 
