@@ -12,10 +12,11 @@
 //              own cell and the neighbour on the side of the cell's half it lies in (a
 //              partner closer than h cannot be further, because the cell is 2h wide); on a
 //              clamped axis both neighbours.  It keeps the entries whose cell id is that
-//              cell (hash collisions are filtered), j > i, and applies the distance test;
+//              cell (hash collisions are filtered), j > i, and applies the distance test,
+//              counting the partners and keeping the first kSlots of them;
 //  5. scan   : exclusive scan of the counts gives each tracer its output slot;
-//  6. write  : the same walk writes (i, j) and sorts the tracer's segment by j, so the list
-//              is ordered by (i, j).
+//  6. write  : each tracer writes its kept partners (or walks again, if it has more than
+//              kSlots) as (i, j) and sorts its segment by j, so the list is ordered by (i, j).
 #include "ddx_internal.cuh"
 #include "ddx_sort.cuh"
 
@@ -91,12 +92,15 @@ __global__ void ranges_kernel(const uint32_t* __restrict__ keys, int n, uint32_t
     if (q == n - 1 || keys[q + 1] != k) end[k] = (uint32_t)q + 1;
 }
 
+constexpr uint32_t kSlots = 4;   // partners kept per tracer by the count pass
+
 template <bool WRITE>
 __global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, uint32_t mask, uint32_t sentinel,
                              const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                              const unsigned long long* __restrict__ cellid, const uint32_t* __restrict__ start,
                              const uint32_t* __restrict__ end, uint32_t* __restrict__ count,
-                             const uint32_t* __restrict__ offs, int2* __restrict__ pairs, long long cap) {
+                             int* __restrict__ slots, const uint32_t* __restrict__ offs, int2* __restrict__ pairs,
+                             long long cap) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;   // sorted order: neighbours share buckets
     if (q >= n) return;
     const uint32_t p = vals[q];
@@ -105,6 +109,20 @@ __global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, 
         return;
     }
     const int i = i0 + (int)p;
+    const long long base = WRITE ? (long long)offs[p] : 0;
+    if (WRITE && count[p] <= kSlots) {
+        // the count pass kept this tracer's partners: no second walk
+        const uint32_t cnt = count[p];
+        for (uint32_t k = 0; k < cnt && base + k < cap; ++k) pairs[base + k] = make_int2(i, slots[(size_t)p * kSlots + k]);
+        const long long last = base + cnt < cap ? base + cnt : cap;
+        for (long long a = base + 1; a < last; ++a) {
+            const int2 v = pairs[a];
+            long long b = a - 1;
+            while (b >= base && pairs[b].y > v.y) { pairs[b + 1] = pairs[b]; --b; }
+            pairs[b + 1] = v;
+        }
+        return;
+    }
     const double xi = s.x[i], yi = s.y[i], zi = s.z[i];
     long long cx, cy, cz;
     unpack_cell(cellid[p], cx, cy, cz);
@@ -112,7 +130,6 @@ __global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, 
     octant(xi, inv, cx, lx, hx);
     octant(yi, inv, cy, ly, hy);
     octant(zi, inv, cz, lz, hz);
-    const long long base = WRITE ? (long long)offs[p] : 0;
     uint32_t c = 0;
     for (int dx = lx; dx <= hx; ++dx)
         for (int dy = ly; dy <= hy; ++dy)
@@ -130,6 +147,7 @@ __global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, 
                     const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
                     if (d2 < h2) {
                         if (WRITE && base + c < cap) pairs[base + c] = make_int2(i, j);
+                        if (!WRITE && c < kSlots) slots[(size_t)p * kSlots + c] = j;
                         ++c;
                     }
                 }
@@ -153,6 +171,7 @@ __global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, 
 struct CollideScratch {
     uint32_t *keys = nullptr, *vals = nullptr, *start = nullptr, *end = nullptr, *count = nullptr,
              *offs = nullptr, *temp = nullptr, *total = nullptr;
+    int* slots = nullptr;
     unsigned long long* cellid = nullptr;
     int n_cap = 0;
     uint32_t t_cap = 0;
@@ -161,7 +180,7 @@ struct CollideScratch {
 void collide_free(CollideScratch*& c) {
     if (!c) return;
     cudaFree(c->keys); cudaFree(c->vals); cudaFree(c->start); cudaFree(c->end); cudaFree(c->count);
-    cudaFree(c->offs); cudaFree(c->temp); cudaFree(c->total); cudaFree(c->cellid);
+    cudaFree(c->offs); cudaFree(c->temp); cudaFree(c->total); cudaFree(c->cellid); cudaFree(c->slots);
     delete c;
     c = nullptr;
 }
@@ -183,7 +202,8 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
         const size_t tw = sort_temp_words(ncap) + scan_temp_words(ncap);
         if (cudaMalloc(&nc->keys, 4ull * ncap) || cudaMalloc(&nc->vals, 4ull * ncap) ||
             cudaMalloc(&nc->count, 4ull * ncap) || cudaMalloc(&nc->offs, 4ull * ncap) ||
-            cudaMalloc(&nc->cellid, 8ull * ncap) || cudaMalloc(&nc->start, 4ull * tcap) ||
+            cudaMalloc(&nc->cellid, 8ull * ncap) || cudaMalloc(&nc->slots, 4ull * kSlots * ncap) ||
+            cudaMalloc(&nc->start, 4ull * tcap) ||
             cudaMalloc(&nc->end, 4ull * tcap) || cudaMalloc(&nc->temp, 4ull * tw) ||
             cudaMalloc(&nc->total, 16)) {
             collide_free(nc);
@@ -206,12 +226,12 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
     cudaMemsetAsync(cs->end, 0, 4ull * T, st);
     ranges_kernel<<<blk, thr, 0, st>>>(cs->keys, n, sentinel, cs->start, cs->end);
     pairs_kernel<false><<<blk, thr, 0, st>>>(s, i0, n, h2, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid,
-                                             cs->start, cs->end, cs->count, nullptr, nullptr, 0);
+                                             cs->start, cs->end, cs->count, cs->slots, nullptr, nullptr, 0);
     uint32_t* scan_temp = cs->temp + sort_temp_words(cs->n_cap);
     if (exclusive_scan(cs->count, cs->offs, n, scan_temp, cs->total, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (pairs && cap > 0)
         pairs_kernel<true><<<blk, thr, 0, st>>>(s, i0, n, h2, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid,
-                                                cs->start, cs->end, nullptr, cs->offs, pairs, cap);
+                                                cs->start, cs->end, cs->count, cs->slots, cs->offs, pairs, cap);
     if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
     uint32_t tot = 0;
     if (cudaMemcpyAsync(&tot, cs->total, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return DDX_ERR_CUDA;
