@@ -56,6 +56,33 @@ def test_argument_errors_without_gpu(built_lib):
     assert lib.ddx_sed(None, C.byref(st), 1, 0, None, None, 0, 0, None) == 1
 
 
+def test_argument_errors_of_the_setup_and_run_calls_without_gpu(built_lib):
+    """The set-up, run and host-buffer calls check their arguments before any CUDA call."""
+    from diskdyn_gb300 import abi, formats
+    lib = abi.load()
+    st = abi.State()
+    ph = abi.Phys()
+    vw = abi.View()
+    cad = abi.Cadence(t_write=1.0, t_fits=1.0, t_sed=1.0, t_end=2.0)
+    hs = formats.HostState()
+    t = abi.OpticalTable()
+    g = abi.GridSetup()
+    lum, bsc = C.c_double(), C.c_double()
+    assert lib.ddx_dust_grid(None, 2, None, None, C.byref(t), C.byref(g), C.byref(t), None, None, None,
+                             C.byref(lum), C.byref(bsc), None) == 1
+    assert lib.ddx_setup_device(None, None, 1e-7, 1e-4, None, 1, C.byref(st), 0, None, None) == 1
+    assert lib.ddx_step_host(None, C.byref(hs), C.byref(hs), C.byref(st), 1, 0, 0.1, C.byref(ph), 1, 0, None) == 1
+    assert lib.ddx_run(None, C.byref(st), 1, 0, 0.1, C.byref(ph), 1, 0, C.byref(vw), None, 0, C.byref(cad),
+                       abi.OUTPUT_FN(lambda u, o: 0), None, None) == 1
+    # host-only calls: bad sizes
+    n = C.c_longlong()
+    bad = abi.Cadence(t_write=0.0, t_fits=1.0, t_sed=1.0, t_end=2.0)
+    assert lib.ddx_schedule(C.byref(bad), 0.1, 0, None, None, C.byref(n)) == 1
+    assert lib.ddx_schedule(C.byref(cad), -1.0, 0, None, None, C.byref(n)) == 1
+    assert lib.ddx_stellar_grid(1, None, 2, None, None, 0, None, None, None) == 1
+    assert lib.ddx_param_grid(None, 1e-7, 1e-4) == 1
+
+
 def test_oracle_builds_and_loads():
     import oracle.cpu as oc
     assert oc.lib() is not None
