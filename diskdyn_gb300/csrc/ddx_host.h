@@ -32,9 +32,14 @@ struct SetupPlan {
     long long n_planets = 0, n_mass = 0, n_dust = 0, n_all = 0;
 };
 
+// The gravitating bodies' masses of a plan: none (counts only), the reference's getbod
+// chain in its long double arithmetic (bit-exact on x86-64), or the same chain in double
+// (fast everywhere; long double is software quad precision on Arm).
+enum class Masses { none, reference, fast };
+
 // Builds the plan of a parameter file after ddx_param_grid; beta (n_grid entries) may be
 // null when only the counts are wanted.  Returns a DDX_* status.
-int plan_setup(const ddx_param& p, double dmin, double dmax, const float* beta, bool with_masses, SetupPlan& plan);
+int plan_setup(const ddx_param& p, double dmin, double dmax, const float* beta, Masses masses, SetupPlan& plan);
 
 // The reference's tokeniser (tokenize_spaces with remove_quotes, src/read_in.cu:12-60):
 // splits buf in place into at most `max` tokens at the separators '@', space, CR, LF and

@@ -92,6 +92,13 @@ void getbod(long double& mmax, double& m, double C, double ome) {
     mmax = mmin;
 }
 
+// The same chain in double.
+void getbod_fast(double& mmax, double& m, double C, double ome) {
+    const double mmin = pow(pow(mmax, ome) - ome / C, 1.0 / ome);
+    m = C * (pow(mmax, 1.0 + ome) - pow(mmin, 1.0 + ome)) / (1.0 + ome) / kMSun * kGrav;
+    mmax = mmin;
+}
+
 void orbit_disk(const ddx_disk& d, double M, double m, double beta, Ran3& r, double* o6) {
     double e;
     do {
@@ -139,7 +146,7 @@ bool plan_ok(const ddx_param* p) {
 
 namespace ddx_host {
 
-int plan_setup(const ddx_param& p, double dmin, double dmax, const float* beta, bool with_masses, SetupPlan& plan) {
+int plan_setup(const ddx_param& p, double dmin, double dmax, const float* beta, Masses masses, SetupPlan& plan) {
     if (!plan_ok(&p)) return DDX_ERR_ARG;
     plan = SetupPlan{};
     plan.n_planets = p.n_planets;
@@ -161,13 +168,21 @@ int plan_setup(const ddx_param& p, double dmin, double dmax, const float* beta, 
             s.id = -1;
             s.N = 1.0;
             s.beta = 0.0;
-            if (with_masses) {
-                long double mmax = kind == 0 ? p.disks[j].mmax : p.blobs[j].mmax;
-                const double C = kind == 0 ? p.disks[j].C : p.blobs[j].C;
-                const double eta = kind == 0 ? p.disks[j].eta : p.blobs[j].eta;
+            const double C = kind == 0 ? p.disks[j].C : p.blobs[j].C;
+            const double eta = kind == 0 ? p.disks[j].eta : p.blobs[j].eta;
+            const double mtop = kind == 0 ? p.disks[j].mmax : p.blobs[j].mmax;
+            if (masses == Masses::reference) {
+                long double mmax = mtop;
                 for (long long l = 0; l < Ng; l++) {
                     double m = 0.0;
                     getbod(mmax, m, C, 1.0 - eta);
+                    plan.mass.push_back(m);
+                }
+            } else if (masses == Masses::fast) {
+                double mmax = mtop;
+                for (long long l = 0; l < Ng; l++) {
+                    double m = 0.0;
+                    getbod_fast(mmax, m, C, 1.0 - eta);
                     plan.mass.push_back(m);
                 }
             }
@@ -299,7 +314,7 @@ extern "C" int ddx_param_grid(ddx_param* p, double dmin, double dmax) {
 extern "C" int ddx_setup_count(const ddx_param* p, double dmin, double dmax, ddx_dat_run* run) {
     if (!p || !run) return DDX_ERR_ARG;
     ddx_host::SetupPlan plan;
-    const int r = ddx_host::plan_setup(*p, dmin, dmax, nullptr, false, plan);
+    const int r = ddx_host::plan_setup(*p, dmin, dmax, nullptr, ddx_host::Masses::none, plan);
     if (r) return r;
     run->n_mass = (int)plan.n_mass;
     run->n_dust = (int)plan.n_dust;
@@ -312,7 +327,7 @@ extern "C" int ddx_setup_host(const ddx_param* p, double dmin, double dmax, cons
     if (!p || !beta || !s || !run) return DDX_ERR_ARG;
     if (!s->x || !s->y || !s->z || !s->vx || !s->vy || !s->vz || !s->N || !s->m || !s->id) return DDX_ERR_ARG;
     ddx_host::SetupPlan plan;
-    int r = ddx_host::plan_setup(*p, dmin, dmax, beta, true, plan);
+    int r = ddx_host::plan_setup(*p, dmin, dmax, beta, ddx_host::Masses::reference, plan);
     if (r) return r;
     if (s->cap < plan.n_all) return DDX_ERR_RANGE;
     for (int j = 0; j < p->n_planets; j++) {

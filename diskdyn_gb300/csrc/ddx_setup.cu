@@ -2,9 +2,10 @@
 // thread each, straight into the device state.
 //
 // The host builds the plan (ddx_setup.cpp: the segments of bodies with the same generator
-// inputs, the gravitating masses of the getbod chain, each mass bin's mass, size bin and
-// grains per tracer), so counts, order, masses, bins and grain numbers are those of the
-// reference's set-up.  The orbits follow the reference's draws (genorb_disk, genorb_blob,
+// inputs, the gravitating masses of the getbod chain in double, each mass bin's mass, size
+// bin and grains per tracer), so counts, order, bins and grain numbers are those of the
+// reference's set-up and the gravitating masses agree with its long double chain to
+// rounding.  The orbits follow the reference's draws (genorb_disk, genorb_blob,
 // src/functions.cu:157-232) and coe2rv (:6-46) in FP64, but the uniform numbers come from
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11) with the key = the seed and the counter = (draw, body index, a constant): every
@@ -165,7 +166,7 @@ size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 int setup_device_run(const ddx_param* p, double dmin, double dmax, const float* beta, unsigned long long seed,
                      const ddx_state& s, long long cap, ddx_dat_run* run, cudaStream_t st) {
     ddx_host::SetupPlan plan;
-    const int r = ddx_host::plan_setup(*p, dmin, dmax, beta, true, plan);
+    const int r = ddx_host::plan_setup(*p, dmin, dmax, beta, ddx_host::Masses::fast, plan);
     if (r) return r;
     if (cap < plan.n_all || plan.n_all > 0x7fffffffLL) return DDX_ERR_RANGE;
 
