@@ -92,11 +92,21 @@ void getbod(long double& mmax, double& m, double C, double ome) {
     mmax = mmin;
 }
 
-// The same chain in double.
+// The same chain in double.  Consecutive masses are close, so the difference of the two
+// powers is formed without cancellation: with r = mmin / mmax,
+//   ln r = log1p(-(ome / C) mmax^-ome) / ome,
+//   mmax^(1+ome) - mmin^(1+ome) = -mmax^(1+ome) expm1((1 + ome) ln r).
+// ome = 0 keeps the direct form (the chain is degenerate there, as in the reference).
 void getbod_fast(double& mmax, double& m, double C, double ome) {
-    const double mmin = pow(pow(mmax, ome) - ome / C, 1.0 / ome);
-    m = C * (pow(mmax, 1.0 + ome) - pow(mmin, 1.0 + ome)) / (1.0 + ome) / kMSun * kGrav;
-    mmax = mmin;
+    if (ome == 0.0) {
+        const double mmin = pow(pow(mmax, ome) - ome / C, 1.0 / ome);
+        m = C * (pow(mmax, 1.0 + ome) - pow(mmin, 1.0 + ome)) / (1.0 + ome) / kMSun * kGrav;
+        mmax = mmin;
+        return;
+    }
+    const double lr = log1p(-(ome / C) * pow(mmax, -ome)) / ome;
+    m = C * (-pow(mmax, 1.0 + ome) * expm1((1.0 + ome) * lr)) / (1.0 + ome) / kMSun * kGrav;
+    mmax = mmax * exp(lr);
 }
 
 void orbit_disk(const ddx_disk& d, double M, double m, double beta, Ran3& r, double* o6) {
