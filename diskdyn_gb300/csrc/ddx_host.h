@@ -33,8 +33,9 @@ struct SetupPlan {
 };
 
 // The gravitating bodies' masses of a plan: none (counts only), the reference's getbod
-// chain in its long double arithmetic (bit-exact on x86-64), or the same chain in double
-// (fast everywhere; long double is software quad precision on Arm).
+// chain in its arithmetic (bit-exact on x86-64), or the same chain in double formed
+// without cancellation (accurate to rounding, and fast everywhere; long double is software
+// quad precision on Arm).
 enum class Masses { none, reference, fast };
 
 // Builds the plan of a parameter file after ddx_param_grid; beta (n_grid entries) may be

@@ -47,9 +47,9 @@ int ddx_setup_host(const ddx_param *p, double dmin, double dmax, const float *be
 /* The same system drawn on the GPU into the device state s (n_all = run->n_all entries,
  * cap >= n_all): the same counts, order, grain masses, size bins and grain numbers as
  * ddx_setup_host, the gravitating masses from the same getbod chain evaluated in double
- * without cancellation (within 1e-7 of the reference's long double chain, which loses about
- * eight digits to the difference of two nearly equal powers; long double is also software
- * quad precision on Arm), and orbits from the
+ * without cancellation (to 1e-16; the reference's chain carries the rounding of each next
+ * limit into a difference of two nearly equal powers, about 1e-6 on typical files), and
+ * orbits from the
  * same distributions, drawn with Philox4x32-10 (Salmon et al., SC'11) keyed by `seed`, one
  * counter stream per body, so the result does not depend on the launch and is reproducible
  * for a seed, but it is not ran3's sequence.  The rejection draws (eccentricities >= 1,
