@@ -225,7 +225,7 @@ def run_ours(args, world, rank, local):
     collide = {"h_AU": h_coll, "pairs": eng.last_pair_count, "ms_per_call": statistics.median(coll_ms),
                "bodies_per_s": nd / (statistics.median(coll_ms) / 1e3),
                "what": "one ddx_collide call over the grains (output buffer sized from the previous call): "
-                       "hash keys on 2h cells, radix sort, cell ranges, octant count, scan, write; host wall "
+                       "hash keys and bucket ranks on 2h cells, bucket scan, scatter to bucket order, octant count, scan, write; host wall "
                        "time, including the count read-back"}
     step_plus_coll_ms = t_total * 1e3 / args.steps + collide["ms_per_call"]
     collide["body_steps_per_s_with_collisions"] = (ng + alive1) / (step_plus_coll_ms / 1e3)

@@ -3,184 +3,302 @@
 // (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2, every operation rounded on its own (no FMA
 // contraction), so the result is identical to a CPU brute force with the same expression.
 //
-//  1. keys   : cell = floor(x / cs) per axis with cs = 2h (1 + 1e-9), clamped to
-//              +-(2^20 - 2) (clamping only merges far cells); the 63-bit cell id is hashed
-//              (the 64-bit finaliser of MurmurHash3) into T = 2^k >= 2n buckets;
-//  2. sort   : stable radix sort of (bucket, local index) (ddx_sort.cu);
-//  3. ranges : first/last sorted position of every bucket;
-//  4. count  : every tracer visits the buckets of the 8 cells of its octant: per axis its
-//              own cell and the neighbour on the side of the cell's half it lies in (a
-//              partner closer than h cannot be further, because the cell is 2h wide); on a
-//              clamped axis both neighbours.  It keeps the entries whose cell id is that
-//              cell (hash collisions are filtered), j > i, and applies the distance test,
-//              counting the partners and keeping the first kSlots of them;
-//  5. scan   : exclusive scan of the counts gives each tracer its output slot;
-//  6. write  : each tracer writes its kept partners (or walks again, if it has more than
-//              kSlots) as (i, j) and sorts its segment by j, so the list is ordered by (i, j).
+//  1. keys    : cell = floor(x / cs) per axis with cs = 2h (1 + 1e-9), clamped to
+//               +-(2^19 - 2) (clamping only merges far cells), and the half of the cell the
+//               tracer lies in; the cell is hashed (the 32-bit finaliser of MurmurHash3 over
+//               a linear form of the three 20-bit coordinates) into T = 2^k >= 2n buckets,
+//               and an atomic increment of the bucket's size gives the tracer its rank in it;
+//  2. starts  : an exclusive scan of the T bucket sizes gives every bucket its first slot;
+//               the bucket table holds 16-byte entries {start, size, cell id of the first
+//               tracer}, so one load answers most lookups;
+//  3. scatter : every live tracer writes {x, y, z, cell id and halves} and its index to slot
+//               start + rank (the tracer of rank 0 also its cell id to the bucket's entry).
+//               Steps 1-3 are a radix sort on the whole bucket id in one pass (a counting
+//               sort): the bucket sizes are its histogram, the scan its offsets;
+//  4. count   : every tracer, in bucket order, visits the buckets of the 8 cells of its
+//               octant: per axis its own cell and the neighbour on the side of the cell's
+//               half it lies in (a partner closer than h cannot be further, because the cell
+//               is 2h wide); on a clamped axis both neighbours.  It keeps the entries whose
+//               cell id is that cell (hash collisions are filtered), j > i, and applies the
+//               distance test, counting the partners and keeping the first kSlots of them.
+//               Most neighbour cells are empty, and their bucket is then empty or holds one
+//               tracer of another cell: the 8 bucket entries, loaded together, settle those
+//               without touching the tracers, and only the rest are walked.  A test in FP32
+//               with a proven margin rejects the far candidates first; the FP64 test decides
+//               the rest (FP64 runs at 1/64 of the FP32 rate here, and a warp pays for it
+//               whenever any of its lanes tests);
+//  5. scan    : exclusive scan of the counts gives each tracer its output slot;
+//  6. write   : each tracer writes its partners (the kept ones, or by walking again if it
+//               has more than kSlots) ordered by j, so the list is ordered by (i, j).
+// The order of the tracers inside a bucket depends on the atomics, but nothing written does:
+// every tracer's partners are sorted by j, and a segment cut by the buffer's end keeps the
+// smallest j, so the output is the first cap pairs of the ordered list.
 #include "ddx_internal.cuh"
-#include "ddx_sort.cuh"
+#include "ddx_scan.cuh"
 
 namespace ddx {
 namespace {
 
-constexpr long long kCellLim = (1LL << 20) - 2;
-constexpr unsigned long long kNoCell = ~0ull;
+// Cell ids: offset coordinates u = c + 2^19 in 20-bit fields (x at bit 40, y at 20, z at 0);
+// bits 60-62 hold the halves the tracer lies in (z, y, x), which are not part of the cell.
+constexpr long long kCellLim = (1LL << 19) - 2;
+constexpr uint32_t kOff = 1u << 19;
+constexpr unsigned long long kIdMask = (1ull << 60) - 1;
 
-__host__ __device__ __forceinline__ unsigned long long pack_cell(long long cx, long long cy, long long cz) {
-    const unsigned long long o = 1ull << 20;
-    return ((unsigned long long)(cx + o) << 42) | ((unsigned long long)(cy + o) << 21) |
-           (unsigned long long)(cz + o);
+// A tracer in bucket order: its position (copied bit for bit) and its cell id with halves,
+// one 32-byte sector.
+struct alignas(32) CellRec {
+    double x, y, z;
+    unsigned long long cell;
+};
+
+__device__ __forceinline__ unsigned long long pack_u(uint32_t ux, uint32_t uy, uint32_t uz) {
+    return ((unsigned long long)ux << 40) | ((unsigned long long)uy << 20) | (unsigned long long)uz;
 }
-__device__ __forceinline__ void unpack_cell(unsigned long long id, long long& cx, long long& cy, long long& cz) {
-    const long long o = 1LL << 20;
-    cx = (long long)((id >> 42) & 0x1FFFFF) - o;
-    cy = (long long)((id >> 21) & 0x1FFFFF) - o;
-    cz = (long long)(id & 0x1FFFFF) - o;
+// Bucket of a cell: fmix32 of lin = ux * kHx + uy * kHy + uz * kHz (mod 2^32).  Cells whose
+// forms coincide share a bucket, which the cell-id test separates.  lin is linear, so a
+// neighbour's form is the cell's plus the offsets' (neighbour_lin).
+constexpr uint32_t kHx = 0x9E3779B1u, kHy = 0x85EBCA77u, kHz = 0xC2B2AE3Du;
+__device__ __forceinline__ uint32_t cell_lin(uint32_t ux, uint32_t uy, uint32_t uz) {
+    return ux * kHx + uy * kHy + uz * kHz;
 }
-__device__ __forceinline__ uint32_t bucket_of(unsigned long long k, uint32_t mask) {
-    k ^= k >> 33;
-    k *= 0xff51afd7ed558ccdull;
-    k ^= k >> 33;
-    k *= 0xc4ceb9fe1a85ec53ull;
-    k ^= k >> 33;
-    return (uint32_t)k & mask;
+__device__ __forceinline__ uint32_t neighbour_lin(uint32_t lin, int dx, int dy, int dz) {
+    return lin + (uint32_t)dx * kHx + (uint32_t)dy * kHy + (uint32_t)dz * kHz;
 }
-__device__ __forceinline__ long long cell_coord(double x, double inv) {
-    double c = floor(x * inv);
-    c = fmin(fmax(c, (double)-kCellLim), (double)kCellLim);
-    return (long long)c;
+__device__ __forceinline__ uint32_t bucket_of(uint32_t h, uint32_t mask) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h & mask;
 }
-// Neighbour offsets [lo, hi] along one axis: the cell itself and the neighbour on the side
-// of the half the tracer lies in; both neighbours on a clamped axis.  With cells 2h (1 +
-// 1e-9) wide, the rounding of x / cs (below 1e-9 of a cell for |cell| < 2^20) cannot put a
-// partner within h outside these cells.
-__device__ __forceinline__ void octant(double x, double inv, long long c, int& lo, int& hi) {
-    if (c <= -kCellLim || c >= kCellLim) {
+// Packed id of the neighbour (dx, dy, dz) of a cell: the fields are in [2, 2^20 - 2], so
+// adding +-1 to each never carries into the next.
+__device__ __forceinline__ unsigned long long neighbour_id(unsigned long long id, int dx, int dy, int dz) {
+    return id + (unsigned long long)((long long)dx << 40) + (unsigned long long)((long long)dy << 20) +
+           (unsigned long long)(long long)dz;
+}
+// Cell along one axis and the half the tracer lies in.  k = floor(x * 2/cs) is the half-cell
+// index: x * (2/cs) is exactly twice the rounded x / cs (a power-of-two scale), so k >> 1 is
+// floor(x / cs) and the low bit of k is the upper half.  The walk takes the cell itself and
+// the neighbour on that side, or both neighbours on a clamped axis.  With cells 2h (1 + 1e-9)
+// wide, the rounding of x / cs (below 1e-9 of a cell for |cell| < 2^19) cannot put a partner
+// within h outside these cells.  The conversion saturates for huge or infinite x (clamped)
+// and gives 0 for NaN, whose distance tests fail.
+__device__ __forceinline__ uint32_t axis_cell(double x, double inv2, uint32_t& upper) {
+    const long long k = __double2ll_rd(x * inv2);
+    long long c = k >> 1;
+    upper = (uint32_t)(k & 1);
+    if (c < -kCellLim) c = -kCellLim;
+    if (c > kCellLim) c = kCellLim;
+    return (uint32_t)(c + kOff);
+}
+// Neighbour offsets [lo, hi] along an axis from the cell's field u and the half bit.
+__device__ __forceinline__ void axis_walk(uint32_t u, uint32_t upper, int& lo, int& hi) {
+    if (u <= kOff - kCellLim || u >= kOff + kCellLim) {
         lo = -1;
         hi = 1;
-        return;
+    } else {
+        lo = upper ? 0 : -1;
+        hi = upper ? 1 : 0;
     }
-    const double f = x * inv - (double)c;
-    lo = f < 0.5 ? -1 : 0;
-    hi = f < 0.5 ? 0 : 1;
+}
+// x rounded toward zero to float with integer operations only (no FP64 instruction): ±0
+// below the float normals, ±inf above the float range or for inf and NaN.  The error is
+// below 2^-23 |x| in the normal range.
+__device__ __forceinline__ float f32_trunc(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FF) - 1023;
+    if (e < -126) return __uint_as_float(sign);
+    if (e > 127) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu));
 }
 
-__global__ void keys_kernel(ddx_state s, int i0, int n, double inv, uint32_t mask, uint32_t sentinel,
-                            uint32_t* keys, uint32_t* vals, unsigned long long* cellid) {
+__global__ void keys_kernel(ddx_state s, int i0, int n, double inv2, uint32_t mask, uint32_t sentinel,
+                            uint32_t* __restrict__ bsize, uint32_t* __restrict__ bucket, uint32_t* __restrict__ rank,
+                            unsigned long long* __restrict__ cellid, uint32_t* __restrict__ count) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int idx = i0 + p;
-    vals[p] = (uint32_t)p;
-    if (s.N[idx] == 0.0) {
-        keys[p] = sentinel;
-        cellid[p] = kNoCell;
+    // N == 0 (either sign) tested on the bits
+    if ((((unsigned long long)__double_as_longlong(s.N[idx])) << 1) == 0ull) {
+        bucket[p] = sentinel;
+        count[p] = 0;
         return;
     }
-    const unsigned long long id =
-        pack_cell(cell_coord(s.x[idx], inv), cell_coord(s.y[idx], inv), cell_coord(s.z[idx], inv));
-    cellid[p] = id;
-    keys[p] = bucket_of(id, mask);
+    uint32_t hx, hy, hz;
+    const uint32_t ux = axis_cell(s.x[idx], inv2, hx);
+    const uint32_t uy = axis_cell(s.y[idx], inv2, hy);
+    const uint32_t uz = axis_cell(s.z[idx], inv2, hz);
+    const uint32_t b = bucket_of(cell_lin(ux, uy, uz), mask);
+    cellid[p] = pack_u(ux, uy, uz) | ((unsigned long long)(hx << 2 | hy << 1 | hz) << 60);
+    bucket[p] = b;
+    rank[p] = atomicAdd(&bsize[b], 1u);
 }
 
-__global__ void ranges_kernel(const uint32_t* __restrict__ keys, int n, uint32_t sentinel,
-                              uint32_t* __restrict__ start, uint32_t* __restrict__ end) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    const uint32_t k = keys[q];
-    if (k == sentinel) return;
-    if (q == 0 || keys[q - 1] != k) start[k] = (uint32_t)q;
-    if (q == n - 1 || keys[q + 1] != k) end[k] = (uint32_t)q + 1;
+__global__ void scatter_kernel(ddx_state s, int i0, int n, uint32_t sentinel, const uint32_t* __restrict__ bucket,
+                               const uint32_t* __restrict__ rank, const unsigned long long* __restrict__ cellid,
+                               uint4* table, CellRec* __restrict__ rec, uint32_t* __restrict__ vals) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t b = bucket[p];
+    if (b == sentinel) return;
+    const uint32_t rk = rank[p];
+    const uint32_t q = table[b].x + rk;   // plain load: other fields of the entry are written here
+    const int idx = i0 + p;
+    CellRec r;
+    r.x = s.x[idx];
+    r.y = s.y[idx];
+    r.z = s.z[idx];
+    r.cell = cellid[p];
+    rec[q] = r;
+    vals[q] = (uint32_t)p;
+    if (rk == 0) {
+        const unsigned long long id = r.cell & kIdMask;
+        table[b].z = (uint32_t)id;
+        table[b].w = (uint32_t)(id >> 32);
+    }
 }
 
 constexpr uint32_t kSlots = 4;   // partners kept per tracer by the count pass
 
+// Inserts (i, j) into the ascending segment seg[0, filled) that holds at most k entries: while
+// it has room the segment grows; when full, j replaces the largest entry if it is smaller.
+__device__ __forceinline__ void keep_smallest(int2* seg, uint32_t& filled, uint32_t k, int i, int j) {
+    long long b;
+    if (filled < k) {
+        b = filled++;
+    } else {
+        if (seg[k - 1].y <= j) return;
+        b = (long long)k - 1;
+    }
+    while (b > 0 && seg[b - 1].y > j) {
+        seg[b] = seg[b - 1];
+        --b;
+    }
+    seg[b] = make_int2(i, j);
+}
+
+// hf: h as a float, rounded up.
 template <bool WRITE>
-__global__ void pairs_kernel(ddx_state s, int i0, int n, double h2, double inv, uint32_t mask, uint32_t sentinel,
-                             const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                             const unsigned long long* __restrict__ cellid, const uint32_t* __restrict__ start,
-                             const uint32_t* __restrict__ end, uint32_t* __restrict__ count,
+__global__ void pairs_kernel(const CellRec* __restrict__ rec, const uint32_t* __restrict__ vals,
+                             const uint4* __restrict__ table, const uint32_t* __restrict__ n_live, int i0,
+                             double h2, float hf, uint32_t mask, uint32_t* __restrict__ count,
                              int* __restrict__ slots, const uint32_t* __restrict__ offs, int2* __restrict__ pairs,
                              long long cap) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;   // sorted order: neighbours share buckets
-    if (q >= n) return;
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;   // bucket order
+    if (q >= *n_live) return;
     const uint32_t p = vals[q];
-    if (keys[q] == sentinel) {
-        if (!WRITE) count[p] = 0;
-        return;
-    }
     const int i = i0 + (int)p;
-    const long long base = WRITE ? (long long)offs[p] : 0;
-    if (WRITE && count[p] <= kSlots) {
-        // the count pass kept this tracer's partners: no second walk
+    int2* seg = nullptr;
+    uint32_t k = 0, filled = 0;
+    if (WRITE) {
         const uint32_t cnt = count[p];
-        for (uint32_t k = 0; k < cnt && base + k < cap; ++k) pairs[base + k] = make_int2(i, slots[(size_t)p * kSlots + k]);
-        const long long last = base + cnt < cap ? base + cnt : cap;
-        for (long long a = base + 1; a < last; ++a) {
-            const int2 v = pairs[a];
-            long long b = a - 1;
-            while (b >= base && pairs[b].y > v.y) { pairs[b + 1] = pairs[b]; --b; }
-            pairs[b + 1] = v;
+        const long long base = offs[p];
+        if (cnt == 0 || base >= cap) return;
+        k = (long long)cnt < cap - base ? cnt : (uint32_t)(cap - base);
+        seg = pairs + base;
+        if (cnt <= kSlots) {
+            // the count pass kept all of this tracer's partners: no second walk
+            for (uint32_t u = 0; u < cnt; ++u) keep_smallest(seg, filled, k, i, slots[(size_t)p * kSlots + u]);
+            return;
         }
-        return;
     }
-    const double xi = s.x[i], yi = s.y[i], zi = s.z[i];
-    long long cx, cy, cz;
-    unpack_cell(cellid[p], cx, cy, cz);
+    const CellRec me = rec[q];
+    const double xi = me.x, yi = me.y, zi = me.z;
+    const unsigned long long id0 = me.cell & kIdMask;
+    const uint32_t ux = (uint32_t)(id0 >> 40) & 0xFFFFFu, uy = (uint32_t)(id0 >> 20) & 0xFFFFFu,
+                   uz = (uint32_t)id0 & 0xFFFFFu;
     int lx, hx, ly, hy, lz, hz;
-    octant(xi, inv, cx, lx, hx);
-    octant(yi, inv, cy, ly, hy);
-    octant(zi, inv, cz, lz, hz);
+    axis_walk(ux, (uint32_t)(me.cell >> 62) & 1u, lx, hx);
+    axis_walk(uy, (uint32_t)(me.cell >> 61) & 1u, ly, hy);
+    axis_walk(uz, (uint32_t)(me.cell >> 60) & 1u, lz, hz);
+    const uint32_t lin0 = cell_lin(ux, uy, uz);
+    // FP32 rejection: float copies (truncated) of both positions differ from the exact ones
+    // by at most 2^-23 of their size, and a partner within h is no larger than M + h (M the
+    // largest own coordinate), so the float separation is within 2^-20 (M + h) of the exact
+    // one and its square below thr = (h + 2^-18 (M + h))^2 (1 + 2^-16) for every pair the
+    // FP64 test accepts.  Used where no float overflows or underflows (M + h < 1e15,
+    // h > 1e-12); elsewhere every candidate takes the FP64 test.
+    const float fxi = f32_trunc(xi), fyi = f32_trunc(yi), fzi = f32_trunc(zi);
+    const float M = fmaxf(fabsf(fxi), fmaxf(fabsf(fyi), fabsf(fzi)));
+    const bool filter = M + hf < 1e15f && hf > 1e-12f;   // false for NaN
+    const float reach = hf + (M + hf) * 0x1p-18f;
+    const float thr = reach * reach * (1.0f + 0x1p-16f);
     uint32_t c = 0;
-    for (int dx = lx; dx <= hx; ++dx)
-        for (int dy = ly; dy <= hy; ++dy)
-            for (int dz = lz; dz <= hz; ++dz) {
-                const unsigned long long nid = pack_cell(cx + dx, cy + dy, cz + dz);
-                const uint32_t b = bucket_of(nid, mask);
-                const uint32_t r1 = end[b];
-                for (uint32_t r = start[b]; r < r1; ++r) {
-                    const uint32_t pj = vals[r];
-                    if (pj <= p || cellid[pj] != nid) continue;
-                    const int j = i0 + (int)pj;
-                    const double ex = __dsub_rn(s.x[j], xi);
-                    const double ey = __dsub_rn(s.y[j], yi);
-                    const double ez = __dsub_rn(s.z[j], zi);
-                    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
-                    if (d2 < h2) {
-                        if (WRITE && base + c < cap) pairs[base + c] = make_int2(i, j);
-                        if (!WRITE && c < kSlots) slots[(size_t)p * kSlots + c] = j;
-                        ++c;
-                    }
-                }
+    // entries of bucket bk that lie in cell nid: j > i within h
+    auto walk = [&](unsigned long long nid, uint4 bk) {
+        for (uint32_t r = bk.x; r < bk.x + bk.y; ++r) {
+            if (r == q) continue;
+            const CellRec o = rec[r];
+            if ((o.cell & kIdMask) != nid) continue;
+            if (filter) {
+                const float fx = f32_trunc(o.x) - fxi, fy = f32_trunc(o.y) - fyi, fz = f32_trunc(o.z) - fzi;
+                if (fmaf(fx, fx, fmaf(fy, fy, fz * fz)) > thr) continue;
             }
-    if (!WRITE) {
-        count[p] = c;
-        return;
+            const uint32_t pj = vals[r];
+            if (pj <= p) continue;
+            const double ex = __dsub_rn(o.x, xi);
+            const double ey = __dsub_rn(o.y, yi);
+            const double ez = __dsub_rn(o.z, zi);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
+            if (d2 < h2) {
+                const int j = i0 + (int)pj;
+                if (WRITE) keep_smallest(seg, filled, k, i, j);
+                if (!WRITE && c < kSlots) slots[(size_t)p * kSlots + c] = j;
+                ++c;
+            }
+        }
+    };
+    if (hx - lx == 1 && hy - ly == 1 && hz - lz == 1) {
+        // the usual octant of 8 cells, cell t at (lx + t/4, ly + t/2 % 2, lz + t % 2): walk only
+        // the buckets that hold more than one tracer or whose one tracer is in that cell
+        const unsigned long long idl = neighbour_id(id0, lx, ly, lz);
+        const uint32_t linl = neighbour_lin(lin0, lx, ly, lz);
+        uint32_t need = 0;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const unsigned long long nid = neighbour_id(idl, t >> 2, (t >> 1) & 1, t & 1);
+            const uint4 e = table[bucket_of(neighbour_lin(linl, t >> 2, (t >> 1) & 1, t & 1), mask)];
+            const bool one_other = e.y == 1 && (((unsigned long long)e.w << 32) | e.z) != nid;
+            if (e.y != 0 && !one_other) need |= 1u << t;
+        }
+        while (need) {
+            const int t = __ffs(need) - 1;
+            need &= need - 1;
+            const int dx = t >> 2, dy = (t >> 1) & 1, dz = t & 1;
+            walk(neighbour_id(idl, dx, dy, dz), table[bucket_of(neighbour_lin(linl, dx, dy, dz), mask)]);
+        }
+    } else {
+        for (int dx = lx; dx <= hx; ++dx)
+            for (int dy = ly; dy <= hy; ++dy)
+                for (int dz = lz; dz <= hz; ++dz)
+                    walk(neighbour_id(id0, dx, dy, dz), table[bucket_of(neighbour_lin(lin0, dx, dy, dz), mask)]);
     }
-    // order this tracer's partners by j (segments are short)
-    const long long last = base + c < cap ? base + c : cap;
-    for (long long a = base + 1; a < last; ++a) {
-        const int2 v = pairs[a];
-        long long b = a - 1;
-        while (b >= base && pairs[b].y > v.y) { pairs[b + 1] = pairs[b]; --b; }
-        pairs[b + 1] = v;
-    }
+    if (!WRITE) count[p] = c;
 }
 
 }  // namespace
 
 struct CollideScratch {
-    uint32_t *keys = nullptr, *vals = nullptr, *start = nullptr, *end = nullptr, *count = nullptr,
-             *offs = nullptr, *temp = nullptr, *total = nullptr;
+    uint32_t *bucket = nullptr, *rank = nullptr, *count = nullptr, *offs = nullptr, *temp = nullptr,
+             *total = nullptr;
+    uint32_t *vals = nullptr, *bsize = nullptr;
+    uint4* table = nullptr;
     int* slots = nullptr;
     unsigned long long* cellid = nullptr;
+    CellRec* rec = nullptr;
     int n_cap = 0;
     uint32_t t_cap = 0;
 };
 
 void collide_free(CollideScratch*& c) {
     if (!c) return;
-    cudaFree(c->keys); cudaFree(c->vals); cudaFree(c->start); cudaFree(c->end); cudaFree(c->count);
-    cudaFree(c->offs); cudaFree(c->temp); cudaFree(c->total); cudaFree(c->cellid); cudaFree(c->slots);
+    cudaFree(c->table); cudaFree(c->bucket); cudaFree(c->rank); cudaFree(c->count); cudaFree(c->offs);
+    cudaFree(c->temp); cudaFree(c->total); cudaFree(c->slots); cudaFree(c->cellid); cudaFree(c->vals); cudaFree(c->bsize);
+    cudaFree(c->rec);
     delete c;
     c = nullptr;
 }
@@ -190,21 +308,21 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
     const int n = i1 - i0;
     *n_pairs = 0;
     if (n <= 1) return DDX_OK;
-    uint32_t T = 1024;
-    while (T < 2u * (uint32_t)n) T <<= 1;
-    int tbits = 0;
-    while ((1u << tbits) < T) ++tbits;
+    uint32_t T = 1024;   // buckets: at least 2n, at most 2^30 (one tracer per bucket at the limit)
+    while (T < 2u * (uint32_t)n && T < (1u << 30)) T <<= 1;
     if (!cs) cs = new CollideScratch();
     if (cs->n_cap < n || cs->t_cap < T) {
         const int ncap = n > cs->n_cap ? n : cs->n_cap;
         const uint32_t tcap = T > cs->t_cap ? T : cs->t_cap;
         CollideScratch* nc = new CollideScratch();
-        const size_t tw = sort_temp_words(ncap) + scan_temp_words(ncap);
-        if (cudaMalloc(&nc->keys, 4ull * ncap) || cudaMalloc(&nc->vals, 4ull * ncap) ||
-            cudaMalloc(&nc->count, 4ull * ncap) || cudaMalloc(&nc->offs, 4ull * ncap) ||
-            cudaMalloc(&nc->cellid, 8ull * ncap) || cudaMalloc(&nc->slots, 4ull * kSlots * ncap) ||
-            cudaMalloc(&nc->start, 4ull * tcap) ||
-            cudaMalloc(&nc->end, 4ull * tcap) || cudaMalloc(&nc->temp, 4ull * tw) ||
+        const size_t tw = scan_temp_words((int)tcap > ncap ? (int)tcap : ncap);
+        if (cudaMalloc(&nc->table, 16ull * tcap) || cudaMalloc(&nc->bsize, 4ull * tcap) ||
+            cudaMalloc(&nc->bucket, 4ull * ncap) ||
+            cudaMalloc(&nc->rank, 4ull * ncap) || cudaMalloc(&nc->count, 4ull * ncap) ||
+            cudaMalloc(&nc->offs, 4ull * ncap) || cudaMalloc(&nc->cellid, 8ull * ncap) ||
+            cudaMalloc(&nc->vals, 4ull * ncap) ||
+            cudaMalloc(&nc->rec, sizeof(CellRec) * (size_t)ncap) ||
+            cudaMalloc(&nc->slots, 4ull * kSlots * ncap) || cudaMalloc(&nc->temp, 4ull * tw) ||
             cudaMalloc(&nc->total, 16)) {
             collide_free(nc);
             cudaGetLastError();
@@ -217,24 +335,30 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
     }
     const uint32_t mask = T - 1, sentinel = T;
     const double cell = 2.0 * h * (1.0 + 1e-9);
-    const double inv = 1.0 / cell;
+    const double inv2 = 2.0 * (1.0 / cell);
     const double h2 = h * h;
+    float hf = (float)h;   // rounded up to a float
+    if ((double)hf < h) hf = nextafterf(hf, INFINITY);
     const int thr = 256, blk = (n + thr - 1) / thr;
-    keys_kernel<<<blk, thr, 0, st>>>(s, i0, n, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid);
-    if (radix_sort_pairs(cs->keys, cs->vals, n, tbits + 1, cs->temp, st) != cudaSuccess) return DDX_ERR_CUDA;
-    cudaMemsetAsync(cs->start, 0, 4ull * T, st);
-    cudaMemsetAsync(cs->end, 0, 4ull * T, st);
-    ranges_kernel<<<blk, thr, 0, st>>>(cs->keys, n, sentinel, cs->start, cs->end);
-    pairs_kernel<false><<<blk, thr, 0, st>>>(s, i0, n, h2, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid,
-                                             cs->start, cs->end, cs->count, cs->slots, nullptr, nullptr, 0);
-    uint32_t* scan_temp = cs->temp + sort_temp_words(cs->n_cap);
-    if (exclusive_scan(cs->count, cs->offs, n, scan_temp, cs->total, st) != cudaSuccess) return DDX_ERR_CUDA;
+    uint32_t* n_live = cs->total;
+    uint32_t* n_found = cs->total + 1;
+    cudaMemsetAsync(cs->bsize, 0, 4ull * T, st);
+    keys_kernel<<<blk, thr, 0, st>>>(s, i0, n, inv2, mask, sentinel, cs->bsize, cs->bucket, cs->rank, cs->cellid,
+                                     cs->count);
+    uint32_t* tw = reinterpret_cast<uint32_t*>(cs->table);   // entries {start, size, first cell}
+    if (exclusive_scan_strided(cs->bsize, 1, tw, 4, (int)T, cs->temp, n_live, st, tw + 1) != cudaSuccess)
+        return DDX_ERR_CUDA;
+    scatter_kernel<<<blk, thr, 0, st>>>(s, i0, n, sentinel, cs->bucket, cs->rank, cs->cellid, cs->table, cs->rec,
+                                        cs->vals);
+    pairs_kernel<false><<<blk, thr, 0, st>>>(cs->rec, cs->vals, cs->table, n_live, i0, h2, hf, mask, cs->count,
+                                             cs->slots, nullptr, nullptr, 0);
+    if (exclusive_scan(cs->count, cs->offs, n, cs->temp, n_found, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (pairs && cap > 0)
-        pairs_kernel<true><<<blk, thr, 0, st>>>(s, i0, n, h2, inv, mask, sentinel, cs->keys, cs->vals, cs->cellid,
-                                                cs->start, cs->end, cs->count, cs->slots, cs->offs, pairs, cap);
+        pairs_kernel<true><<<blk, thr, 0, st>>>(cs->rec, cs->vals, cs->table, n_live, i0, h2, hf, mask, cs->count,
+                                                cs->slots, cs->offs, pairs, cap);
     if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
     uint32_t tot = 0;
-    if (cudaMemcpyAsync(&tot, cs->total, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return DDX_ERR_CUDA;
+    if (cudaMemcpyAsync(&tot, n_found, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return DDX_ERR_CUDA;
     *n_pairs = tot;
     return DDX_OK;

@@ -178,8 +178,9 @@ int ddx_image(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
 int ddx_sed(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust,
             const ddx_view *view, double *Fsed, int precision, int mode, void *stream);
 
-/* Collision candidates through a spatial-hash grid built by radix sort (no counterpart
- * in the reference, which has no collision detection).  Two live tracers (N != 0)
+/* Collision candidates through a spatial-hash grid built by a one-pass radix (counting)
+ * sort on the hashed cell ids (no counterpart in the reference, which has no collision
+ * detection).  Two live tracers (N != 0)
  * i < j of the state range [i0, i1) collide when
  *     (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2     (FP64, every operation rounded alone),
  * which makes the list identical to a brute-force test with that expression.  Writes up

@@ -28,6 +28,11 @@ def test_pairs_match_brute_force_ring(engine):
         o = oc.collide(s.state, s.n_grav, n, h, "brute")
         assert tot == len(o)
         np.testing.assert_array_equal(g, o)
+    # a buffer too small keeps the first cap pairs of the ordered list
+    for cap in (1, tot // 3, tot - 1):
+        part, tot2 = gpu_pairs(engine, s.state, s.n_grav, n, 2.0, cap)
+        assert tot2 == tot
+        np.testing.assert_array_equal(part, o[:cap])
 
 
 def test_pairs_match_cell_list_full_size(engine):
@@ -55,9 +60,12 @@ def test_dense_cluster_dead_tracers_and_capacity(engine):
     o = oc.collide(st, 0, 3000, 2e-3, "brute")
     assert tot == len(o) > 100000
     np.testing.assert_array_equal(g, o)
-    part, tot2 = gpu_pairs(engine, st, 0, 3000, 2e-3, cap=1000)   # buffer too small
-    assert tot2 == tot
-    assert len(part) == 1000
+    # buffers too small: the cut falls inside tracers' segments of tens of partners (found
+    # by a second walk), which keep their smallest j
+    for cap in (1000, 77777):
+        part, tot2 = gpu_pairs(engine, st, 0, 3000, 2e-3, cap=cap)
+        assert tot2 == tot
+        np.testing.assert_array_equal(part, o[:cap])
 
 
 def test_boundary_distances_and_cell_edges(engine):
@@ -72,6 +80,38 @@ def test_boundary_distances_and_cell_edges(engine):
     o = oc.collide(st, 0, n, h, "brute")
     np.testing.assert_array_equal(g, o)
     assert [0, 1] not in o.tolist() and [2, 3] in o.tolist()
+
+
+def margin_state(base, h, n, seed):
+    """n tracers within +-1.2 h of (base, base, base) on each axis, plus pairs placed at one
+    FP64 step inside and outside h along a diagonal."""
+    g = synth.rng(seed)
+    pts = base + g.uniform(-1.2 * h, 1.2 * h, (n, 3))
+    d = np.array([1.0, 1.0, 1.0]) / math.sqrt(3.0)
+    extra = []
+    for k in range(8):
+        a = base + g.uniform(-h, h, 3)
+        for f in (1.0 - 2.0 ** -50, 1.0, 1.0 + 2.0 ** -50):
+            extra += [a, a + d * h * f]
+    pts = np.vstack([pts, np.array(extra)])
+    m = len(pts)
+    st = {"x": pts[:, 0].copy(), "y": pts[:, 1].copy(), "z": pts[:, 2].copy(), "vx": np.zeros(m), "vy": np.zeros(m),
+          "vz": np.zeros(m), "m": np.zeros(m), "N": np.ones(m), "id": np.full(m, -1, np.int32)}
+    return st, m
+
+
+@pytest.mark.parametrize("base,h", [(130.0, 0.1), (1.0, 0.3), (1.0e5, 0.25), (3.0e3, 1e-4), (-2.5e4, 0.5),
+                                    (7.0e15, 1e3), (0.0, 1e-13)])
+def test_float_rejection_keeps_every_pair(engine, base, h):
+    """The FP32 rejection in front of the FP64 test drops no pair: separations within one FP64
+    step of h where its margin is small against h (the ring's scale), at coordinates where a
+    float's step (2^-23 of the coordinate) is near or above h, beyond the range where the
+    rejection is used (1e15), and at an h below it (1e-12)."""
+    st, m = margin_state(base, h, 400, 11)
+    g, tot = gpu_pairs(engine, st, 0, m, h)
+    o = oc.collide(st, 0, m, h, "brute")
+    assert tot == len(o) > 0
+    np.testing.assert_array_equal(g, o)
 
 
 def test_empty_and_single_ranges(engine):
