@@ -6,13 +6,15 @@
 //  1. keys    : cell = floor(x / cs) per axis with cs = 2h (1 + 1e-9), clamped to
 //               +-(2^19 - 2) (clamping only merges far cells), and the half of the cell the
 //               tracer lies in; the cell is hashed (the 32-bit finaliser of MurmurHash3 over
-//               a linear form of the three 20-bit coordinates) into T = 2^k >= 2n buckets,
+//               a linear form lin of the three 20-bit coordinates) into T = 2^k >= 2n buckets,
 //               and an atomic increment of the bucket's size gives the tracer its rank in it;
 //  2. starts  : an exclusive scan of the T bucket sizes gives every bucket its first slot;
-//               the bucket table holds 16-byte entries {start, size, cell id of the first
-//               tracer}, so one load answers most lookups;
+//               the bucket table holds 16-byte entries {start, size, lin of the first two
+//               tracers' cells} (equal cells have equal lin), so one load answers most
+//               lookups;
 //  3. scatter : every live tracer writes {x, y, z, cell id and halves} and its index to slot
-//               start + rank (the tracer of rank 0 also its cell id to the bucket's entry).
+//               start + rank; the tracers of rank 0 and 1 also their cells' lin to the
+//               bucket's entry.
 //               Steps 1-3 are a radix sort on the whole bucket id in one pass (a counting
 //               sort): the bucket sizes are its histogram, the scan its offsets;
 //  4. count   : every tracer, in bucket order, visits the buckets of the 8 cells of its
@@ -22,8 +24,9 @@
 //               cell id is that cell (hash collisions are filtered), j > i, and applies the
 //               distance test, counting the partners and keeping the first kSlots of them.
 //               Most neighbour cells are empty, and their bucket is then empty or holds one
-//               tracer of another cell: the 8 bucket entries, loaded together, settle those
-//               without touching the tracers, and only the rest are walked.  A test in FP32
+//               or two tracers of other cells: the 8 bucket entries, loaded together, settle
+//               those without touching the tracers (a lin that differs means another cell),
+//               and only the rest are walked.  A test in FP32
 //               with a proven margin rejects the far candidates first; the FP64 test decides
 //               the rest (FP64 runs at 1/64 of the FP32 rate here, and a warp pays for it
 //               whenever any of its lanes tests);
@@ -155,10 +158,12 @@ __global__ void scatter_kernel(ddx_state s, int i0, int n, uint32_t sentinel, co
     r.cell = cellid[p];
     rec[q] = r;
     vals[q] = (uint32_t)p;
-    if (rk == 0) {
+    if (rk < 2) {
         const unsigned long long id = r.cell & kIdMask;
-        table[b].z = (uint32_t)id;
-        table[b].w = (uint32_t)(id >> 32);
+        const uint32_t lin = cell_lin((uint32_t)(id >> 40) & 0xFFFFFu, (uint32_t)(id >> 20) & 0xFFFFFu,
+                                      (uint32_t)id & 0xFFFFFu);
+        if (rk == 0) table[b].z = lin;
+        else table[b].w = lin;
     }
 }
 
@@ -254,16 +259,19 @@ __global__ void pairs_kernel(const CellRec* __restrict__ rec, const uint32_t* __
     };
     if (hx - lx == 1 && hy - ly == 1 && hz - lz == 1) {
         // the usual octant of 8 cells, cell t at (lx + t/4, ly + t/2 % 2, lz + t % 2): walk only
-        // the buckets that hold more than one tracer or whose one tracer is in that cell
+        // the buckets with three or more tracers, or with one of the first two (other than this
+        // tracer) in that cell
         const unsigned long long idl = neighbour_id(id0, lx, ly, lz);
         const uint32_t linl = neighbour_lin(lin0, lx, ly, lz);
+        const int own = (lx ? 4 : 0) | (ly ? 2 : 0) | (lz ? 1 : 0);   // t of the tracer's cell
         uint32_t need = 0;
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
-            const unsigned long long nid = neighbour_id(idl, t >> 2, (t >> 1) & 1, t & 1);
-            const uint4 e = table[bucket_of(neighbour_lin(linl, t >> 2, (t >> 1) & 1, t & 1), mask)];
-            const bool one_other = e.y == 1 && (((unsigned long long)e.w << 32) | e.z) != nid;
-            if (e.y != 0 && !one_other) need |= 1u << t;
+            const uint32_t nlin = neighbour_lin(linl, t >> 2, (t >> 1) & 1, t & 1);
+            const uint4 e = table[bucket_of(nlin, mask)];
+            const bool self0 = t == own && e.x == q, self1 = t == own && e.x + 1 == q;
+            const bool hit = (e.y >= 1 && e.z == nlin && !self0) || (e.y >= 2 && e.w == nlin && !self1) || e.y >= 3;
+            if (hit) need |= 1u << t;
         }
         while (need) {
             const int t = __ffs(need) - 1;
