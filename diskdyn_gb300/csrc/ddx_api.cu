@@ -66,12 +66,31 @@ cudaError_t dalloc(T** p, size_t n) {
 
 void free_massive(MassiveScratch& ms) {
     cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.PP); cudaFree(ms.A); cudaFree(ms.R);
-    cudaFree(ms.part);
+    cudaFree(ms.part); cudaFree(ms.slot);
+    order_free(ms.src_order);
+    order_free(ms.dust_order);
     ms = MassiveScratch{};   // the status word belongs to the context, not to the scratch
 }
 
-int ensure_massive(ddx_ctx* c, int n_grav) {
-    if (c->ms.cap >= n_grav && c->ms.P) return DDX_OK;
+int alloc_massive(ddx_ctx* c, int n_grav);
+
+// The massive set's scratch for n_grav bodies and, for the mixed path, the scratch of the
+// spatial order of the sources and of n_dust tracers (grown on demand).
+int ensure_massive(ddx_ctx* c, int n_grav, int n_dust, int precision) {
+    if (!(c->ms.cap >= n_grav && c->ms.P)) {
+        const int r = alloc_massive(c, n_grav);
+        if (r) return r;
+    }
+    if (precision == DDX_PREC_MIXED && c->ms.dust_order.cap < n_dust) {
+        if (order_alloc(c->ms.dust_order, n_dust, false) != cudaSuccess) {
+            cudaGetLastError();
+            return DDX_ERR_NOMEM;
+        }
+    }
+    return DDX_OK;
+}
+
+int alloc_massive(ddx_ctx* c, int n_grav) {
     free_massive(c->ms);
     int cap = 64;
     while (cap < n_grav) cap *= 2;
@@ -83,7 +102,8 @@ int ensure_massive(ddx_ctx* c, int n_grav) {
     if (dalloc(&ms.P, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.Phi, (size_t)4 * cap) != cudaSuccess ||
         dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.PP, (size_t)4 * ms.pcap) != cudaSuccess ||
         dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess || dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess ||
-        dalloc(&ms.part, (size_t)ms.part_words) != cudaSuccess) {
+        dalloc(&ms.part, (size_t)ms.part_words) != cudaSuccess || dalloc(&ms.slot, (size_t)cap) != cudaSuccess ||
+        order_alloc(ms.src_order, cap, true) != cudaSuccess) {
         ms.status = nullptr;
         free_massive(ms);
         cudaGetLastError();
@@ -361,7 +381,7 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
     int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
     if (r) return r;
     cudaSetDevice(c->device);
-    if ((r = ensure_massive(c, n_grav)) || (r = ensure_pipeline(c))) return r;
+    if ((r = ensure_massive(c, n_grav, n_dust, precision)) || (r = ensure_pipeline(c))) return r;
     cudaStream_t st = (cudaStream_t)stream;
     take_injection(c, a);
     // the massive bodies: in, step, out (small)
@@ -400,7 +420,7 @@ int ddx_evolve(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt
     int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
     if (r) return r;
     cudaSetDevice(c->device);
-    if ((r = ensure_massive(c, n_grav))) return r;
+    if ((r = ensure_massive(c, n_grav, n_dust, precision))) return r;
     cudaStream_t st = (cudaStream_t)stream;
     for (int k = 0; k < n_steps; ++k)
         if ((r = enqueue_step(c, *s, a, precision, st))) return r;
@@ -416,7 +436,7 @@ int prepare_call(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double 
     int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
     if (r) return r;
     cudaSetDevice(c->device);
-    return ensure_massive(c, n_grav);
+    return ensure_massive(c, n_grav, n_dust, precision);
 }
 }  // namespace
 

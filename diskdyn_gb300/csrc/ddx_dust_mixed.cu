@@ -4,7 +4,19 @@
 // PR + stellar-wind drag, Lorentz force), the gravity of the planets (bodies
 // 1..n_exact-1) and the RK4 combination.  FP32: the gravity of the planetesimals, on
 // hi/lo split positions so the separation keeps FP32 relative precision at any distance
-// from the star, with plain sums over spans of 16 sources and a Kahan sum across spans.
+// from the star, with plain sums over spans of 16 pair records (32 sources) and a Kahan sum
+// across spans.
+//
+// Far spans.  The low parts matter only for sources near the tracer: for a source at
+// distance r >= X (X the largest |coordinate| of the two), the high parts alone give the
+// separation within (sqrt(3) 2^-23 + 2^-24) r, below the error of rsqrt.approx already in
+// every term.  So a tracer takes a span with the high-part separation (3 of the 9
+// separation operations) when the span's box (high parts of its 32 sources) lies at least
+// X from the tracer's own point, X over the box and the point.  The choice depends on the
+// tracer and the sources alone, so a tracer's result does not depend on the others or on
+// their order.  The tracers are visited in cell order and the sources sit in their pair
+// records in cell order (ddx_order.cu), so the lanes of a warp lie close together and
+// nearly always make the same choice for a span.
 //
 // Blackwell mapping:
 //  - perturbers arrive as 64-byte pair records (two bodies per record, one quantity of
@@ -60,16 +72,99 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, unsigned parity, unsigned
     return true;
 }
 
+// Box of every span's sources (high parts, padding slots left out) at every stage, written
+// into the pad slots of the span's first four pair records, so it reaches shared memory with
+// the tile: record 0 {min x, max x}, record 1 {min y, max y}, record 2 {min z, max z},
+// record 3 {max |coordinate|, 0}; the maximum is NaN when a coordinate is NaN (such a span
+// never counts as far).
+__global__ void span_box_kernel(BodyPair* __restrict__ PP, int pcap, int n_src, int nspans) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 4 * nspans) return;
+    const int stage = k / nspans, span = k - stage * nspans;
+    BodyPair* const R = PP + (size_t)stage * pcap + (size_t)span * kPairSpan;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool nan = false;
+    for (int u = 0; u < 2 * kPairSpan; ++u) {
+        const int q = span * 2 * kPairSpan + u;
+        if (q >= n_src) break;
+        const BodyPair& r = R[u >> 1];
+        const float v[3] = {r.hx[u & 1], r.hy[u & 1], r.hz[u & 1]};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            nan |= !(v[a] == v[a]);
+            lo[a] = fminf(lo[a], v[a]);
+            hi[a] = fmaxf(hi[a], v[a]);
+        }
+    }
+    float xm = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) xm = fmaxf(xm, fmaxf(fabsf(lo[a]), fabsf(hi[a])));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { R[a].pad[0] = lo[a]; R[a].pad[1] = hi[a]; }
+    R[3].pad[0] = nan ? __int_as_float(0x7FC00000) : xm;
+    R[3].pad[1] = 0.f;
+}
+
+// The test of one tracer (high parts xh, yh, zh; own = its largest |coordinate|) against one
+// span box (bx, by, bz: min and max per axis; xm: its largest |coordinate|, NaN when a
+// coordinate is NaN): far when the box lies at least X = max(xm, own) away.  Rounded
+// operations only (no contraction), so the block tests below imply its outcome.
+__device__ __forceinline__ bool lane_far(float2 bx, float2 by, float2 bz, float xm, float xh, float yh, float zh,
+                                         float own) {
+    const float gx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, xh), __fsub_rn(xh, bx.y)));
+    const float gy = fmaxf(0.f, fmaxf(__fsub_rn(by.x, yh), __fsub_rn(yh, by.y)));
+    const float gz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, zh), __fsub_rn(zh, bz.y)));
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+    const float X = fmaxf(xm, own);
+    return xm == xm && d2 >= __fmul_rn(X, X);
+}
+
+// The same tests for a whole block of tracers from its box b (min and max of the high parts
+// per axis, and the largest own): far for every tracer when the nearest point of b is far
+// with X = max(xm, largest own); near for every tracer when even the farthest point of b is
+// nearer than xm.  Each rounded step is monotone, so these imply lane_far's outcome for any
+// tracer inside b.
+__device__ __forceinline__ void block_far(float2 bx, float2 by, float2 bz, float xm, const float* b, bool& all_far,
+                                          bool& all_near) {
+    const float nx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, b[1]), __fsub_rn(b[0], bx.y)));
+    const float ny = fmaxf(0.f, fmaxf(__fsub_rn(by.x, b[3]), __fsub_rn(b[2], by.y)));
+    const float nz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, b[5]), __fsub_rn(b[4], bz.y)));
+    const float fx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, b[0]), __fsub_rn(b[1], bx.y)));
+    const float fy = fmaxf(0.f, fmaxf(__fsub_rn(by.x, b[2]), __fsub_rn(b[3], by.y)));
+    const float fz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, b[4]), __fsub_rn(b[5], bz.y)));
+    const float dn = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
+    const float df = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+    const float X = fmaxf(xm, b[6]);
+    all_far = xm == xm && dn >= __fmul_rn(X, X);
+    all_near = !(xm == xm) || df < __fmul_rn(xm, xm);
+}
+
+__device__ __forceinline__ void span_box(const BodyPair* R, float2& bx, float2& by, float2& bz, float& xm) {
+    bx = *reinterpret_cast<const float2*>(R[0].pad);
+    by = *reinterpret_cast<const float2*>(R[1].pad);
+    bz = *reinterpret_cast<const float2*>(R[2].pad);
+    xm = R[3].pad[0];
+}
+
+// Spans with one bit per block test (all far, all near) in shared memory, per stage; beyond
+// this many spans every tracer tests every span itself.
+constexpr int kFlagSpans = 4096;
+
 // Three blocks per SM (80 registers): the few FP64 values the compiler keeps in local
 // memory are touched only between stages, and the extra warps hide the latency of the
 // broadcast shared-memory reads and of rsqrt.approx better than two blocks without spills.
 __global__ void __launch_bounds__(kThreads, 3)
-dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins) {
+dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins,
+                      const int* __restrict__ perm, bool boxes) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar[2];
+    __shared__ float bred[kThreads / 32][7];
+    __shared__ float bbox[7];                     // the block's box at the current stage, largest own
+    __shared__ uint32_t allfar[kFlagSpans / 32], allnear[kFlagSpans / 32];
     BodyPair* const tiles = reinterpret_cast<BodyPair*>(smem);
     const int tid = threadIdx.x;
-    const int i = blockIdx.x * blockDim.x + tid;
+    const int slot = blockIdx.x * blockDim.x + tid;   // position in the visiting order
+    const int i = perm && slot < a.n_dust ? perm[slot] : slot;
     const int ng = a.n_grav;
     const int t = ng + i;
 
@@ -161,6 +256,50 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
         split_hilo(xt, xh, xl); split_hilo(yt, yh, yl); split_hilo(zt, zh, zl);
         const f2 XH = f2_dup(xh), XL = f2_dup(xl), YH = f2_dup(yh), YL = f2_dup(yl);
         const f2 ZH = f2_dup(zh), ZL = f2_dup(zl);
+        const float own = fmaxf(fabsf(xh), fmaxf(fabsf(yh), fabsf(zh)));   // largest |coordinate|
+        // per stage: the block's box (live tracers) and, per span, whether the box settles
+        // every tracer's choice (bits in shared memory); spans left open are tested per tracer
+        const int nspans = npairs / kPairSpan;
+        const bool flags = boxes && nspans <= kFlagSpans;
+        if (flags) {
+            const float v[7] = {xh, xh, yh, yh, zh, zh, own};
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                const bool mx = (q & 1) || q == 6;
+                float w = alive ? v[q] : (mx ? -INFINITY : INFINITY);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float u = __shfl_xor_sync(0xffffffffu, w, o);
+                    w = mx ? fmaxf(w, u) : fminf(w, u);
+                }
+                if ((tid & 31) == 0) bred[tid >> 5][q] = w;
+            }
+            __syncthreads();
+            if (tid < 7) {
+                const bool mx = (tid & 1) || tid == 6;
+                float w = bred[0][tid];
+                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) w = mx ? fmaxf(w, bred[k][tid]) : fminf(w, bred[k][tid]);
+                bbox[tid] = tid == 6 ? fmaxf(w, 0.f) : w;
+            }
+            __syncthreads();
+            float b[7];
+#pragma unroll
+            for (int q = 0; q < 7; ++q) b[q] = bbox[q];
+            const BodyPair* PPs = ms.PP + (size_t)st * ms.pcap;
+            for (int j0 = 0; j0 < nspans; j0 += blockDim.x) {   // uniform trip count: ballots below
+                const int j = j0 + tid;
+                bool f = false, nr = false;
+                if (j < nspans) {
+                    float2 bx, by, bz;
+                    float xm;
+                    span_box(PPs + (size_t)j * kPairSpan, bx, by, bz, xm);
+                    block_far(bx, by, bz, xm, b, f, nr);
+                }
+                const uint32_t wf = __ballot_sync(0xffffffffu, f), wn = __ballot_sync(0xffffffffu, nr);
+                if ((tid & 31) == 0 && j < nspans) { allfar[j >> 5] = wf; allnear[j >> 5] = wn; }   // lane 0: j = 32 w
+            }
+            __syncthreads();
+        }
         f2 Sx = 0, Sy = 0, Sz = 0, Cx = 0, Cy = 0, Cz = 0;
         for (int tt = 0; tt < ntiles; ++tt, ++g) {
             lost = __syncthreads_or(lost);      // also: every thread is done with tile g-1
@@ -171,24 +310,58 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
             if (!alive) continue;
             const BodyPair* T = tiles + (g & 1) * kTilePairs;
             const int cnt = min(kTilePairs, npairs - tt * kTilePairs);   // a multiple of kPairSpan
+            static_assert(kTilePairs / kPairSpan <= 32, "one mask bit per span of a tile");
+            uint32_t fm = 0u;
+            if (boxes) {
+                const uint32_t all = cnt / kPairSpan == 32 ? 0xFFFFFFFFu : (1u << (cnt / kPairSpan)) - 1u;
+                uint32_t open = all;
+                if (flags) {
+                    fm = allfar[tt] & all;
+                    open = all & ~(allfar[tt] | allnear[tt]);
+                }
+                while (open) {   // the same mask in every lane: no divergence here
+                    const int j = __ffs(open) - 1;
+                    open &= open - 1;
+                    float2 bx, by, bz;
+                    float xm;
+                    span_box(T + j * kPairSpan, bx, by, bz, xm);
+                    if (lane_far(bx, by, bz, xm, xh, yh, zh, own)) fm |= 1u << j;
+                }
+            }
             for (int k = 0; k < cnt; k += kPairSpan) {
                 f2 px = 0, py = 0, pz = 0;
+                if ((fm >> (k / kPairSpan)) & 1u) {
 #pragma unroll
-                for (int u = 0; u < kPairSpan; ++u) {
-                    const BodyPair* r = T + k + u;
-                    const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);  // hx, hy
-                    const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);  // hz, m
-                    const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r->lx);  // lx, ly
-                    const f2 lz = *reinterpret_cast<const f2*>(r->lz);
-                    const f2 dX = add2(sub2(q0.x, XH), sub2(q2.x, XL));
-                    const f2 dY = add2(sub2(q0.y, YH), sub2(q2.y, YL));
-                    const f2 dZ = add2(sub2(q1.x, ZH), sub2(lz, ZL));
-                    const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
-                    float r0, r1;
-                    f2_split(RR, r0, r1);
-                    const f2 ri = f2_join(rsqrt_approx(r0), rsqrt_approx(r1));
-                    const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
-                    px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+                    for (int u = 0; u < kPairSpan; ++u) {
+                        const BodyPair* r = T + k + u;
+                        const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);  // hx, hy
+                        const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);  // hz, m
+                        const f2 dX = sub2(q0.x, XH), dY = sub2(q0.y, YH), dZ = sub2(q1.x, ZH);
+                        const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+                        float r0, r1;
+                        f2_split(RR, r0, r1);
+                        const f2 ri = f2_join(rsqrt_approx(r0), rsqrt_approx(r1));
+                        const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
+                        px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+                    }
+                } else {
+#pragma unroll
+                    for (int u = 0; u < kPairSpan; ++u) {
+                        const BodyPair* r = T + k + u;
+                        const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);  // hx, hy
+                        const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);  // hz, m
+                        const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r->lx);  // lx, ly
+                        const f2 lz = *reinterpret_cast<const f2*>(r->lz);
+                        const f2 dX = add2(sub2(q0.x, XH), sub2(q2.x, XL));
+                        const f2 dY = add2(sub2(q0.y, YH), sub2(q2.y, YL));
+                        const f2 dZ = add2(sub2(q1.x, ZH), sub2(lz, ZL));
+                        const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+                        float r0, r1;
+                        f2_split(RR, r0, r1);
+                        const f2 ri = f2_join(rsqrt_approx(r0), rsqrt_approx(r1));
+                        const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
+                        px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+                    }
                 }
                 kahan2(Sx, Cx, px); kahan2(Sy, Cy, py); kahan2(Sz, Cz, pz);
             }
@@ -247,7 +420,19 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
     }
     const int threads = dust_block_threads(a.n_dust);   // 256 unless the grains are few
     const int blocks = (a.n_dust + threads - 1) / threads;
-    dust_rk4_mixed_kernel<<<blocks, threads, smem, st>>>(s, a, ms, bins);
+    // the tracers' visiting order and the spans' boxes, when the context keeps their scratch
+    const int* perm = nullptr;
+    bool boxes = false;
+    const int n_src = a.n_grav - a.n_exact;
+    if (ms.slot && ms.dust_order.cap >= a.n_dust && n_src > 0) {
+        cudaError_t e = order_bodies(s, a.n_grav, a.n_dust, true, ms.dust_order, ms.dust_order.perm, nullptr, st);
+        if (e != cudaSuccess) return e;
+        const int nspans = pair_count(n_src) / kPairSpan;
+        span_box_kernel<<<(4 * nspans + 127) / 128, 128, 0, st>>>(ms.PP, ms.pcap, n_src, nspans);
+        perm = ms.dust_order.perm;
+        boxes = true;
+    }
+    dust_rk4_mixed_kernel<<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,8 @@ __host__ __device__ __forceinline__ Body make_body(double x, double y, double z,
 // dust kernel consumes: every 8-byte slot holds the same quantity of both bodies, so one
 // f32x2 instruction works on the pair.  hi/lo is the FP32 split x = hi + lo with
 // hi = fp32(x), lo = fp32(x - hi).  64 bytes, moved into shared memory by TMA bulk copies.
+// pad: free for the force loops; the mixed dust launch writes the box of each span of
+// kPairSpan records into the pads of its first four records.
 struct __align__(16) BodyPair {
     float hx[2], hy[2], hz[2], m[2];
     float lx[2], ly[2], lz[2], pad[2];
@@ -66,6 +68,27 @@ __host__ __device__ constexpr int pair_count(int n_src) {
     const int np = (n_src + 1) / 2;
     return (np + kPairSpan - 1) / kPairSpan * kPairSpan;
 }
+
+// Scratch of one cell ordering (ddx_order.cu) of up to cap bodies.
+struct OrderScratch {
+    uint32_t *key, *rank;      // [cap] cell of each body, its rank in the cell
+    uint32_t *count, *start;   // [kOrderBins + 1] bodies per cell, first position of each cell
+    uint32_t *temp;            // scan scratch
+    int      *box;             // [6] bounding box, min then max per axis (ordered-int floats)
+    int      *perm;            // [cap] the order: perm[position] = body
+    int       cap;
+    bool      stable;          // stable radix sort (timing-independent order) instead of atomics
+};
+constexpr int kOrderBits = 6;                                   // cell index bits per axis
+constexpr uint32_t kOrderBins = 1u << (3 * kOrderBits);         // cells; one more for removed bodies
+cudaError_t order_alloc(OrderScratch& o, int cap, bool stable);
+void order_free(OrderScratch& o);
+// Orders bodies [first, first + n) of s by the Morton code of their cell on a grid over
+// their bounding box (64^3 cells; 32^3 and equal codes in index order when o is stable):
+// perm[position] = body - first and, when inv is given, inv[body - first] = position.  With
+// dead_last, bodies with N == 0 come last.  Stream-ordered.
+cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, const OrderScratch& o, int* perm,
+                         int* inv, cudaStream_t st);
 
 // Stage scratch for the massive set.  Positions of the four RK4 stages are kept as
 // {x, y, z, m} records for the FP64 dust kernels.  The mixed path also keeps an FP32
@@ -84,10 +107,26 @@ struct MassiveScratch {
     double   *part;   // [slices][6][n_grav rounded to 256] per-slice sums of the mixed passes
                       // (null: one warp per target instead)
     long long part_words;
+    // Spatial order of the mixed dust kernel (all null: index order, every span near).
+    int      *slot;      // [cap] pair slot of FP32 source k (body n_exact + k), in cell order
+    OrderScratch src_order;    // ordering of the FP32 sources (cap bodies)
+    OrderScratch dust_order;   // ordering of the tracers of one dust launch
 };
 
 // Bits of the device status word.
 constexpr int kStatusTimeout = 1;   // a bounded mbarrier wait gave up
+
+// FP64 -> FP32 toward zero with integer operations only (FP64 instructions, conversions
+// included, issue at 1/64 of the FP32 rate on sm_103a): +-0 below the FP32 normals, +-inf
+// beyond the FP32 range and for inf or NaN; the error is below 2^-23 |v|.
+__device__ __forceinline__ float d2f_toward0(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023;
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    if (e < -126) return __uint_as_float(sign);
+    if (e > 127) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu));
+}
 
 __device__ __forceinline__ void split_hilo(double v, float& hi, float& lo) {
     hi = __double2float_rn(v);

@@ -92,7 +92,7 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     int r = scratch_address(device, &base);
     if (r) return r;
 
-    MassiveScratch ms;
+    MassiveScratch ms{};   // no spatial order here: slot and the order scratch stay null
     ms.P = reinterpret_cast<Body*>(base + kOffP);
     ms.Phi = reinterpret_cast<float4*>(base + kOffPhi);
     ms.Plo = reinterpret_cast<float4*>(base + kOffPlo);

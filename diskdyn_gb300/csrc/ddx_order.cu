@@ -1,0 +1,272 @@
+// Cell order of a set of bodies (no counterpart in the reference).  The mixed dust kernel
+// reads its FP32 sources, and visits its tracers, in this order, so that the sources of a
+// span of pair records and the tracers of a warp each lie in a small region, and a tracer
+// far from a span can take the separation from the high parts alone.
+//
+// The order: the bodies' bounding box (in FP32), a cell index per axis inside it, and the
+// Morton code of the cell (x, y, z bits interleaved, so cells close on the curve are close
+// in space), sorted in one of two ways:
+//  - counting sort (the tracers: 6 bits per axis): an atomic increment gives each body its
+//    rank in its cell, an exclusive scan of the cell counts the cells' first positions, and
+//    perm[start + rank] = body.  The order inside a cell follows the atomics, which is
+//    fine for the tracers: each tracer's result depends on its own data and the sources;
+//  - stable LSD radix sort of (code, index), 8-bit digits (the sources: 5 bits per axis).
+//    The sources' order is the order of the FP32 sums over them, so it must not depend on
+//    timing: equal codes keep their index order.  Per digit pass: every block counts the
+//    digits of its tile, digit-major; an exclusive scan gives every (digit, block) its first
+//    output slot; the scatter ranks equal digits inside a warp with __match_any_sync and
+//    orders warps and rounds by counts in shared memory.
+#include "ddx_internal.cuh"
+#include "ddx_scan.cuh"
+
+namespace ddx {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 8;                       // keys per thread in a radix pass
+constexpr int kSortTile = kThreads * kItems;
+
+// Floats as ints with the same order (for atomicMin / atomicMax), and back.
+__device__ __forceinline__ int ord_of(float f) {
+    const int b = __float_as_int(f);
+    return b >= 0 ? b : b ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float float_of(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7FFFFFFF); }
+
+__device__ __forceinline__ bool removed(const ddx_state& s, int i) {
+    return (((unsigned long long)__double_as_longlong(s.N[i])) << 1) == 0ull;   // N == +-0
+}
+
+__global__ void order_init_kernel(uint32_t* __restrict__ count, int* __restrict__ box) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k <= kOrderBins) count[k] = 0;
+    if (k < 3) {
+        box[k] = ord_of(INFINITY);
+        box[3 + k] = ord_of(-INFINITY);
+    }
+}
+
+// Bounding box of the bodies' FP32 positions (NaN left out): a block reduction, then one
+// atomic per block and bound.
+__global__ void order_box_kernel(ddx_state s, int first, int n, bool dead_last, int* __restrict__ box) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (k < n && !(dead_last && removed(s, first + k))) {
+        const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]), d2f_toward0(s.z[first + k])};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], v[a]);
+            hi[a] = fmaxf(hi[a], v[a]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    __shared__ float red[kThreads / 32][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) { red[warp][a] = lo[a]; red[warp][3 + a] = hi[a]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        float v = red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            v = threadIdx.x < 3 ? fminf(v, red[w][threadIdx.x]) : fmaxf(v, red[w][threadIdx.x]);
+        if (threadIdx.x < 3) atomicMin(&box[threadIdx.x], ord_of(v));
+        else atomicMax(&box[threadIdx.x], ord_of(v));
+    }
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {   // bit b of v to bit 3b
+    uint32_t r = 0;
+#pragma unroll
+    for (int b = 0; b < kOrderBits; ++b) r |= ((v >> b) & 1u) << (3 * b);
+    return r;
+}
+
+// Morton code of each body's cell (bits per axis; removed bodies get 1 << 3 bits when
+// dead_last).  count given: rank[k] = the body's rank in its cell by an atomic increment;
+// else rank[k] = k (the values of the stable sort).
+__global__ void order_keys_kernel(ddx_state s, int first, int n, bool dead_last, int bits, const int* __restrict__ box,
+                                  uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
+                                  uint32_t* __restrict__ count) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int cells = 1 << bits;
+    uint32_t bin = 1u << (3 * bits);
+    if (!(dead_last && removed(s, first + k))) {
+        const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]), d2f_toward0(s.z[first + k])};
+        uint32_t c[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float lo = float_of(box[a]), hi = float_of(box[3 + a]);
+            const float scale = hi > lo ? (float)cells / (hi - lo) : 0.0f;
+            // NaN, or a span too wide for FP32, gives cell 0 or the last: any cell is valid
+            const float u = fminf(fmaxf((v[a] - lo) * scale, 0.0f), (float)(cells - 1));
+            c[a] = (uint32_t)(u == u ? (int)u : 0);
+        }
+        bin = spread3(c[0]) << 2 | spread3(c[1]) << 1 | spread3(c[2]);
+    }
+    key[k] = bin;
+    rank[k] = count ? atomicAdd(&count[bin], 1u) : (uint32_t)k;
+}
+
+__global__ void hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, uint32_t* __restrict__ hist,
+                            int nblocks) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+    for (int r = 0; r < kItems; ++r) {
+        const int e = base + r * kThreads + threadIdx.x;
+        if (e < n) atomicAdd(&cnt[(keys[e] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void radix_scatter_kernel(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                     uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int n, int shift,
+                                     const uint32_t* __restrict__ offs, int nblocks) {
+    __shared__ uint32_t wcnt[kThreads / 32][257];
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t gofs[256];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    run[t] = 0;
+    gofs[t] = offs[t * nblocks + blockIdx.x];
+    for (int w = 0; w < kThreads / 32; ++w) wcnt[w][t] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+    for (int r = 0; r < kItems; ++r) {
+        const int e = base + r * kThreads + t;
+        const bool valid = e < n;
+        uint32_t key = 0, val = 0, d = 256;
+        if (valid) { key = kin[e]; val = vin[e]; d = (key >> shift) & 255u; }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        {   // thread t owns digit t: exclusive offsets over the warps, then the running total
+            uint32_t acc = run[t];
+            for (int w = 0; w < kThreads / 32; ++w) {
+                const uint32_t c = wcnt[w][t];
+                wcnt[w][t] = acc;
+                acc += c;
+            }
+            run[t] = acc;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = gofs[d] + wcnt[warp][d] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        for (int w = 0; w < kThreads / 32; ++w) wcnt[w][t] = 0;
+        __syncthreads();
+    }
+}
+
+// Words of radix_sort_stable's scratch for n keys.
+size_t radix_temp_words(int n) {
+    const int nb = (n + kSortTile - 1) / kSortTile;
+    const int nh = 256 * (nb > 0 ? nb : 1);
+    return 2 * (size_t)nh + scan_temp_words(nh) + 2 * (size_t)n + 16;
+}
+
+// Stable ascending sort of (keys, vals) by the low key_bits bits of the keys; the result is
+// in (keys, vals) or in the scratch, returned through *ko / *vo.
+cudaError_t radix_sort_stable(uint32_t* keys, uint32_t* vals, int n, int key_bits, uint32_t* temp,
+                              uint32_t** ko, uint32_t** vo, cudaStream_t st) {
+    const int nb = (n + kSortTile - 1) / kSortTile;
+    const int nh = 256 * nb;
+    uint32_t* hist = temp;
+    uint32_t* offs = hist + nh;
+    uint32_t* stmp = offs + nh;
+    uint32_t* k2 = stmp + scan_temp_words(nh);
+    uint32_t* v2 = k2 + n;
+    uint32_t *ka = keys, *va = vals, *kb = k2, *vb = v2;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        hist_kernel<<<nb, kThreads, 0, st>>>(ka, n, shift, hist, nb);
+        const cudaError_t e = exclusive_scan(hist, offs, nh, stmp, nullptr, st);
+        if (e != cudaSuccess) return e;
+        radix_scatter_kernel<<<nb, kThreads, 0, st>>>(ka, va, kb, vb, n, shift, offs, nb);
+        uint32_t* tk = ka; ka = kb; kb = tk;
+        uint32_t* tv = va; va = vb; vb = tv;
+    }
+    *ko = ka;
+    *vo = va;
+    return cudaGetLastError();
+}
+
+__global__ void order_from_sorted_kernel(int n, const uint32_t* __restrict__ sorted, int* __restrict__ perm,
+                                         int* __restrict__ inv) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t k = sorted[p];
+    if (perm) perm[p] = (int)k;
+    if (inv) inv[k] = p;
+}
+
+__global__ void order_scatter_kernel(int n, const uint32_t* __restrict__ key, const uint32_t* __restrict__ rank,
+                                     const uint32_t* __restrict__ start, int* __restrict__ perm,
+                                     int* __restrict__ inv) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t pos = start[key[k]] + rank[k];
+    if (perm) perm[pos] = k;
+    if (inv) inv[k] = (int)pos;
+}
+
+}  // namespace
+
+cudaError_t order_alloc(OrderScratch& o, int cap, bool stable) {
+    OrderScratch n{};
+    n.cap = cap;
+    n.stable = stable;
+    const size_t bins = kOrderBins + 1;
+    const size_t tw = stable ? radix_temp_words(cap) : scan_temp_words((int)bins);
+    if (cudaMalloc(&n.key, 4ull * cap) || cudaMalloc(&n.rank, 4ull * cap) || cudaMalloc(&n.perm, 4ull * cap) ||
+        cudaMalloc(&n.count, 4 * bins) || cudaMalloc(&n.start, 4 * bins) || cudaMalloc(&n.temp, 4 * tw) ||
+        cudaMalloc(&n.box, 6 * sizeof(int))) {
+        order_free(n);
+        return cudaErrorMemoryAllocation;
+    }
+    order_free(o);
+    o = n;
+    return cudaSuccess;
+}
+
+void order_free(OrderScratch& o) {
+    cudaFree(o.key); cudaFree(o.rank); cudaFree(o.perm); cudaFree(o.count); cudaFree(o.start);
+    cudaFree(o.temp); cudaFree(o.box);
+    o = OrderScratch{};
+}
+
+cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, const OrderScratch& o, int* perm,
+                         int* inv, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > o.cap) return cudaErrorInvalidValue;
+    const int blk = (n + kThreads - 1) / kThreads;
+    order_init_kernel<<<(kOrderBins + 1 + kThreads - 1) / kThreads, kThreads, 0, st>>>(o.count, o.box);
+    order_box_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, o.box);
+    if (o.stable) {
+        constexpr int kBits = kOrderBits - 1;   // 32^3 cells: two 8-bit digit passes
+        order_keys_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, kBits, o.box, o.key, o.rank, nullptr);
+        uint32_t *ko = nullptr, *vo = nullptr;
+        cudaError_t e = radix_sort_stable(o.key, o.rank, n, 3 * kBits + 1, o.temp, &ko, &vo, st);
+        if (e != cudaSuccess) return e;
+        order_from_sorted_kernel<<<blk, kThreads, 0, st>>>(n, vo, perm, inv);
+        return cudaGetLastError();
+    }
+    order_keys_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, kOrderBits, o.box, o.key, o.rank, o.count);
+    cudaError_t e = exclusive_scan(o.count, o.start, (int)kOrderBins + 1, o.temp, nullptr, st);
+    if (e != cudaSuccess) return e;
+    order_scatter_kernel<<<blk, kThreads, 0, st>>>(n, o.key, o.rank, o.start, perm, inv);
+    return cudaGetLastError();
+}
+
+}  // namespace ddx

@@ -25,23 +25,29 @@ namespace ddx {
 
 constexpr float kFarAway = 1.0e18f;  // padding source position, AU (mass 0)
 
-// FP32 source q = i - n_exact (body i >= n_exact) into its half of pair record q/2 of a
-// stage.
-__device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, int q, const float4 h,
+// FP32 source k = i - n_exact (body i >= n_exact) into its slot q of the pair records of a
+// stage: half q & 1 of record q / 2.  The slots follow the sources' cell order when one
+// was made for this step (ms.slot), else q = k.
+__device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, int k, const float4 h,
                                                 const float4 l) {
+    const int q = ms.slot ? ms.slot[k] : k;
     BodyPair* r = ms.PP + (size_t)stage * ms.pcap + (q >> 1);
-    const int k = q & 1;
-    r->hx[k] = h.x; r->hy[k] = h.y; r->hz[k] = h.z; r->m[k] = h.w;
-    r->lx[k] = l.x; r->ly[k] = l.y; r->lz[k] = l.z; r->pad[k] = 0.f;
+    const int u = q & 1;
+    r->hx[u] = h.x; r->hy[u] = h.y; r->hz[u] = h.z; r->m[u] = h.w;
+    r->lx[u] = l.x; r->ly[u] = l.y; r->lz[u] = l.z; r->pad[u] = 0.f;
 }
 
 // Zero-mass, far-away filler for the slots past the last FP32 source, so the dust kernel
 // always processes whole spans of kPairSpan records.
 __device__ __forceinline__ void store_pair_padding(MassiveScratch& ms, int n_src) {
     const int np = pair_count(n_src);
-    const float4 h = make_float4(kFarAway, kFarAway, kFarAway, 0.f), l = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int stage = 0; stage < 4; ++stage)
-        for (int q = n_src; q < 2 * np; ++q) store_pair_slot(ms, stage, q, h, l);
+        for (int q = n_src; q < 2 * np; ++q) {
+            BodyPair* r = ms.PP + (size_t)stage * ms.pcap + (q >> 1);
+            const int k = q & 1;
+            r->hx[k] = kFarAway; r->hy[k] = kFarAway; r->hz[k] = kFarAway; r->m[k] = 0.f;
+            r->lx[k] = 0.f; r->ly[k] = 0.f; r->lz[k] = 0.f; r->pad[k] = 0.f;
+        }
 }
 
 // P1 = x, P2 = x + v dt/2 (src/gpu_functions.cu:90-99, 219-230).
@@ -540,6 +546,12 @@ dust_rk4_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __res
 
 cudaError_t launch_massive_prepare(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                    int precision, cudaStream_t st) {
+    // the FP32 sources' pair slots in cell order, from their positions at the start of the step
+    if (precision == DDX_PREC_MIXED && ms.slot) {
+        const cudaError_t e =
+            order_bodies(s, a.n_exact, a.n_grav - a.n_exact, false, ms.src_order, nullptr, ms.slot, st);
+        if (e != cudaSuccess) return e;
+    }
     const int threads = 128;
     const int blocks = (a.n_grav + threads - 1) / threads;
     massive_prepare_kernel<<<blocks, threads, 0, st>>>(s, a, ms, precision);

@@ -115,7 +115,12 @@ int ddx_set_optics(ddx_ctx *ctx, int n_grid, int n_wav, int n_theta, const doubl
  * optional Lorentz force and the gravity of every massive body, then the massive
  * combination.  Equivalent to the reference's
  *     massive_RK4(dt); small_RK4(dt); massive_final(dt);   (src/grid.cu:387-389)
- * The size table must be set.  `precision` is DDX_PREC_*, `mode` is DDX_MODE_*. */
+ * The size table must be set.  `precision` is DDX_PREC_*, `mode` is DDX_MODE_*.
+ * DDX_PREC_MIXED visits the tracers and reads the FP32 planetesimals in a spatial order
+ * (Morton cells) and takes planetesimals farther from a tracer than its largest
+ * coordinate with the FP32 high parts alone; each tracer's result depends on its own data
+ * and the massive set only (not on the other tracers or their order), and the result is
+ * the same from run to run. */
 int ddx_step(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
              const ddx_phys *phys, int precision, int mode, void *stream);
 
@@ -148,7 +153,11 @@ int ddx_evolve(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double 
  * fixed size (about 12 MiB), which every GPU that loads the library holds until the
  * process exits.  It takes at most DDX_NOALLOC_MAX_GRAV massive bodies and
  * DDX_MAX_SIZE_BINS size bins and answers DDX_ERR_RANGE beyond that.  beta, betasw and q
- * are device pointers with n_grid entries; everything else is as for ddx_step.
+ * are device pointers with n_grid entries; everything else is as for ddx_step.  In FP64
+ * the results equal ddx_step's to the bit.  In DDX_PREC_MIXED the spatial order needs
+ * scratch that grows with n_dust, so this entry point reads the planetesimals in index
+ * order and always with the full hi/lo separation: its results agree with ddx_step's to
+ * the rounding of the FP32 perturbations.
  *
  * The first call on a device resolves the array's device address (cudaGetSymbolAddress
  * with that device current).  Make that first call before any stream capture.  All

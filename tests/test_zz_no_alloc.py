@@ -4,9 +4,12 @@ Those callers -- a host inside a framework whose pool allocator owns the device 
 or a loop that must keep a fixed device footprint -- get a step whose scratch is a fixed
 file-scope device array instead of cudaMalloc'd context buffers.  The test calls it
 through the C ABI twice in a row (the second call reuses the array the first one left
-behind) and checks every result against ddx_step on the same input, bit for bit, since
-both run the same kernels.  It passes alone in a fresh process and after the other
-tests.
+behind) and checks every result against ddx_step on the same input: bit for bit in FP64,
+where both run the same kernels.  In mixed precision the context's step visits the
+tracers and the sources in a spatial order and takes far sources with the high-part
+separation, which the fixed array has no room to order for; the positions and velocities
+then agree to 1e-12 of the largest position or velocity component after two steps, and
+the removed tracers are the same.  It passes alone in a fresh process and after the other tests.
 """
 import ctypes as C
 
@@ -46,7 +49,13 @@ def test_noalloc_step_matches_ddx_step_twice(built_lib, prec, mode):
         noalloc_step(lib, b, sysm, tab, prec, mode)
         torch.cuda.synchronize()
         for f in ("x", "y", "z", "vx", "vy", "vz", "N"):
-            assert torch.equal(getattr(a, f), getattr(b, f)), f
+            if prec == abi.DDX_PREC_FP64 or f == "N":
+                assert torch.equal(getattr(a, f), getattr(b, f)), f
+            else:
+                group = ("x", "y", "z") if f in ("x", "y", "z") else ("vx", "vy", "vz")
+                scale = max(float(getattr(a, g).abs().max()) for g in group)
+                u, v = getattr(a, f), getattr(b, f)
+                assert float((u - v).abs().max()) <= 1e-12 * scale, f
     eng.close()
 
 
