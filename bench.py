@@ -34,10 +34,11 @@ WORKLOAD = "dusty_ring"
 # star term (gravity reduced by beta + PR/stellar-wind drag), per tracer per stage.
 FLOP_PAIR = 20
 FLOP_STAR = 45
-# Mixed dust kernel, bytes per grain and launch: DRAM traffic measured by ncu (30.8 MB for
-# 262,144 grains), and the algorithmic bytes (the state read, 68 B, and the positions,
-# velocities and grain number written, 56 B).
-DUST_TRAFFIC_PER_GRAIN = 30.8e6 / 262144
+# Mixed dust kernel, bytes per grain and launch: DRAM traffic measured by ncu (19.46 MB read
+# + 0.29 MB written for 262,144 grains; the written state stays in L2 past the launch), and
+# the algorithmic bytes (the state read, 68 B, and the positions, velocities and grain
+# number written, 56 B).
+DUST_TRAFFIC_PER_GRAIN = (19.46e6 + 0.29e6) / 262144
 ALG_BYTES_PER_GRAIN = 68 + 56
 
 
@@ -317,14 +318,16 @@ def run_ours(args, world, rank, local):
                      "flops_per_launch": flops, "dust_kernel_ms": t_dust * 1e3,
                      "fp64_peak_tflops": fp64_peak,
                      # DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
-                     # one 262,144-grain launch of this kernel (18.4 MB + 12.4 MB, the same 4,099
-                     # massive bodies), scaled by the grains to a 1,048,576-grain launch
+                     # one 262,144-grain launch of this kernel (the same 4,099 massive bodies),
+                     # scaled by the grains to a 1,048,576-grain launch
                      "traffic": DUST_TRAFFIC_PER_GRAIN * nd,
                      "traffic_source": "ncu capture of a 262,144-grain launch, scaled by the grains",
                      "algorithmic_bytes": ALG_BYTES_PER_GRAIN * nd,
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 6 * args.steps,      # prepare, 2 x (slice sums + gather), dust
+        # per step: planetesimal order (14), prepare, 2 x (slice sums + gather), tracer order
+        # (7), span boxes, dust
+        "gpu_launches": 28 * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and args.adjoint_steps > 0:
