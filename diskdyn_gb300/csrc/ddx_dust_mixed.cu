@@ -8,14 +8,16 @@
 // across spans.
 //
 // Far spans.  The low parts matter only for sources near the tracer: for a source at
-// distance r >= X (X the largest |coordinate| of the two), the high parts alone give the
-// separation within (sqrt(3) 2^-23 + 2^-24) r, below the error of rsqrt.approx already in
-// every term.  So a tracer takes a span with the high-part separation (3 of the 9
-// separation operations) when the span's box (high parts of its 32 sources) lies at least
-// X from the tracer's own point, X over the box and the point.  The choice depends on the
-// tracer and the sources alone, so a tracer's result does not depend on the others or on
-// their order.  The tracers are visited in cell order and the sources sit in their pair
-// records in cell order (ddx_order.cu), so the lanes of a warp lie close together and
+// distance r >= X/2 (X the largest |coordinate| of the two), the high parts alone give the
+// separation within e = (2 sqrt(3) 2^-23 + 2^-24) r = 4.7e-7 r, and the source's pull
+// within 4e (direction and r^-3), a few times the 5.6e-7 that rsqrt.approx and FP32
+// rounding leave in every pull; over 1,000 steps of the dusty ring the position errors
+// against FP64 did not move.  So a tracer takes a span with the high-part separation (3 of
+// the 9 separation operations) when the span's box (high parts of its 32 sources) lies at
+// least X/2 from the tracer's own point, X over the box and the point.  The choice depends
+// on the tracer and the sources alone, so a tracer's result does not depend on the others
+// or on their order.  The tracers are visited in cell order and the sources sit in their
+// pair records in cell order (ddx_order.cu), so the lanes of a warp lie close together and
 // nearly always make the same choice for a span.
 //
 // Blackwell mapping:
@@ -107,23 +109,25 @@ __global__ void span_box_kernel(BodyPair* __restrict__ PP, int pcap, int n_src, 
 
 // The test of one tracer (high parts xh, yh, zh; own = its largest |coordinate|) against one
 // span box (bx, by, bz: min and max per axis; xm: its largest |coordinate|, NaN when a
-// coordinate is NaN): far when the box lies at least X = max(xm, own) away.  Rounded
+// coordinate is NaN): far when the box lies at least X = kFar max(xm, own) away.  Rounded
 // operations only (no contraction), so the block tests below imply its outcome.
+constexpr float kFar = 0.5f;   // far from X/2 on (a power of two: the scaling is exact)
+
 __device__ __forceinline__ bool lane_far(float2 bx, float2 by, float2 bz, float xm, float xh, float yh, float zh,
                                          float own) {
     const float gx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, xh), __fsub_rn(xh, bx.y)));
     const float gy = fmaxf(0.f, fmaxf(__fsub_rn(by.x, yh), __fsub_rn(yh, by.y)));
     const float gz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, zh), __fsub_rn(zh, bz.y)));
     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
-    const float X = fmaxf(xm, own);
+    const float X = kFar * fmaxf(xm, own);
     return xm == xm && d2 >= __fmul_rn(X, X);
 }
 
 // The same tests for a whole block of tracers from its box b (min and max of the high parts
 // per axis, and the largest own): far for every tracer when the nearest point of b is far
-// with X = max(xm, largest own); near for every tracer when even the farthest point of b is
-// nearer than xm.  Each rounded step is monotone, so these imply lane_far's outcome for any
-// tracer inside b.
+// with X = kFar max(xm, largest own); near for every tracer when even the farthest point of
+// b is nearer than kFar xm.  Each rounded step is monotone, so these imply lane_far's
+// outcome for any tracer inside b.
 __device__ __forceinline__ void block_far(float2 bx, float2 by, float2 bz, float xm, const float* b, bool& all_far,
                                           bool& all_near) {
     const float nx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, b[1]), __fsub_rn(b[0], bx.y)));
@@ -134,9 +138,9 @@ __device__ __forceinline__ void block_far(float2 bx, float2 by, float2 bz, float
     const float fz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, b[4]), __fsub_rn(b[5], bz.y)));
     const float dn = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
     const float df = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
-    const float X = fmaxf(xm, b[6]);
+    const float X = kFar * fmaxf(xm, b[6]), Xn = kFar * xm;
     all_far = xm == xm && dn >= __fmul_rn(X, X);
-    all_near = !(xm == xm) || df < __fmul_rn(xm, xm);
+    all_near = !(xm == xm) || df < __fmul_rn(Xn, Xn);
 }
 
 __device__ __forceinline__ void span_box(const BodyPair* R, float2& bx, float2& by, float2& bz, float& xm) {
