@@ -325,9 +325,9 @@ def run_ours(args, world, rank, local):
                      "algorithmic_bytes": ALG_BYTES_PER_GRAIN * nd,
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        # per step: planetesimal order (14), prepare, 2 x (slice sums + gather), tracer order
-        # (7), span boxes, dust
-        "gpu_launches": 28 * args.steps,
+        # per step: planetesimal order (one block up to 8,192 planetesimals, else 14 launches of
+        # the radix sort), prepare, 2 x (slice sums + gather), tracer order (7), span boxes, dust
+        "gpu_launches": ((1 if args.n_plsml <= 8192 else 14) + 14) * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and args.adjoint_steps > 0:

@@ -10,12 +10,14 @@
 //    rank in its cell, an exclusive scan of the cell counts the cells' first positions, and
 //    perm[start + rank] = body.  The order inside a cell follows the atomics, which is
 //    fine for the tracers: each tracer's result depends on its own data and the sources;
-//  - stable LSD radix sort of (code, index), 8-bit digits (the sources: 5 bits per axis).
-//    The sources' order is the order of the FP32 sums over them, so it must not depend on
-//    timing: equal codes keep their index order.  Per digit pass: every block counts the
+//  - sorted by (code, index) (the sources: 5 bits per axis).  The sources' order is the
+//    order of the FP32 sums over them, so it must not depend on timing: equal codes keep
+//    their index order.  Up to 8,192 bodies one block does it all (box, keys, a bitonic sort
+//    of code << 13 | index in shared memory, the slots), in one launch; beyond that a stable
+//    LSD radix sort of (code, index) with 8-bit digits: per digit pass every block counts the
 //    digits of its tile, digit-major; an exclusive scan gives every (digit, block) its first
 //    output slot; the scatter ranks equal digits inside a warp with __match_any_sync and
-//    orders warps and rounds by counts in shared memory.
+//    orders warps and rounds by counts in shared memory.  Both give the same order.
 #include "ddx_internal.cuh"
 #include "ddx_scan.cuh"
 
@@ -87,6 +89,86 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v) {   // bit b of v to bit
     return r;
 }
 
+// Morton code of the cell of v on a (1 << bits)^3 grid over the box [lo, hi] per axis.
+__device__ __forceinline__ uint32_t cell_code(const float* v, const float* lo, const float* hi, int bits) {
+    const int cells = 1 << bits;
+    uint32_t c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float scale = hi[a] > lo[a] ? (float)cells / (hi[a] - lo[a]) : 0.0f;
+        // NaN, or a span too wide for FP32, gives cell 0 or the last: any cell is valid
+        const float u = fminf(fmaxf((v[a] - lo[a]) * scale, 0.0f), (float)(cells - 1));
+        c[a] = (uint32_t)(u == u ? (int)u : 0);
+    }
+    return spread3(c[0]) << 2 | spread3(c[1]) << 1 | spread3(c[2]);
+}
+
+// The whole stable order of up to kSmallOrder bodies in one block.
+constexpr int kSmallOrder = 8192;        // index < 2^13 below the 15-bit code + removed bit
+constexpr int kSmallThreads = 1024;
+__global__ void __launch_bounds__(kSmallThreads)
+order_small_kernel(ddx_state s, int first, int n, bool dead_last, int* __restrict__ perm, int* __restrict__ inv) {
+    __shared__ uint32_t keys[kSmallOrder];
+    __shared__ float red[kSmallThreads / 32][6];
+    __shared__ float box[6];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    constexpr int kBits = kOrderBits - 1;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = t; k < n; k += kSmallThreads) {
+        if (dead_last && removed(s, first + k)) continue;
+        const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]), d2f_toward0(s.z[first + k])};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { lo[a] = fminf(lo[a], v[a]); hi[a] = fmaxf(hi[a], v[a]); }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) { red[warp][a] = lo[a]; red[warp][3 + a] = hi[a]; }
+    __syncthreads();
+    if (t < 6) {
+        float v = red[0][t];
+        for (int w = 1; w < kSmallThreads / 32; ++w) v = t < 3 ? fminf(v, red[w][t]) : fmaxf(v, red[w][t]);
+        box[t] = v;
+    }
+    __syncthreads();
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int k = t; k < m; k += kSmallThreads) {
+        uint32_t key = 0xFFFFFFFFu;   // padding sorts last
+        if (k < n) {
+            uint32_t code = 1u << (3 * kBits);
+            if (!(dead_last && removed(s, first + k))) {
+                const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]),
+                                    d2f_toward0(s.z[first + k])};
+                code = cell_code(v, box, box + 3, kBits);
+            }
+            key = code << 13 | (uint32_t)k;
+        }
+        keys[k] = key;
+    }
+    __syncthreads();
+    // bitonic sort, ascending, of the m keys (all distinct)
+    for (int size = 2; size <= m; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = t; i < m / 2; i += kSmallThreads) {
+                const int a = 2 * i - (i & (stride - 1)), b = a + stride;
+                const uint32_t ka = keys[a], kb = keys[b];
+                if ((ka > kb) == ((a & size) == 0)) { keys[a] = kb; keys[b] = ka; }
+            }
+            __syncthreads();
+        }
+    for (int p = t; p < n; p += kSmallThreads) {
+        const int k = (int)(keys[p] & 0x1FFFu);
+        if (perm) perm[p] = k;
+        if (inv) inv[k] = p;
+    }
+}
+
 // Morton code of each body's cell (bits per axis; removed bodies get 1 << 3 bits when
 // dead_last).  count given: rank[k] = the body's rank in its cell by an atomic increment;
 // else rank[k] = k (the values of the stable sort).
@@ -95,20 +177,12 @@ __global__ void order_keys_kernel(ddx_state s, int first, int n, bool dead_last,
                                   uint32_t* __restrict__ count) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const int cells = 1 << bits;
     uint32_t bin = 1u << (3 * bits);
     if (!(dead_last && removed(s, first + k))) {
         const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]), d2f_toward0(s.z[first + k])};
-        uint32_t c[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float lo = float_of(box[a]), hi = float_of(box[3 + a]);
-            const float scale = hi > lo ? (float)cells / (hi - lo) : 0.0f;
-            // NaN, or a span too wide for FP32, gives cell 0 or the last: any cell is valid
-            const float u = fminf(fmaxf((v[a] - lo) * scale, 0.0f), (float)(cells - 1));
-            c[a] = (uint32_t)(u == u ? (int)u : 0);
-        }
-        bin = spread3(c[0]) << 2 | spread3(c[1]) << 1 | spread3(c[2]);
+        const float lo[3] = {float_of(box[0]), float_of(box[1]), float_of(box[2])};
+        const float hi[3] = {float_of(box[3]), float_of(box[4]), float_of(box[5])};
+        bin = cell_code(v, lo, hi, bits);
     }
     key[k] = bin;
     rank[k] = count ? atomicAdd(&count[bin], 1u) : (uint32_t)k;
@@ -250,6 +324,10 @@ cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, c
                          int* inv, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > o.cap) return cudaErrorInvalidValue;
+    if (o.stable && n <= kSmallOrder) {
+        order_small_kernel<<<1, kSmallThreads, 0, st>>>(s, first, n, dead_last, perm, inv);
+        return cudaGetLastError();
+    }
     const int blk = (n + kThreads - 1) / kThreads;
     order_init_kernel<<<(kOrderBins + 1 + kThreads - 1) / kThreads, kThreads, 0, st>>>(o.count, o.box);
     order_box_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, o.box);
