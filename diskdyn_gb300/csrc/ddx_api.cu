@@ -390,13 +390,13 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
     if (!d2h_range(*out, *s, 0, n_grav, st)) return DDX_ERR_CUDA;
     // the dust, chunk by chunk: copy-in stream -> compute stream -> copy-out stream.  The
     // reference mode's stage-4 write lands at the chunk's own index, so it runs unchunked.
-    // So does the spatially ordered mixed step (planetesimals present): a chunk is a range
+    // So does the spatially ordered mixed step (enough planetesimals): a chunk is a range
     // of indices, which covers the whole disk at a fraction of its density, so the chunks'
     // orders give looser boxes and fewer far spans, and every chunk repeats the order and
     // the span boxes.  Measured on the dusty ring, three chunks cost more (10.2 ms a step)
     // than the copies they hide: one chunk has its copy in overlapped with the massive set's
     // work and only the copy out exposed (0.3 ms).
-    const bool ordered = precision == DDX_PREC_MIXED && n_grav > a.n_exact;
+    const bool ordered = precision == DDX_PREC_MIXED && spatial_order_on(a);
     const std::vector<int> chunks =
         a.mode == DDX_MODE_REFERENCE || ordered ? std::vector<int>{n_dust} : dust_chunks(n_dust);
     int o = 0;

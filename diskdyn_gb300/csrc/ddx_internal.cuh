@@ -90,6 +90,15 @@ void order_free(OrderScratch& o);
 cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, const OrderScratch& o, int* perm,
                          int* inv, cudaStream_t st);
 
+// The mixed step orders its tracers and FP32 sources in space (far spans, ddx_order.cu)
+// from this many sources on.  With fewer, the dust kernel is short and the orders and span
+// boxes (about 60 us a step) cost more than the far spans save: with 256 planetesimals and
+// 262,144 grains a step took 0.15 ms longer.
+constexpr int kOrderMinSources = 1024;
+__host__ __device__ inline bool spatial_order_on(const StepArgs& a) {
+    return a.n_grav - a.n_exact >= kOrderMinSources;
+}
+
 // Stage scratch for the massive set.  Positions of the four RK4 stages are kept as
 // {x, y, z, m} records for the FP64 dust kernels.  The mixed path also keeps an FP32
 // hi/lo split of each stage position, per body (Phi/Plo, for the massive passes) and in

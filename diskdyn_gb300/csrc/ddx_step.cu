@@ -50,6 +50,14 @@ __device__ __forceinline__ void store_pair_padding(MassiveScratch& ms, int n_src
         }
 }
 
+// The scratch as the kernels of a step see it: the pair slots in cell order only when the
+// step orders its sources (else slot k holds source k).
+static MassiveScratch slotted(const MassiveScratch& ms, const StepArgs& a) {
+    MassiveScratch m = ms;
+    if (!spatial_order_on(a)) m.slot = nullptr;
+    return m;
+}
+
 // P1 = x, P2 = x + v dt/2 (src/gpu_functions.cu:90-99, 219-230).
 __global__ void massive_prepare_kernel(ddx_state s, StepArgs a, MassiveScratch ms, int prec) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -547,14 +555,14 @@ dust_rk4_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __res
 cudaError_t launch_massive_prepare(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                    int precision, cudaStream_t st) {
     // the FP32 sources' pair slots in cell order, from their positions at the start of the step
-    if (precision == DDX_PREC_MIXED && ms.slot) {
+    if (precision == DDX_PREC_MIXED && ms.slot && spatial_order_on(a)) {
         const cudaError_t e =
             order_bodies(s, a.n_exact, a.n_grav - a.n_exact, false, ms.src_order, nullptr, ms.slot, st);
         if (e != cudaSuccess) return e;
     }
     const int threads = 128;
     const int blocks = (a.n_grav + threads - 1) / threads;
-    massive_prepare_kernel<<<blocks, threads, 0, st>>>(s, a, ms, precision);
+    massive_prepare_kernel<<<blocks, threads, 0, st>>>(s, a, slotted(ms, a), precision);
     return cudaGetLastError();
 }
 
@@ -588,10 +596,10 @@ cudaError_t launch_sliced(const ddx_state& s, const StepArgs& a, MassiveScratch&
     if (S > 0) {
         const int per = (spans + S - 1) / S * kPairSpan;
         const dim3 grid((a.n_grav + kSliceThreads - 1) / kSliceThreads + 1, S);   // + the star's row
-        massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, ms, PASS == 1 ? 0 : 2, per, np, ms.part);
+        massive_slice_kernel<<<grid, kSliceThreads, 0, st>>>(a, slotted(ms, a), PASS == 1 ? 0 : 2, per, np, ms.part);
     }
     massive_gather_kernel<PASS><<<(a.n_grav + kGatherTargets - 1) / kGatherTargets, kGatherThreads, 0, st>>>(
-        s, a, ms, S, np, ms.part);
+        s, a, slotted(ms, a), S, np, ms.part);
     return cudaGetLastError();
 }
 }  // namespace
@@ -617,7 +625,8 @@ cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveS
     if (precision == DDX_PREC_MIXED && sliced_fits(a, ms)) return launch_sliced<1>(s, a, ms, st);
     const int threads = 128;  // 4 targets per block
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
-    if (precision == DDX_PREC_MIXED) massive_pass1_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
+    if (precision == DDX_PREC_MIXED)
+        massive_pass1_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, slotted(ms, a));
     else massive_pass1_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
     return cudaGetLastError();
 }
@@ -627,7 +636,8 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
     if (precision == DDX_PREC_MIXED && sliced_fits(a, ms)) return launch_sliced<2>(s, a, ms, st);
     const int threads = 128;
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
-    if (precision == DDX_PREC_MIXED) massive_pass2_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, ms);
+    if (precision == DDX_PREC_MIXED)
+        massive_pass2_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, slotted(ms, a));
     else massive_pass2_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
     return cudaGetLastError();
 }

@@ -66,9 +66,9 @@ int ddx_run(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
  * massive bodies go first; the dust's copy in runs on its own stream, overlapping the massive
  * set's work.  The dust then goes through in up to three chunks (one wave of the dust
  * kernel, the bulk, one wave), the copy in of chunk k+1 and the copy out of chunk k-1 on their
- * own streams overlapping chunk k's compute.  The reference mode, the mixed step with
- * planetesimals (whose spatial order works best over all the grains at once), and fewer than
- * four waves of grains run the dust in one chunk.  Overlap needs page-locked host memory.
+ * own streams overlapping chunk k's compute.  The reference mode, the mixed step with 1,024
+ * planetesimals or more (whose spatial order works best over all the grains at once), and
+ * fewer than four waves of grains run the dust in one chunk.  Overlap needs page-locked host memory.
  * in and out may be the same arrays.  Synchronises `stream`. */
 int ddx_step_host(ddx_ctx *ctx, const ddx_host_state *in, ddx_host_state *out, const ddx_state *s, int n_grav,
                   int n_dust, double dt, const ddx_phys *phys, int precision, int mode, void *stream);

@@ -1,9 +1,9 @@
 """ddx_step_host: one step of a system in host memory, the dust streamed through the GPU in
 up to three chunks with the copies on their own streams.  Each tracer's step does
 not depend on the others, so the result must equal ddx_step on the device bit for bit,
-whatever the chunking.  The reference mode and the spatially ordered mixed step (with
-planetesimals) run unchunked; FP64 at 500,000 grains runs in three chunks of unequal
-size."""
+whatever the chunking.  The reference mode and the spatially ordered mixed step (1,024
+planetesimals or more) run unchunked; FP64, and mixed with the 64 planetesimals here, run
+500,000 grains in three chunks of unequal size."""
 import numpy as np
 import pytest
 import torch
@@ -24,7 +24,7 @@ def pinned(arrays):
                                        (abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED),
                                        (abi.DDX_PREC_MIXED, abi.DDX_MODE_REFERENCE)])
 def test_host_step_equals_device_step(prec, mode):
-    n_dust = 500000     # FP64, fixed mode: three chunks of unequal size
+    n_dust = 500000     # fixed mode: three chunks of unequal size
     s = synth.dusty_ring(n_dust=n_dust, n_plsml=64, seed=12)
     eng = Engine(0)
     eng.set_size_table(**s.size_table)
