@@ -38,7 +38,7 @@ namespace ddx {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTilePairs = 512;                 // pair records per tile (32 KiB)
+constexpr int kTilePairs = 384;                 // pair records per tile (24 KiB)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -154,10 +154,22 @@ __device__ __forceinline__ void span_box(const BodyPair* R, float2& bx, float2& 
 // this many spans every tracer tests every span itself.
 constexpr int kFlagSpans = 4096;
 
-// Three blocks per SM (80 registers): the few FP64 values the compiler keeps in local
-// memory are touched only between stages, and the extra warps hide the latency of the
-// broadcast shared-memory reads and of rsqrt.approx better than two blocks without spills.
-__global__ void __launch_bounds__(kThreads, 3)
+// Bits j0 .. j0 + n - 1 (n <= 32 spans of one tile) of the span bit array w, as bits 0 .. n-1.
+// The next word is read only when the range runs into it, so only words of existing spans.
+__device__ __forceinline__ uint32_t span_bits(const uint32_t* w, int j0, int n) {
+    const int q = j0 >> 5, r = j0 & 31;
+    unsigned long long v = w[q];
+    if (r + n > 32) v |= (unsigned long long)w[q + 1] << 32;
+    return (uint32_t)(v >> r) & (n == 32 ? 0xFFFFFFFFu : (1u << n) - 1u);
+}
+
+// Four blocks per SM (64 registers, two 24 KiB tiles each): the FP64 values the compiler
+// keeps in local memory are touched only between stages, and the kernel is held by the
+// latency of the broadcast shared-memory reads and of rsqrt.approx, which more warps hide.
+// Measured on the dusty ring (dust kernel): 3 blocks (80 registers, 32 KiB tiles) 8.50 ms,
+// 4 blocks 8.34 ms, 5 blocks (48 registers, 20 KiB tiles) 8.41 ms; two blocks without
+// spills were slower than three.
+__global__ void __launch_bounds__(kThreads, 4)
 dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins,
                       const int* __restrict__ perm, bool boxes) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -320,8 +332,10 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
                 const uint32_t all = cnt / kPairSpan == 32 ? 0xFFFFFFFFu : (1u << (cnt / kPairSpan)) - 1u;
                 uint32_t open = all;
                 if (flags) {
-                    fm = allfar[tt] & all;
-                    open = all & ~(allfar[tt] | allnear[tt]);
+                    const int j0 = tt * (kTilePairs / kPairSpan);   // the tile's first span
+                    const uint32_t af = span_bits(allfar, j0, cnt / kPairSpan);
+                    fm = af;
+                    open = all & ~(af | span_bits(allnear, j0, cnt / kPairSpan));
                 }
                 while (open) {   // the same mask in every lane: no divergence here
                     const int j = __ffs(open) - 1;
