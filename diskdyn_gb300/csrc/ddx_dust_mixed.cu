@@ -79,32 +79,45 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, unsigned parity, unsigned
 // the tile: record 0 {min x, max x}, record 1 {min y, max y}, record 2 {min z, max z},
 // record 3 {max |coordinate|, 0}; the maximum is NaN when a coordinate is NaN (such a span
 // never counts as far).
+// One warp per (stage, span): lane u reads source slot u of the span's 32.
 __global__ void span_box_kernel(BodyPair* __restrict__ PP, int pcap, int n_src, int nspans) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= 4 * nspans) return;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;   // stage * nspans + span
+    const int u = threadIdx.x & 31;
+    if (k >= 4 * nspans) return;                                   // whole warps leave together
     const int stage = k / nspans, span = k - stage * nspans;
     BodyPair* const R = PP + (size_t)stage * pcap + (size_t)span * kPairSpan;
+    const int q = span * 2 * kPairSpan + u;
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     bool nan = false;
-    for (int u = 0; u < 2 * kPairSpan; ++u) {
-        const int q = span * 2 * kPairSpan + u;
-        if (q >= n_src) break;
+    if (q < n_src) {
         const BodyPair& r = R[u >> 1];
         const float v[3] = {r.hx[u & 1], r.hy[u & 1], r.hz[u & 1]};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            nan |= !(v[a] == v[a]);
-            lo[a] = fminf(lo[a], v[a]);
-            hi[a] = fmaxf(hi[a], v[a]);
+            nan = nan || !(v[a] == v[a]);
+            lo[a] = v[a];
+            hi[a] = v[a];
         }
+        if (nan) lo[0] = lo[1] = lo[2] = INFINITY, hi[0] = hi[1] = hi[2] = -INFINITY;
     }
-    float xm = 0.f;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) xm = fmaxf(xm, fmaxf(fabsf(lo[a]), fabsf(hi[a])));
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { R[a].pad[0] = lo[a]; R[a].pad[1] = hi[a]; }
-    R[3].pad[0] = nan ? __int_as_float(0x7FC00000) : xm;
-    R[3].pad[1] = 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    nan = __any_sync(0xffffffffu, nan);
+    if (u < 3) {
+        R[u].pad[0] = lo[u];
+        R[u].pad[1] = hi[u];
+    } else if (u == 3) {
+        float xm = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) xm = fmaxf(xm, fmaxf(fabsf(lo[a]), fabsf(hi[a])));
+        R[3].pad[0] = nan ? __int_as_float(0x7FC00000) : xm;
+        R[3].pad[1] = 0.f;
+    }
 }
 
 // The test of one tracer (high parts xh, yh, zh; own = its largest |coordinate|) against one
@@ -446,7 +459,7 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
         cudaError_t e = order_bodies(s, a.n_grav, a.n_dust, true, ms.dust_order, ms.dust_order.perm, nullptr, st);
         if (e != cudaSuccess) return e;
         const int nspans = pair_count(n_src) / kPairSpan;
-        span_box_kernel<<<(4 * nspans + 127) / 128, 128, 0, st>>>(ms.PP, ms.pcap, n_src, nspans);
+        span_box_kernel<<<(4 * nspans * 32 + 127) / 128, 128, 0, st>>>(ms.PP, ms.pcap, n_src, nspans);
         perm = ms.dust_order.perm;
         boxes = true;
     }
