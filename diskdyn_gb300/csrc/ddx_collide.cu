@@ -14,9 +14,9 @@
 //               lookups;
 //  3. scatter : every live tracer writes {x, y, z, cell id and halves} and its index to slot
 //               start + rank; the tracers of rank 0 and 1 also their cells' lin to the
-//               bucket's entry.
-//               Steps 1-3 are a radix sort on the whole bucket id in one pass (a counting
-//               sort): the bucket sizes are its histogram, the scan its offsets;
+//               bucket's entry.  Steps 1-3 are a radix sort on the whole bucket id in one
+//               pass (a counting sort): the bucket sizes are its histogram, the scan its
+//               offsets;
 //  4. count   : every tracer, in bucket order, visits the buckets of the 8 cells of its
 //               octant: per axis its own cell and the neighbour on the side of the cell's
 //               half it lies in (a partner closer than h cannot be further, because the cell
@@ -26,10 +26,10 @@
 //               Most neighbour cells are empty, and their bucket is then empty or holds one
 //               or two tracers of other cells: the 8 bucket entries, loaded together, settle
 //               those without touching the tracers (a lin that differs means another cell),
-//               and only the rest are walked.  A test in FP32
-//               with a proven margin rejects the far candidates first; the FP64 test decides
-//               the rest (FP64 runs at 1/64 of the FP32 rate here, and a warp pays for it
-//               whenever any of its lanes tests);
+//               and only the rest are walked.  A test in FP32 with a proven margin rejects
+//               the far candidates first; the FP64 test decides the rest (FP64 runs at 1/64
+//               of the FP32 rate here, and a warp pays for it whenever any of its lanes
+//               tests);
 //  5. scan    : exclusive scan of the counts gives each tracer its output slot;
 //  6. write   : each tracer writes its partners (the kept ones, or by walking again if it
 //               has more than kSlots) ordered by j, so the list is ordered by (i, j).

@@ -18,13 +18,17 @@
 // on the tracer and the sources alone, so a tracer's result does not depend on the others
 // or on their order.  The tracers are visited in cell order and the sources sit in their
 // pair records in cell order (ddx_order.cu), so the lanes of a warp lie close together and
-// nearly always make the same choice for a span.
+// nearly always make the same choice for a span; per stage the block settles most spans for
+// all its tracers at once from its own box (tests whose outcome implies each tracer's), and
+// the lanes test only the rest.  This runs from kOrderMinSources planetesimals on; with
+// fewer, every span takes the full separation in index order.
 //
 // Blackwell mapping:
 //  - perturbers arrive as 64-byte pair records (two bodies per record, one quantity of
 //    both bodies per 8-byte slot), and every FP32 operation of the pair force runs as one
 //    f32x2 instruction (add/sub/mul/fma.rn.f32x2) on both bodies, halving the issue
-//    slots of the FP32 work, which is what bounds this kernel;
+//    slots of the FP32 work; what bounds the kernel now is the latency of the rsqrt.approx
+//    and shared-memory results, hence four blocks per SM;
 //  - the pair records of all four stages stream through two shared-memory tiles filled
 //    by TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx), so tile k+1 lands while
 //    tile k is consumed; every thread of the block reads the same record (broadcast);
