@@ -5,11 +5,11 @@ or a loop that must keep a fixed device footprint -- get a step whose scratch is
 file-scope device array instead of cudaMalloc'd context buffers.  The test calls it
 through the C ABI twice in a row (the second call reuses the array the first one left
 behind) and checks every result against ddx_step on the same input: bit for bit in FP64,
-where both run the same kernels.  In mixed precision the context's step visits the
-tracers and the sources in a spatial order and takes far sources with the high-part
-separation, which the fixed array has no room to order for; the positions and velocities
-then agree to 1e-12 of the largest position or velocity component after two steps, and
-the removed tracers are the same.  It passes alone in a fresh process and after the other tests.
+where both run the same kernels.  In mixed precision, from 1,024 planetesimals on, the
+context's step visits the tracers and the sources in a spatial order and takes far sources
+with the high-part separation, which the fixed array has no room to order for; the test
+then allows 1e-12 of the largest position or velocity component after two steps and the
+same removed tracers (with the 300 planetesimals here both run in index order).  It passes alone in a fresh process and after the other tests.
 """
 import ctypes as C
 
