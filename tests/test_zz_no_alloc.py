@@ -9,7 +9,7 @@ where both run the same kernels.  In mixed precision, from 1,024 planetesimals o
 context's step visits the tracers and the sources in a spatial order and takes far sources
 with the high-part separation, which the fixed array has no room to order for; the test
 then allows 1e-12 of the largest position or velocity component after two steps and the
-same removed tracers (with the 300 planetesimals here both run in index order).  It passes alone in a fresh process and after the other tests.
+same removed tracers.  It passes alone in a fresh process and after the other tests.
 """
 import ctypes as C
 
@@ -38,7 +38,7 @@ def test_noalloc_step_matches_ddx_step_twice(built_lib, prec, mode):
     from diskdyn_gb300.engine import Engine
     lib = abi.load()
     eng = Engine(0)
-    sysm = synth.dusty_ring(n_dust=4096, n_plsml=300, seed=21, n_steps=2)
+    sysm = synth.dusty_ring(n_dust=4096, n_plsml=1100, seed=21, n_steps=2)   # ddx_step orders in space
     eng.set_size_table(**sysm.size_table)
     tab = {k: torch.tensor(np.asarray(sysm.size_table[k], np.float32), device="cuda")
            for k in ("beta", "betasw", "q")}
