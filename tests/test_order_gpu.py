@@ -16,8 +16,8 @@ pytestmark = pytest.mark.gpu
 FIELDS = ("x", "y", "z", "vx", "vy", "vz", "N")
 
 
-def ring():
-    return synth.dusty_ring(n_dust=20000, n_plsml=1024, seed=31, n_steps=20)
+def ring(n_plsml=1024):
+    return synth.dusty_ring(n_dust=20000, n_plsml=n_plsml, seed=31, n_steps=20)
 
 
 def permuted(state, n_grav, perm):
@@ -28,8 +28,9 @@ def permuted(state, n_grav, perm):
     return out
 
 
-def test_mixed_step_does_not_depend_on_tracer_order(engine):
-    s = ring()
+@pytest.mark.parametrize("n_plsml", [1024, 9000])   # the planetesimals ordered in one block / by radix sort
+def test_mixed_step_does_not_depend_on_tracer_order(engine, n_plsml):
+    s = ring(n_plsml)
     engine.set_size_table(**s.size_table)
     n_dust = len(s.state["x"]) - s.n_grav
     perm = np.random.default_rng(7).permutation(n_dust)
@@ -47,8 +48,9 @@ def test_mixed_step_does_not_depend_on_tracer_order(engine):
         assert torch.equal(u[s.n_grav:], v[s.n_grav:][inv]), f
 
 
-def test_mixed_step_repeats_bit_for_bit(engine):
-    s = ring()
+@pytest.mark.parametrize("n_plsml", [1024, 9000])
+def test_mixed_step_repeats_bit_for_bit(engine, n_plsml):
+    s = ring(n_plsml)
     engine.set_size_table(**s.size_table)
     phys = make_phys(**s.phys)
     runs = []
