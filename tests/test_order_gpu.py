@@ -94,3 +94,34 @@ def test_far_spans_keep_the_mixed_error(engine):
     assert alive.mean() > 0.99
     assert np.median(e) < 1e-13
     assert np.quantile(e, 0.99) < 1e-12
+
+
+@pytest.mark.parametrize("n_dust", [3000, 100])   # 100 grains: blocks of 64 threads
+def test_ordered_step_with_removed_non_finite_and_distant_tracers(engine, n_dust):
+    """The ordered step (1,100 planetesimals) with removed tracers (N = 0), a NaN and an
+    infinite coordinate, and a tracer at 1e30 AU: the boxes and the far tests take them
+    like any other, and the mixed step removes the same tracers as FP64 and keeps the rest
+    within the mixed tolerance."""
+    s = synth.dusty_ring(n_dust=n_dust, n_plsml=1100, seed=17, n_steps=20)
+    st = {k: np.array(v, copy=True) for k, v in s.state.items()}
+    g = s.n_grav
+    st["N"][g::7] = 0.0
+    st["x"][g + 5] = np.nan
+    st["y"][g + 9] = np.inf
+    st["z"][g + 13] = 1e30
+    engine.set_size_table(**s.size_table)
+    phys = make_phys(**s.phys)
+    out = {}
+    for prec in (abi.DDX_PREC_FP64, abi.DDX_PREC_MIXED):
+        d = DeviceState.from_numpy(st)
+        engine.step(d, g, s.dt, phys, prec, abi.DDX_MODE_FIXED)
+        torch.cuda.synchronize()
+        out[prec] = d.to_numpy()
+    f, m = out[abi.DDX_PREC_FP64], out[abi.DDX_PREC_MIXED]
+    np.testing.assert_array_equal(m["N"] == 0, f["N"] == 0)
+    assert f["N"][g + 5] == 0 and f["N"][g + 9] == 0
+    ok = (f["N"][g:] != 0) & np.isfinite(f["x"][g:])
+    pf = np.stack([f[k][g:][ok] for k in ("x", "y", "z")])
+    pm = np.stack([m[k][g:][ok] for k in ("x", "y", "z")])
+    e = np.linalg.norm(pm - pf, axis=0) / np.linalg.norm(pf, axis=0)
+    assert e.max() < 1e-12
