@@ -124,3 +124,19 @@ def test_empty_and_single_ranges(engine):
         gpu_pairs(engine, s.state, 0, n, -1.0)
     with pytest.raises(abi.DDXError):
         gpu_pairs(engine, s.state, 5, 2, 1.0)
+
+
+def test_non_finite_positions_take_no_pairs(engine):
+    """Tracers with NaN or infinite coordinates get a cell like any other (the conversion
+    saturates, or gives 0 for NaN), never pass the distance test, and leave the other
+    pairs as brute force finds them."""
+    st = cluster_state(2000, seed=8)
+    st["x"][10] = np.nan
+    st["y"][20] = np.inf
+    st["z"][30] = -np.inf
+    st["x"][40] = 1e300
+    g, tot = gpu_pairs(engine, st, 0, 2000, 2e-3)
+    o = oc.collide(st, 0, 2000, 2e-3, "brute")
+    assert tot == len(o) > 1000
+    np.testing.assert_array_equal(g, o)
+    assert not np.isin(o, [10, 20, 30, 40]).any()
