@@ -12,6 +12,7 @@ same size against a replica of the massive set (weak scaling, no data-path colle
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -55,7 +56,9 @@ def parse():
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar", "setup", "cadence"], default="dusty_ring")
+    p.add_argument("--no-configs", action="store_true", help="leave out the brief legs of the other configurations")
+    p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar", "setup", "cadence", "accuracy"],
+                   default="dusty_ring")
     p.add_argument("--solar-steps", type=int, default=1000)
     p.add_argument("--scale-err-steps", type=int, default=60)
     p.add_argument("--adjoint-steps", type=int, default=2000)
@@ -176,7 +179,18 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
     stream = torch.cuda.current_stream()
 
-    def one_step(prec, ev=None):
+    # spatial-hash collisions over the grains, every step (the workload's collision pass):
+    # pairs closer than h_coll into a buffer sized once, with room to spare
+    h_coll = 0.1
+    n_found = C.c_longlong(0)
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def collide_call(buf):
+        abi.check(eng.lib.ddx_collide(eng.ctx, C.byref(st._abi), ng, ng + nd, C.c_double(h_coll),
+                                      C.c_void_p(buf.data_ptr()), buf.shape[0], C.byref(n_found), sh), "ddx_collide")
+        return n_found.value
+
+    def one_step(prec, ev=None, coll=None):
         if ev:
             ev[0].record(stream)
         eng.stage("massive_rk4", st, ng, sysm.dt, phys, prec)
@@ -188,48 +202,48 @@ def run_ours(args, world, rank, local):
         eng.stage("massive_final", st, ng, sysm.dt, phys, prec)
         if ev:
             ev[3].record(stream)
+        if coll is not None:
+            found = collide_call(coll)   # synchronises the stream: the count comes back to the host
+            if ev:
+                ev[4].record(stream)
+            return found
 
+    pair_buf = torch.empty((1, 2), dtype=torch.int32, device="cuda")
+    pair_buf = torch.empty((4 * collide_call(pair_buf) + 65536, 2), dtype=torch.int32, device="cuda")
     for _ in range(args.warmup):
-        one_step(MIX)
+        found = one_step(MIX, coll=pair_buf)
+        if found > pair_buf.shape[0]:
+            pair_buf = torch.empty((4 * found + 65536, 2), dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     alive0 = int((st.N[ng:] != 0).sum().item())
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+    pairs_per_step = []
     barrier()
     torch.cuda.synchronize()
     with Clocks(smi_index(local)) as clk:
         t0 = time.perf_counter()
         for k in range(args.steps):
             flush.zero_()
-            one_step(MIX, evs[k])
+            pairs_per_step.append(one_step(MIX, evs[k], coll=pair_buf))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     barrier()
-    step_ms = [e[0].elapsed_time(e[3]) for e in evs]
+    step_ms = [e[0].elapsed_time(e[4]) for e in evs]
+    rk4_ms = [e[0].elapsed_time(e[3]) for e in evs]
+    coll_ms = [e[3].elapsed_time(e[4]) for e in evs]
     dust_ms = [e[1].elapsed_time(e[2]) for e in evs]
     alive1 = int((st.N[ng:] != 0).sum().item())
+    assert max(pairs_per_step) <= pair_buf.shape[0], "collision buffer too small"
     # whole job: units of all ranks over the slowest rank's time (diskdyn_gb300.shard)
     units, t_total, value = shard.job_rate((ng + 0.5 * (alive0 + alive1)) * args.steps, sum(step_ms) / 1e3,
                                            device="cuda")
-
-    # spatial-hash collision pass over the grains (the workload detects collisions every step)
-    h_coll = 0.1
-    for _ in range(2):
-        pairs = eng.collide(st, ng, ng + nd, h_coll)
-    torch.cuda.synchronize()
-    coll_ms = []
-    for _ in range(5):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        pairs = eng.collide(st, ng, ng + nd, h_coll)
-        coll_ms.append((time.perf_counter() - t1) * 1e3)
-    collide = {"h_AU": h_coll, "pairs": eng.last_pair_count, "ms_per_call": statistics.median(coll_ms),
-               "bodies_per_s": nd / (statistics.median(coll_ms) / 1e3),
-               "what": "one ddx_collide call over the grains (output buffer sized from the previous call): "
-                       "hash keys and bucket ranks on 2h cells, bucket scan, scatter to bucket order, octant count, scan, write; host wall "
-                       "time, including the count read-back"}
-    step_plus_coll_ms = t_total * 1e3 / args.steps + collide["ms_per_call"]
-    collide["body_steps_per_s_with_collisions"] = (ng + alive1) / (step_plus_coll_ms / 1e3)
+    _, _, value_rk4 = shard.job_rate((ng + 0.5 * (alive0 + alive1)) * args.steps, sum(rk4_ms) / 1e3, device="cuda")
+    collide = {"h_AU": h_coll, "pairs_per_step_median": statistics.median(pairs_per_step),
+               "ms_per_call": statistics.mean(coll_ms),
+               "bodies_per_s": nd / (statistics.mean(coll_ms) / 1e3),
+               "what": "ddx_collide over the grains after every timed step, inside the timed region: hash keys "
+                       "and bucket ranks on 2h cells, bucket scan, scatter to bucket order, octant count, scan, "
+                       "write, count read back to the host (CUDA events around the call)"}
 
     # roofline of the dust kernel (FP32-pipe bound in the mixed path)
     fp32_peak, fp64_peak = probe_fma_peak(local)
@@ -279,24 +293,38 @@ def run_ours(args, world, rank, local):
     # end to end through the C ABI with host buffers (ddx_step_host): per step, the state
     # from pinned host memory to the device, the step, the updated state back; the dust
     # streams through in chunks with the copies overlapping the compute
+    # ... then the step's collision pairs: ddx_collide on the device state, and the pairs
+    # found copied to pinned host memory
     host = {k: getattr(st0, k).cpu().pin_memory() for k in ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id")}
     out = {k: torch.empty_like(host[k]).pin_memory() for k in host}
+    pairs_host = torch.empty(pair_buf.shape, dtype=torch.int32).pin_memory()
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = sum(out[k].numel() * out[k].element_size() for k in ("x", "y", "z", "vx", "vy", "vz", "N"))
     st = st0.clone()
-    eng.step_host(st, host, out, ng, sysm.dt, phys, MIX)      # creates the copy streams
+
+    def e2e_step():
+        eng.step_host(st, host, out, ng, sysm.dt, phys, MIX)
+        found = collide_call(pair_buf)
+        pairs_host[:found].copy_(pair_buf[:found], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return found
+
+    e2e_step()                                  # creates the copy streams
     torch.cuda.synchronize()
     barrier()
-    e2e_ms = []
+    e2e_ms, e2e_pairs = [], []
     for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        eng.step_host(st, host, out, ng, sysm.dt, phys, MIX)
+        e2e_pairs.append(e2e_step())
         e2e_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_value = allsum((ng + alive0) * args.steps) / allmax(sum(e2e_ms) / 1e3)
+    d2h_pairs = 8.0 * statistics.mean(e2e_pairs)
 
     peaks = measured_peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
@@ -304,17 +332,26 @@ def run_ours(args, world, rank, local):
         "data": "synthetic (seeded Philox), dusty-ring configuration",
         "config": {"workload": WORKLOAD, "n_grav": ng, "n_dust_per_gpu": nd, "n_planetesimals": args.n_plsml,
                    "dt_yr": sysm.dt, "precision": "mixed", "physics": "radiation+PR+stellar-wind drag",
-                   "l2": "flushed between timed steps (256 MiB write)"},
+                   "step": "massive_rk4 + small_rk4 + massive_final + ddx_collide (h = %.2f AU)" % h_coll,
+                   "near_radius_eta": 4e-3, "l2": "flushed between timed steps (256 MiB write)"},
         "wall_s_timed_region": wall,
+        "rk4_only": {"value": value_rk4, "unit": UNIT, "ms_per_step": statistics.mean(rk4_ms),
+                     "what": "the same timed steps without the collision call"},
         "fp64": fp64,
         "mixed_over_fp64": value / fp64["value"] if fp64 else None,
         "error_vs_fp64": err_short,
         "error_vs_fp64_long": err_long,
         "collide": collide,
-        "roofline": {"kernel": "dust_rk4_kernel<mixed>", "bound": "fp32_pipe", "achieved": achieved,
+        "roofline": {"kernel": "dust_rk4_mixed_kernel", "bound": "fp32_pipe", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "peak_source": "ddx_probe_fma_peak (FMA chains, measured in this run); "
                                     "MEASURED_PEAKS.json has no FP32/FP64 pipe figure",
+                     "sm_count": sms,
+                     "fp32_nominal_tflops": sms * 128 * 2 * 2.070e9 / 1e12,
+                     "fp32_nominal_at_median_clock_tflops": (sms * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12
+                                                             if clocks.get("sm_mhz") else None),
+                     "frac_of_nominal": achieved / (sms * 128 * 2 * 2.070e9 / 1e12),
+                     "nominal_definition": "SMs x 128 FP32 lanes x 2 flops (FMA) x 2,070 MHz",
                      "flops_per_launch": flops, "dust_kernel_ms": t_dust * 1e3,
                      "fp64_peak_tflops": fp64_peak,
                      # DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of
@@ -324,12 +361,19 @@ def run_ours(args, world, rank, local):
                      "traffic_source": "ncu capture of a 262,144-grain launch, scaled by the grains",
                      "algorithmic_bytes": ALG_BYTES_PER_GRAIN * nd,
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h + d2h_pairs,
+                "what": "ddx_step_host (state in from pinned host memory, step, state out) + ddx_collide + the "
+                        "pairs found copied to pinned host memory, host wall time per step"},
         # per step: planetesimal order (one block up to 8,192 planetesimals, else 14 launches of
-        # the radix sort), prepare, 2 x (slice sums + gather), tracer order (7), span boxes, dust
-        "gpu_launches": ((1 if args.n_plsml <= 8192 else 14) + 14) * args.steps,
-        "clocks": clk.summary(),
+        # the radix sort), prepare, 2 x (slice sums + gather), tracer order (7), span boxes, dust;
+        # collisions: keys, bucket scan (3), scatter, count, scan (3), write
+        "gpu_launches": ((1 if args.n_plsml <= 8192 else 14) + 14 + 10) * args.steps,
+        "clocks": clocks,
     }
+    if rank == 0 and world == 1 and not args.no_configs:
+        # the other configurations in brief, each with its own roofline
+        line["configs"] = {"solar": solar_leg(local, fp64_peak), "imaging": imaging_leg(local),
+                           "scale": scale_leg(local, fp32_peak)}
     if rank == 0 and args.adjoint_steps > 0:
         line["adjoint"] = adjoint_leg(local, n_steps=args.adjoint_steps)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -444,6 +488,101 @@ def long_error_leg(eng, phys, args, n_plsml=None, seed=None, n_steps=None, floor
     return out
 
 
+def run_accuracy(args, world, rank, local):
+    """Near radius of the mixed step (ddx_set_near_radius) against time and error on the
+    dusty ring: for each radius eta, the full workload's step time (CUDA events, L2 flushed
+    between steps) and the error of a 1,000-step run against the FP64 step on a shard of
+    err_dust grains with all massive bodies.  Beside it, the FP64 CPU oracle runs the same
+    1,000 steps of a 2,048-grain shard on the host cores (a thread; ctypes releases the
+    interpreter lock), and the GPU's FP64 and mixed steps are compared with it."""
+    import threading as th
+    import torch
+    import oracle.cpu as oc
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys
+
+    torch.cuda.set_device(local)
+    n_steps = args.err_steps
+    osys = synth.dusty_ring(n_dust=2048, n_plsml=args.n_plsml, seed=synth.SEED + 29)
+    oracle_out = {}
+
+    def oracle_run():
+        t0 = time.perf_counter()
+        oracle_out["state"] = oc.step(osys.state, osys.n_grav, osys.dt, osys.size_table, osys.phys, n_steps)
+        oracle_out["s"] = time.perf_counter() - t0
+    worker = th.Thread(target=oracle_run, daemon=True)
+    worker.start()
+
+    full = synth.dusty_ring(n_dust=args.n_dust, n_plsml=args.n_plsml)
+    ng = full.n_grav
+    eng = Engine(local)
+    eng.set_size_table(**full.size_table)
+    phys = make_phys(**full.phys)
+    st0 = DeviceState.from_numpy(full.state, device=f"cuda:{local}")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    MIX, F64 = abi.DDX_PREC_MIXED, abi.DDX_PREC_FP64
+
+    small = synth.dusty_ring(n_dust=args.err_dust, n_plsml=args.n_plsml, seed=synth.SEED + 17)
+    sng = small.n_grav
+
+    def evolve(sysm, prec, k, eta):
+        st = DeviceState.from_numpy(sysm.state)
+        eng.set_near_radius(eta)
+        eng.set_size_table(**sysm.size_table)
+        eng.evolve(st, sysm.n_grav, sysm.dt, k, make_phys(**sysm.phys), prec, abi.DDX_MODE_FIXED)
+        torch.cuda.synchronize()
+        return st
+
+    def errs(a, b, n_grav):
+        live = (a.N[n_grav:] != 0) & (b.N[n_grav:] != 0)
+        d = torch.sqrt((a.x - b.x) ** 2 + (a.y - b.y) ** 2 + (a.z - b.z) ** 2)
+        r = torch.sqrt(b.x ** 2 + b.y ** 2 + b.z ** 2)
+        e = (d / r)[n_grav:][live].double().cpu().numpy()
+        em = (d / r)[1:n_grav].double().cpu().numpy()
+        return {"dust_median": float(np.median(e)), "dust_p99": float(np.quantile(e, 0.99)),
+                "dust_max": float(e.max()), "massive_median": float(np.median(em)), "massive_max": float(em.max()),
+                "removed_differently": int((a.N[n_grav:] != b.N[n_grav:]).sum().item())}
+
+    ref = evolve(small, F64, n_steps, 0.0)
+    sweep = []
+    for eta in (0.0, 1e-3, 2e-3, 4e-3, 8e-3, 1.6e-2, 3.2e-2):
+        eng.set_size_table(**full.size_table)
+        eng.set_near_radius(eta)
+        st = st0.clone()
+        for _ in range(args.warmup):
+            eng.step(st, ng, full.dt, phys, MIX)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            eng.step(st, ng, full.dt, phys, MIX)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+        m = evolve(small, MIX, n_steps, eta)
+        sweep.append({"eta": eta, "near_radius_at_130AU": eta * 130.0, "ms_per_step": ms,
+                      "body_steps_per_s": (ng + full.n_dust) / (ms / 1e3), "error_vs_fp64": errs(m, ref, sng)})
+    worker.join()
+    vs_oracle = None
+    if "state" in oracle_out:
+        o = oracle_out["state"]
+        ost = DeviceState.from_numpy(o)
+        f = evolve(osys, F64, n_steps, 4e-3)
+        m = evolve(osys, MIX, n_steps, 4e-3)
+        vs_oracle = {"steps": n_steps, "n_dust": 2048, "n_grav": osys.n_grav, "oracle_s": oracle_out["s"],
+                     "oracle_cores": os.cpu_count(),
+                     "fp64_gpu_vs_oracle": errs(f, ost, osys.n_grav),
+                     "mixed_gpu_vs_oracle": errs(m, ost, osys.n_grav)}
+    line = {"metric": "near radius vs step time and 1,000-step error (mixed precision)", "workload": "accuracy",
+            "n_grav": ng, "n_dust": full.n_dust, "err_dust": args.err_dust, "err_steps": n_steps,
+            "error_definition": "|x - x_ref| / |x_ref| per body after err_steps steps from the same state",
+            "sweep": sweep, "vs_oracle": vs_oracle}
+    eng.close()
+    print(json.dumps(line), flush=True)
+
+
 def run_scale(args, world, rank, local):
     """Mixed precision at scale: 16,777,216 grains + 65,536 gravitating planetesimals with
     the dusty ring's star and two planets.  Times `steps` full steps (L2 flushed between
@@ -514,6 +653,154 @@ def run_scale(args, world, rank, local):
         line["error_vs_fp64"] = long_error_leg(eng, phys, args, n_plsml=n_plsml, seed=seed,
                                                n_steps=args.scale_err_steps, floor=False)
     print(json.dumps(line), flush=True)
+
+
+def solar_leg(local, fp64_peak, n_steps=1000, reps=3):
+    """Configuration 1 in brief: 9 massive bodies + 16,384 planetesimals, the whole
+    1,000-step FP64 run replayed as one CUDA graph, CUDA events; roofline of the FP64 pipe
+    (20 flops per body-body interaction, 45 per star term)."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys
+    sysm = synth.solar_like(n_dust=16384)
+    ng, nd = sysm.n_grav, sysm.n_dust
+    eng = Engine(local)
+    eng.set_size_table(**sysm.size_table)
+    phys = make_phys(**sysm.phys)
+    st0 = DeviceState.from_numpy(sysm.state, device=f"cuda:{local}")
+    st = st0.clone()
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        eng.evolve(st, ng, sysm.dt, 10, phys, abi.DDX_PREC_FP64, stream=stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        eng.evolve(st, ng, sysm.dt, n_steps, phys, abi.DDX_PREC_FP64, stream=stream)
+    ms = []
+    for _ in range(reps + 1):
+        st.copy_from_({f: getattr(st0, f) for f in ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id")})
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = statistics.mean(ms[1:]) / 1e3
+    flops = n_steps * (FLOP_PAIR * 4.0 * (nd * (ng - 1) + ng * (ng - 1)) + FLOP_STAR * 4.0 * nd)
+    eng.close()
+    return {"workload": "solar: 9 massive + 16,384 planetesimals, 1,000 FP64 steps (dt 0.05 yr) as one CUDA graph",
+            "value": (ng + nd) * n_steps / t, "unit": UNIT, "ms_per_run": t * 1e3, "precision": "fp64",
+            "gpu_launches_per_step": 4,
+            "roofline": {"kernel": "whole step (dust_rk4_kernel<fp64> + massive passes)", "bound": "fp64_pipe",
+                         "achieved": flops / t / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": flops / t / 1e12 / fp64_peak,
+                         "note": "16,384 tracers fill 64 blocks of 256 on 152 SMs: launch- and occupancy-bound"}}
+
+
+def imaging_leg(local, reps=5):
+    """Configuration 3 in brief: 4,194,304 tracers, 10 images of 1024 x 1024 and the
+    200-wavelength SED in mixed precision, CUDA events with L2 flushed between calls;
+    roofline of HBM with the algorithmic bytes (36 B per tracer read once plus 8 B per pixel
+    and image written; the SED writes 200 doubles)."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_view
+    n = 4194304
+    s = synth.imaging(n_dust=n)
+    eng = Engine(local)
+    eng.set_size_table(**s.size_table)
+    o = s.optics
+    eng.set_optics(o["w"], o["in"], o["Qabs"], o["Qsca"], o["Qpfunc"], o["Td"], o["Rmin"], o["Rmax"])
+    st = DeviceState.from_numpy(s.state, device=f"cuda:{local}")
+    view = make_view(**s.view)
+    n_img = len(s.image_wj)
+    F = torch.empty((n_img, s.view["xsize"], s.view["ysize"]), dtype=torch.float64, device="cuda")
+    Fs = torch.empty(len(o["w"]), dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=abi.DDX_PREC_MIXED)
+        eng.sed(st, s.n_grav, view, out=Fs, precision=abi.DDX_PREC_MIXED)
+    ti, ts = [], []
+    for _ in range(reps):
+        flush.zero_()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=abi.DDX_PREC_MIXED)
+        e[1].record(stream)
+        flush.zero_()
+        e[2].record(stream)
+        eng.sed(st, s.n_grav, view, out=Fs, precision=abi.DDX_PREC_MIXED)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        ti.append(e[0].elapsed_time(e[1]))
+        ts.append(e[2].elapsed_time(e[3]))
+    t_img, t_sed = statistics.mean(ti) / 1e3, statistics.mean(ts) / 1e3
+    npix = s.view["xsize"] * s.view["ysize"]
+    b_img = n * 36 + n_img * npix * 8
+    b_sed = n * 36 + len(o["w"]) * 8
+    hbm = measured_peaks().get("hbm_gbs", 6800.0)
+    eng.close()
+    return {"workload": "imaging: 4,194,304 tracers, 10 images 1024x1024 + 200-wavelength SED, mixed precision",
+            "value": n * n_img / t_img, "unit": "particle-wavelengths/s (images)", "image_ms": t_img * 1e3,
+            "sed_ms": t_sed * 1e3, "sed_particle_wavelengths_per_s": n * len(o["w"]) / t_sed,
+            "roofline": {"kernel": "image_mixed_kernel (+ convert)", "bound": "hbm", "achieved": b_img / t_img / 1e9,
+                         "peak": hbm, "unit": "GB/s", "frac": b_img / t_img / 1e9 / hbm,
+                         "algorithmic_bytes": b_img},
+            "sed_roofline": {"kernel": "sed_mixed_kernel", "bound": "hbm", "achieved": b_sed / t_sed / 1e9,
+                             "peak": hbm, "unit": "GB/s", "frac": b_sed / t_sed / 1e9 / hbm,
+                             "algorithmic_bytes": b_sed}}
+
+
+def scale_leg(local, fp32_peak, steps=2, warmup=1):
+    """Configuration 4 in brief: 16,777,216 grains + 65,536 gravitating planetesimals (with
+    the dusty ring's star and planets), mixed precision, `steps` full steps after `warmup`,
+    CUDA events with L2 flushed; roofline of the dust kernel on the FP32 pipe."""
+    import torch
+    from diskdyn_gb300 import abi, synth
+    from diskdyn_gb300.engine import DeviceState, Engine, make_phys
+    sysm = synth.dusty_ring(n_dust=16777216, n_plsml=65536, seed=synth.SEED + 4243, n_steps=500)
+    ng, nd = sysm.n_grav, sysm.n_dust
+    eng = Engine(local)
+    eng.set_size_table(**sysm.size_table)
+    phys = make_phys(**sysm.phys)
+    st = DeviceState.from_numpy(sysm.state, device=f"cuda:{local}")
+    del sysm.state
+    MIX = abi.DDX_PREC_MIXED
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        eng.step(st, ng, sysm.dt, phys, MIX)
+    torch.cuda.synchronize()
+    alive0 = int((st.N[ng:] != 0).sum().item())
+    rows = []
+    for _ in range(steps):
+        flush.zero_()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
+        eng.stage("massive_rk4", st, ng, sysm.dt, phys, MIX)
+        ev[1].record(stream)
+        eng.stage("small_rk4", st, ng, sysm.dt, phys, MIX)
+        ev[2].record(stream)
+        eng.stage("massive_final", st, ng, sysm.dt, phys, MIX)
+        ev[3].record(stream)
+        rows.append(ev)
+    torch.cuda.synchronize()
+    alive1 = int((st.N[ng:] != 0).sum().item())
+    step_ms = statistics.mean(e[0].elapsed_time(e[3]) for e in rows)
+    dust_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in rows)
+    alive = 0.5 * (alive0 + alive1)
+    flops = FLOP_PAIR * 4.0 * alive * (ng - 1) + FLOP_STAR * 4.0 * alive
+    del st
+    eng.close()
+    torch.cuda.empty_cache()
+    return {"workload": "scale: 65,539 massive + 16,777,216 grains, mixed precision, %d steps" % steps,
+            "value": (ng + alive) / (step_ms / 1e3), "unit": UNIT, "ms_per_step": step_ms,
+            "dust_kernel_ms": dust_ms, "massive_ms": step_ms - dust_ms,
+            "roofline": {"kernel": "dust_rk4_mixed_kernel", "bound": "fp32_pipe", "achieved": flops / (dust_ms / 1e3) / 1e12,
+                         "peak": fp32_peak, "unit": "TFLOP/s", "frac": flops / (dust_ms / 1e3) / 1e12 / fp32_peak}}
 
 
 def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
@@ -1010,6 +1297,9 @@ def main():
         return
     if args.workload == "scale":
         run_scale(args, world, rank, local)
+        return
+    if args.workload == "accuracy":
+        run_accuracy(args, world, rank, local)
         return
     if args.workload == "solar" and args.impl == "ours":
         run_solar(args, world, rank, local)

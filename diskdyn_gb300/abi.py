@@ -13,6 +13,7 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libddx.so"
 
 DDX_OK = 0
+DDX_ERR_ARG, DDX_ERR_CUDA, DDX_ERR_NOMEM, DDX_ERR_STATE, DDX_ERR_RANGE, DDX_ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
 DDX_PREC_FP64 = 0
 DDX_PREC_MIXED = 1
 DDX_MODE_FIXED = 0
@@ -152,6 +153,9 @@ SIGNATURES = [
                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
     ("ddx_sync_status", C.c_int, [C.c_void_p, C.c_void_p]),
     ("ddx_debug_lose_tile_copy", C.c_int, [C.c_void_p, C.c_int, C.c_ulonglong]),
+    ("ddx_noalloc_sync_status", C.c_int, [C.c_int, C.c_void_p]),
+    ("ddx_debug_noalloc_lose_tile_copy", C.c_int, [C.c_int, C.c_int, C.c_ulonglong]),
+    ("ddx_set_near_radius", C.c_int, [C.c_void_p, C.c_double]),
     ("ddx_probe_fma_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
 

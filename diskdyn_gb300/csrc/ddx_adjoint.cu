@@ -260,7 +260,7 @@ dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, doub
     bool alive = N[i] != 0.0;
     float bet = 0.f, betsw = 0.f;
     const int id = A.id[i];
-    if (id >= 0) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
+    if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
     const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw);
     const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
     for (int n = n0; n < n1; ++n) {
@@ -419,7 +419,7 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
     if (on) {
         for (int c = 0; c < 3; ++c) { lx[c] = lam[c * nd + i]; lv[c] = lam[(3 + c) * nd + i]; }
         const int id = A.id[i];
-        if (id >= 0) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
+        if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
     }
     const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw);
     RowTile T{tbuf[warp], wpart[warp], 0, 0, lane};
@@ -610,7 +610,7 @@ __global__ void image_splat_kernel(const double* __restrict__ y, const double* _
     if (i >= nd) return;
     const int id = idv[i];
     const double n = N[i];
-    if (id < 0 || n == 0.0) return;
+    if (id < 0 || id >= o.n_grid || n == 0.0) return;
     TracerFlux g;
     tracer_geometry(y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i], id, v, o, g);
     if (!(g.R > o.Rmin)) return;
@@ -643,7 +643,7 @@ __global__ void image_splat_adjoint_kernel(const double* __restrict__ y, const d
     active[i] = 0;
     const int id = idv[i];
     const double n = N[i];
-    if (id < 0 || n == 0.0) return;
+    if (id < 0 || id >= o.n_grid || n == 0.0) return;
     TracerFlux g;
     tracer_geometry(y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i], id, v, o, g);
     if (!(g.R > o.Rmin)) return;

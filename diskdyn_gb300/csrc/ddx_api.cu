@@ -31,6 +31,7 @@ struct ddx_ctx {
     int sed_partial_cap = 0;
     unsigned long long* counters = nullptr;   // [0]: tracers that took the exact pixel path
     int* status = nullptr;                      // kStatus* bits set by kernels (device)
+    float near_eta = kDefaultNearEta;           // mixed path: FP64 pulls within near_eta * |coordinate|
     int inject_lose_tile = -1;                  // one-shot test hook for the next mixed dust launch
     unsigned long long inject_wait_ns = 0;
     CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
@@ -66,7 +67,7 @@ cudaError_t dalloc(T** p, size_t n) {
 
 void free_massive(MassiveScratch& ms) {
     cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.PP); cudaFree(ms.A); cudaFree(ms.R);
-    cudaFree(ms.part); cudaFree(ms.slot);
+    cudaFree(ms.part); cudaFree(ms.slot); cudaFree(ms.src);
     order_free(ms.src_order);
     order_free(ms.dust_order);
     ms = MassiveScratch{};   // the status word belongs to the context, not to the scratch
@@ -103,6 +104,7 @@ int alloc_massive(ddx_ctx* c, int n_grav) {
         dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.PP, (size_t)4 * ms.pcap) != cudaSuccess ||
         dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess || dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess ||
         dalloc(&ms.part, (size_t)ms.part_words) != cudaSuccess || dalloc(&ms.slot, (size_t)cap) != cudaSuccess ||
+        dalloc(&ms.src, (size_t)cap) != cudaSuccess ||
         order_alloc(ms.src_order, cap, true) != cudaSuccess) {
         ms.status = nullptr;
         free_massive(ms);
@@ -117,8 +119,10 @@ bool state_ok(const ddx_state* s) {
     return s && s->x && s->y && s->z && s->vx && s->vy && s->vz && s->m && s->N && s->id;
 }
 
-int make_step_args(const ddx_phys* p, int n_grav, int n_dust, double dt, int mode, StepArgs& a) {
+int make_step_args(const ddx_ctx* c, const ddx_phys* p, int n_grav, int n_dust, double dt, int mode, StepArgs& a) {
     if (!p || n_grav < 1 || n_dust < 0) return DDX_ERR_ARG;
+    a.near_eta = c->near_eta;
+    a.n_grid = c->n_grid;
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
     if (p->n_planets < 0 || p->n_planets > n_grav) return DDX_ERR_ARG;
     a.n_grav = n_grav;
@@ -268,7 +272,8 @@ int ddx_create(ddx_ctx** out, int device) {
         cudaGetLastError();
         return DDX_ERR_CUDA;
     }
-    if (cudaSetDevice(device) != cudaSuccess) return DDX_ERR_CUDA;
+    DeviceGuard dg(device);
+    if (!dg.ok()) return DDX_ERR_CUDA;
     ddx_ctx* c = new ddx_ctx();
     c->device = device;
     if (dalloc(&c->vc, 1) != cudaSuccess || dalloc(&c->od_dev, 1) != cudaSuccess ||
@@ -285,7 +290,7 @@ int ddx_create(ddx_ctx** out, int device) {
 
 int ddx_destroy(ddx_ctx* c) {
     if (!c) return DDX_ERR_ARG;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     free_massive(c->ms);
     free_optics(c);
     cudaFree(c->bins); cudaFree(c->size_d); cudaFree(c->vc); cudaFree(c->od_dev);
@@ -306,7 +311,7 @@ int ddx_set_size_table(ddx_ctx* c, int n_grid, const double* size, const float* 
                        const float* betasw, const float* q) {
     if (!c || n_grid < 0 || (n_grid > 0 && (!size || !beta || !betasw || !q))) return DDX_ERR_ARG;
     if (n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     std::vector<SizeBin> h(n_grid > 0 ? n_grid : 1);
     for (int k = 0; k < n_grid; ++k) h[k] = SizeBin{beta[k], betasw[k], q[k], 0.f};
     cudaFree(c->bins); cudaFree(c->size_d);
@@ -330,7 +335,7 @@ int ddx_set_optics(ddx_ctx* c, int n_grid, int n_wav, int n_theta, const double*
     if (n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
     if (!(Rmin > 0.0) || !(Rmax > Rmin)) return DDX_ERR_ARG;
     if (c->n_grid != n_grid) return DDX_ERR_STATE;   // the size table gives the grain sizes
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     free_optics(c);
     const size_t nq = (size_t)n_grid * n_theta * n_wav, nw = (size_t)n_grid * n_wav,
                  nt = (size_t)n_grid * DDX_NR;
@@ -378,9 +383,9 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
     if (!host_state_ok(in, n_all) || !host_state_ok(out, n_all)) return DDX_ERR_ARG;
     if (!c->bins) return DDX_ERR_STATE;
     StepArgs a;
-    int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a);
     if (r) return r;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     if ((r = ensure_massive(c, n_grav, n_dust, precision)) || (r = ensure_pipeline(c))) return r;
     cudaStream_t st = (cudaStream_t)stream;
     take_injection(c, a);
@@ -425,9 +430,9 @@ int ddx_evolve(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt
     if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
     if (!c->bins) return DDX_ERR_STATE;
     StepArgs a;
-    int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a);
     if (r) return r;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     if ((r = ensure_massive(c, n_grav, n_dust, precision))) return r;
     cudaStream_t st = (cudaStream_t)stream;
     for (int k = 0; k < n_steps; ++k)
@@ -441,15 +446,16 @@ int prepare_call(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double 
     if (!c || !state_ok(s)) return DDX_ERR_ARG;
     if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
     if (!c->bins) return DDX_ERR_STATE;
-    int r = make_step_args(phys, n_grav, n_dust, dt, mode, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a);
     if (r) return r;
-    cudaSetDevice(c->device);
-    return ensure_massive(c, n_grav, n_dust, precision);
+    return ensure_massive(c, n_grav, n_dust, precision);   // the caller made c's device current
 }
 }  // namespace
 
 int ddx_massive_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
                     const ddx_phys* phys, int precision, int mode, void* stream) {
+    if (!c) return DDX_ERR_ARG;
+    DeviceGuard dg(c->device);
     StepArgs a;
     int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
     if (r) return r;
@@ -464,6 +470,8 @@ int ddx_massive_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, doub
 
 int ddx_small_rk4(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
                   const ddx_phys* phys, int precision, int mode, void* stream) {
+    if (!c) return DDX_ERR_ARG;
+    DeviceGuard dg(c->device);
     StepArgs a;
     int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
     if (r) return r;
@@ -476,7 +484,7 @@ int ddx_collide(ddx_ctx* c, const ddx_state* s, int i0, int i1, double h, int* p
     if (!c || !state_ok(s) || !n_pairs || i0 < 0 || i1 < i0 || cap < 0 || (cap > 0 && !pairs) || !(h > 0.0))
         return DDX_ERR_ARG;
     if ((long long)i1 - i0 > (1LL << 30)) return DDX_ERR_RANGE;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     return collide_run(c->collide, *s, i0, i1, h, reinterpret_cast<int2*>(pairs), cap, n_pairs,
                        (cudaStream_t)stream);
 }
@@ -487,7 +495,7 @@ int ddx_det_step(ddx_ctx* c, const ddx_state* s, int n_grav, int n_step, const d
     if (!c || !s || !s->x || !s->y || !s->z || !s->m || !dt || n_grav < 1 || n_step < 1 || n_disks < 0 ||
         n_blobs < 0 || (n_disks > 0 && !disk_Rin) || (n_blobs > 0 && (!blob_a || !blob_ecc || !blob_sigma)))
         return DDX_ERR_ARG;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     std::vector<double> rr, mi;
     double m0 = 0.0;
     const int r = det_step_scan(c->detstep, *s, n_grav, (cudaStream_t)stream, rr, mi, m0);
@@ -517,7 +525,7 @@ int ddx_dust_temp(ddx_ctx* c, int n_grid, int n_wav, const double* w, const doub
     if (!c || n_grid < 1 || n_wav < 2 || !w || !in || !Qabs || !Rmin_AU || !Rmax_AU || !Td) return DDX_ERR_ARG;
     if (!(dist > 0.0) || !(*Rmax_AU > 0.0)) return DDX_ERR_ARG;
     if (n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     return dust_temp_run(n_grid, n_wav, w, in, Qabs, dist, Rmin_AU, Rmax_AU, Td, (cudaStream_t)stream);
 }
 
@@ -532,7 +540,7 @@ int ddx_dust_grid(ddx_ctx* c, int n_wav, const double* w, const double* in, cons
     if (file->n_size < 2 || g->n_grid < 2 || grid->n_size != g->n_grid) return DDX_ERR_ARG;
     if (!(g->amin > 0.0) || !(g->amax > g->amin) || !(g->rho > 0.0) || !(g->mstar > 0.0)) return DDX_ERR_ARG;
     if (g->n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     return dust_grid_run(n_wav, w, in, *file, *g, *grid, q, beta, betasw, Lum, betaswconst, (cudaStream_t)stream);
 }
 
@@ -548,7 +556,7 @@ extern "C" {
 int ddx_setup_device(ddx_ctx* c, const ddx_param* p, double dmin, double dmax, const float* beta,
                      unsigned long long seed, const ddx_state* s, long long cap, ddx_dat_run* run, void* stream) {
     if (!c || !p || !beta || !run || !state_ok(s)) return DDX_ERR_ARG;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     return setup_device_run(p, dmin, dmax, beta, seed, *s, cap, run, (cudaStream_t)stream);
 }
 
@@ -561,7 +569,7 @@ int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, 
     if (n_img < 1 || n_img > kMaxImages || view->xsize < 1 || view->ysize < 1 || !(view->fov > 0.0)) return DDX_ERR_ARG;
     if (!c->bins || !c->optics_set) return DDX_ERR_STATE;
     StepArgs a;
-    int r = make_step_args(phys, n_grav, n_dust, dt, DDX_MODE_FIXED, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, DDX_MODE_FIXED, a);
     if (r) return r;
     ImageList il;
     il.n = n_img;
@@ -569,7 +577,7 @@ int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, 
         if (wj[k] < 0 || wj[k] >= c->od.n_wav) return DDX_ERR_ARG;
         il.wj[k] = wj[k];
     }
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     const int K = ckpt_every < n_steps ? ckpt_every : n_steps;
     return adjoint_forward(c->adjoint, *s, n_grav, n_dust, dt, n_steps, K, a, *view, il, c->bins, c->od, image,
                            (cudaStream_t)stream);
@@ -579,8 +587,14 @@ int ddx_adjoint_backward(ddx_ctx* c, const double* dL_dimage, double* grad_state
                          void* stream) {
     if (!c || !dL_dimage || !grad_state || !grad_mass) return DDX_ERR_ARG;
     if (!c->adjoint) return DDX_ERR_STATE;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     return adjoint_backward(c->adjoint, dL_dimage, grad_state, grad_mass, c->bins, c->od, (cudaStream_t)stream);
+}
+
+int ddx_set_near_radius(ddx_ctx* c, double eta) {
+    if (!c || !(eta >= 0.0) || eta > (double)kMaxNearEta) return DDX_ERR_ARG;
+    c->near_eta = (float)eta;
+    return DDX_OK;
 }
 
 int ddx_debug_lose_tile_copy(ddx_ctx* c, int tile, unsigned long long wait_ns) {
@@ -592,6 +606,8 @@ int ddx_debug_lose_tile_copy(ddx_ctx* c, int tile, unsigned long long wait_ns) {
 
 int ddx_massive_final(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
                       const ddx_phys* phys, int precision, int mode, void* stream) {
+    if (!c) return DDX_ERR_ARG;
+    DeviceGuard dg(c->device);
     StepArgs a;
     int r = prepare_call(c, s, n_grav, n_dust, dt, phys, precision, mode, a);
     if (r) return r;
@@ -613,7 +629,7 @@ int ddx_image(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_
         if (wj[k] < 0 || wj[k] >= c->od.n_wav) return DDX_ERR_ARG;
         il.wj[k] = wj[k];
     }
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     if (precision == DDX_PREC_MIXED) {
         const size_t need = (size_t)view->xsize * view->ysize * image_k4(n_img);
         if (need > c->img32_words) {
@@ -640,7 +656,7 @@ int ddx_sed(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, const ddx_vi
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
     if (!(view->dist > 0.0)) return DDX_ERR_ARG;
     if (!c->optics_set) return DDX_ERR_STATE;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     const int nb = sed_blocks(n_dust);
     const int need = nb * c->od.n_wav;
     if (need > c->sed_partial_cap) {
@@ -661,14 +677,14 @@ int ddx_debug_pixels(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, con
                      int* pix, int* exact) {
     if (!c || !state_ok(s) || !view || !pix || !exact || n_grav < 0 || n_dust < 0) return DDX_ERR_ARG;
     if (view->xsize < 1 || view->ysize < 1 || !(view->fov > 0.0)) return DDX_ERR_ARG;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     const int n_theta = c->optics_set ? c->od.n_theta : 2;
     return cuda_status(launch_pixels(*s, n_grav, n_dust, *view, n_theta, c->vc, pix, exact, 0));
 }
 
 int ddx_sync_status(ddx_ctx* c, void* stream) {
     if (!c) return DDX_ERR_ARG;
-    cudaSetDevice(c->device);
+    DeviceGuard dg(c->device);
     if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return DDX_ERR_CUDA;
     int h = 0;
     if (cudaMemcpy(&h, c->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DDX_ERR_CUDA;

@@ -35,6 +35,16 @@
 //  - each mbarrier wait is bounded by the global timer; a block that gives up sets the
 //    context's status word, waits (bounded) for its own copies, leaves its tracers
 //    untouched and exits.
+//
+// Near sources.  FP32 leaves about 5.6e-7 of relative error in every pull, which a close
+// encounter amplifies: over 1,000 steps of the dusty ring the worst grains ended 1e-8 from
+// their FP64 positions while the median stayed at 3e-11.  So a source nearer to the tracer
+// than near_eta times the tracer's largest |coordinate| takes the FP64 pair force from the
+// FP64 stage positions instead (the FP64 step's arithmetic).  The loop over a span of 32
+// sources keeps the largest FP32 reciprocal distance (one three-input max per pair
+// record); a span whose largest exceeds 1 / (near_eta own) is summed again without its
+// near sources, which are added in FP64.  Far spans never hold a near source (near_eta is
+// at most a quarter, far spans start at a half).
 #include "ddx_internal.cuh"
 #include "ddx_f32x2.cuh"
 
@@ -167,6 +177,63 @@ __device__ __forceinline__ void span_box(const BodyPair* R, float2& bx, float2& 
     xm = R[3].pad[0];
 }
 
+// The tracer's FP64 stage coordinate from its three FP32 parts hi + lo + rest (hi = fp32(v),
+// lo = fp32(v - hi), rest = fp32(v - hi - lo)): hi + lo is exact in FP64 and within 2^-48 |v|
+// of v, rest brings the sum within 2^-72 |v|, below half an FP64 ulp, so the rounded sum is v.
+__device__ __forceinline__ double join3(f2 H, f2 L, float rest) {
+    float h, l, u;
+    f2_split(H, h, u);
+    f2_split(L, l, u);
+    return ((double)h + (double)l) + (double)rest;
+}
+__device__ __forceinline__ float rest3(double v, float hi, float lo) {
+    return __double2float_rn((v - (double)hi) - (double)lo);
+}
+
+// One span of kPairSpan pair records (slots q0 .. q0 + 2 kPairSpan - 1) summed again for a
+// tracer with a near source among them: the FP32 partial sum of the sources at or beyond the
+// near radius (the same operations as the main loop, so each of their pulls is the same),
+// and the FP64 pull of each near source from its FP64 stage position (P: the stage's
+// records of bodies n_exact.., src: source of each slot, null when slot q holds source q),
+// added to k.  A zero FP64 separation gives an infinite pull, which removes the tracer as in
+// the FP64 step.
+__device__ __forceinline__ void near_span(const BodyPair* R, int q0, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH, f2 ZL,
+                                          float xr, float yr, float zr, float inv_near, const Body* __restrict__ P,
+                                          const int* __restrict__ src, f2& px, f2& py, f2& pz, double& kx,
+                                          double& ky, double& kz) {
+    const double xt = join3(XH, XL, xr), yt = join3(YH, YL, yr), zt = join3(ZH, ZL, zr);
+    px = 0; py = 0; pz = 0;
+    for (int u = 0; u < kPairSpan; ++u) {
+        const BodyPair* r = R + u;
+        const ulonglong2 q0v = *reinterpret_cast<const ulonglong2*>(r->hx);
+        const ulonglong2 q1v = *reinterpret_cast<const ulonglong2*>(r->hz);
+        const ulonglong2 q2v = *reinterpret_cast<const ulonglong2*>(r->lx);
+        const f2 lz = *reinterpret_cast<const f2*>(r->lz);
+        const f2 dX = add2(sub2(q0v.x, XH), sub2(q2v.x, XL));
+        const f2 dY = add2(sub2(q0v.y, YH), sub2(q2v.y, YL));
+        const f2 dZ = add2(sub2(q1v.x, ZH), sub2(lz, ZL));
+        const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+        float r0, r1;
+        f2_split(RR, r0, r1);
+        const float i0 = rsqrt_approx(r0), i1 = rsqrt_approx(r1);
+        const bool n0 = i0 > inv_near, n1 = i1 > inv_near;
+        const f2 ri = f2_join(n0 ? 0.f : i0, n1 ? 0.f : i1);
+        const f2 f = mul2(mul2(q1v.y, ri), mul2(ri, ri));
+        px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!(h ? n1 : n0)) continue;
+            const int q = q0 + 2 * u + h;
+            const Body p = P[src ? src[q] : q];
+            const double ex = p.x - xt, ey = p.y - yt, ez = p.z - zt;
+            const double rr = ex * ex + ey * ey + ez * ez;
+            const double ri64 = rsqrt(rr);
+            const double f64 = p.m * (ri64 * ri64 * ri64);
+            kx = fma(f64, ex, kx); ky = fma(f64, ey, ky); kz = fma(f64, ez, kz);
+        }
+    }
+}
+
 // Spans with one bit per block test (all far, all near) in shared memory, per stage; beyond
 // this many spans every tracer tests every span itself.
 constexpr int kFlagSpans = 4096;
@@ -188,7 +255,7 @@ __device__ __forceinline__ uint32_t span_bits(const uint32_t* w, int j0, int n) 
 // spills were slower than three.
 __global__ void __launch_bounds__(kThreads, 4)
 dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins,
-                      const int* __restrict__ perm, bool boxes) {
+                      const int* __restrict__ perm, bool boxes, const int* __restrict__ src) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar[2];
     __shared__ float bred[kThreads / 32][7];
@@ -211,7 +278,7 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
             vx = s.vx[t]; vy = s.vy[t]; vz = s.vz[t];
             m = s.m[t];
             const int id = s.id[t];
-            if (id >= 0) {
+            if (id >= 0 && id < a.n_grid) {
                 const SizeBin b = bins[id];
                 bet = b.beta; betsw = b.betasw; qe = b.q;
             }
@@ -287,9 +354,12 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
         }
         float xh, xl, yh, yl, zh, zl;
         split_hilo(xt, xh, xl); split_hilo(yt, yh, yl); split_hilo(zt, zh, zl);
+        const float xr = rest3(xt, xh, xl), yr = rest3(yt, yh, yl), zr = rest3(zt, zh, zl);
         const f2 XH = f2_dup(xh), XL = f2_dup(xl), YH = f2_dup(yh), YL = f2_dup(yl);
         const f2 ZH = f2_dup(zh), ZL = f2_dup(zl);
         const float own = fmaxf(fabsf(xh), fmaxf(fabsf(yh), fabsf(zh)));   // largest |coordinate|
+        const float inv_near = near_inv(a.near_eta, own);
+        const Body* const Pn = ms.P + (size_t)st * ms.cap + a.n_exact;     // FP64 records of the sources
         // per stage: the block's box (live tracers) and, per span, whether the box settles
         // every tracer's choice (bits in shared memory); spans left open are tested per tracer
         const int nspans = npairs / kPairSpan;
@@ -380,6 +450,7 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
                         px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
                     }
                 } else {
+                    float mx = 0.f;   // largest reciprocal distance of the span
 #pragma unroll
                     for (int u = 0; u < kPairSpan; ++u) {
                         const BodyPair* r = T + k + u;
@@ -393,10 +464,15 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
                         const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
                         float r0, r1;
                         f2_split(RR, r0, r1);
-                        const f2 ri = f2_join(rsqrt_approx(r0), rsqrt_approx(r1));
+                        const float i0 = rsqrt_approx(r0), i1 = rsqrt_approx(r1);
+                        mx = fmax3(mx, i0, i1);
+                        const f2 ri = f2_join(i0, i1);
                         const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
                         px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
                     }
+                    if (mx > inv_near)   // rare: a source of this span lies within the near radius
+                        near_span(T + k, 2 * (tt * kTilePairs + k), XH, XL, YH, YL, ZH, ZL, xr, yr, zr, inv_near,
+                                  Pn, src, px, py, pz, kx, ky, kz);
                 }
                 kahan2(Sx, Cx, px); kahan2(Sy, Cy, py); kahan2(Sz, Cz, pz);
             }
@@ -467,7 +543,10 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
         perm = ms.dust_order.perm;
         boxes = true;
     }
-    dust_rk4_mixed_kernel<<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes);
+    // the source of each pair slot, for the FP64 pulls of near sources: the sources sit in
+    // cell order when the step ordered them (massive_prepare), else slot q holds source q
+    const int* src = ms.slot && spatial_order_on(a) ? ms.src : nullptr;
+    dust_rk4_mixed_kernel<<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes, src);
     return cudaGetLastError();
 }
 

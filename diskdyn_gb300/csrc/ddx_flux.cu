@@ -175,7 +175,7 @@ image_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ 
     if (i >= n_dust) return;
     const int t = n_grav + i;
     const int id = s.id[t];
-    if (id < 0) return;
+    if (id < 0 || id >= o.n_grid) return;
     const double x = s.x[t], y = s.y[t], z = s.z[t];
     const double n = s.N[t];
     const double R = sqrt(x * x + y * y + z * z);
@@ -266,7 +266,7 @@ sed_partial_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
         if (i < n_dust) {
             const int t = n_grav + i;
             id = s.id[t];
-            if (id >= 0) {
+            if (id >= 0 && id < o.n_grid) {
                 const double x = s.x[t], y = s.y[t], z = s.z[t];
                 n = s.N[t];
                 R = sqrt(x * x + y * y + z * z);
@@ -620,7 +620,7 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
     if (i >= n_dust) return;
     const int t = n_grav + i;
     const int id = s.id[t];
-    if (id < 0) return;
+    if (id < 0 || id >= o.n_grid) return;
     const double x = s.x[t], y = s.y[t], z = s.z[t];
     const float xf = d2f_trunc(x), yf = d2f_trunc(y), zf = d2f_trunc(z);
     const float R = sqrtf(fmaf(xf, xf, fmaf(yf, yf, zf * zf)));
@@ -717,7 +717,7 @@ sed_mixed_kernel(ddx_state s, int n_grav, int n_dust, View32 v32, OpticsDev o,
         if (i < n_dust) {
             const int t = n_grav + i;
             const int id = s.id[t];
-            if (id >= 0) {
+            if (id >= 0 && id < o.n_grid) {
                 const double x = s.x[t], y = s.y[t], z = s.z[t];
                 const float xf = d2f_trunc(x), yf = d2f_trunc(y), zf = d2f_trunc(z);
                 const float R = sqrtf(fmaf(xf, xf, fmaf(yf, yf, zf * zf)));

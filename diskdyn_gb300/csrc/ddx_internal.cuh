@@ -29,6 +29,7 @@ struct __align__(16) SizeBin {
 // Scalars of one RK4 step, passed by value to the kernels.
 struct StepArgs {
     int    n_grav, n_dust;
+    int    n_grid;          // size bins; a tracer whose id is outside [0, n_grid) has no bin
     int    n_exact;         // bodies 0..n_exact-1 (star, planets) act in FP64 in the mixed path
     double dt, dt2, dt6;    // dt, dt/2, dt/6 formed exactly as the reference forms them
     int    SWQ, FLQ;
@@ -36,7 +37,28 @@ struct StepArgs {
     int    mode;            // DDX_MODE_*
     int    lose_tile;       // test hook: tile whose copy is never issued (-1: none)
     unsigned long long wait_ns;   // bound on any one device-side wait
+    float  near_eta;        // mixed path: an FP32 source nearer to a body than near_eta times the
+                            // body's largest |coordinate| takes the FP64 pair force instead (0: none)
 };
+
+// Default near radius of the mixed path, relative to the body's largest |coordinate|.
+constexpr float kDefaultNearEta = 4.0e-3f;
+// Largest accepted near radius: far spans (dust kernel) start at half the largest coordinate,
+// so a near source can never sit in a far span.
+constexpr float kMaxNearEta = 0.25f;
+
+// 1 / (near_eta * own): a source is near when its FP32 reciprocal distance exceeds this
+// (infinite when either factor is 0, so nothing is near).
+__device__ __forceinline__ float near_inv(float near_eta, float own) {
+    const float r = near_eta * own;
+    return r > 0.f ? __frcp_rn(r) : INFINITY;
+}
+// Largest of three floats (one sm_100+ instruction); a NaN input is ignored unless all are.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 
 constexpr unsigned long long kDefaultWaitNs = 2000000000ull;   // 2 s
 
@@ -118,9 +140,41 @@ struct MassiveScratch {
     long long part_words;
     // Spatial order of the mixed dust kernel (all null: index order, every span near).
     int      *slot;      // [cap] pair slot of FP32 source k (body n_exact + k), in cell order
+    int      *src;       // [cap] its inverse: FP32 source of pair slot q (written with slot)
     OrderScratch src_order;    // ordering of the FP32 sources (cap bodies)
     OrderScratch dust_order;   // ordering of the tracers of one dust launch
 };
+
+// Makes `device` current for the scope of an entry point and makes the caller's current
+// device current again on every return path, so a host that drives several GPUs from one
+// thread keeps its own choice of device.
+class DeviceGuard {
+  public:
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+        ok_ = cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev_ >= 0) cudaSetDevice(prev_);
+    }
+    bool ok() const { return ok_; }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+  private:
+    int prev_ = -1;
+    bool ok_ = false;
+};
+
+// Mixed massive passes over source slices (ddx_step.cu): targets per block, and the blocks
+// per SM the slices aim at.  The slice sums of a system of up to cap bodies on a GPU with
+// sms SMs take massive_part_words_for(cap, sms) doubles: S slices * np targets with
+// S <= kSliceBlocksPerSM * sms / groups + 1, so S * np <= (kSliceBlocksPerSM * sms + groups) * 256.
+constexpr int kSliceThreads = 256;
+constexpr int kSliceBlocksPerSM = 4;
+constexpr long long massive_part_words_for(int cap, int sms) {
+    return 6LL * kSliceThreads * ((long long)kSliceBlocksPerSM * sms + (cap + kSliceThreads - 1) / kSliceThreads);
+}
 
 // Bits of the device status word.
 constexpr int kStatusTimeout = 1;   // a bounded mbarrier wait gave up
@@ -188,7 +242,8 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
 cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
                         const SizeBin* bins, int precision, cudaStream_t st);
 // Source slices of the mixed massive passes for n_grav bodies (about four blocks per SM),
-// and the doubles of MassiveScratch::part that cover every system of up to cap bodies.
+// and the doubles of MassiveScratch::part that cover every system of up to cap bodies on
+// this device (massive_part_words_for with its SM count).
 int massive_slices(int n_grav, int n_exact);
 long long massive_part_words(int cap);
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,

@@ -31,8 +31,11 @@ constexpr size_t kOffA = kOffPP + align256(sizeof(BodyPair) * 4 * kPcap);
 constexpr size_t kOffR = kOffA + align256(sizeof(double) * 12 * kCap);
 constexpr size_t kOffBins = kOffR + align256(sizeof(double) * 9 * kCap);
 constexpr size_t kOffStatus = kOffBins + align256(sizeof(SizeBin) * DDX_MAX_SIZE_BINS);
-// slice sums of the mixed passes: massive_part_words(kCap) for up to 160 SMs
-constexpr long long kPartWords = 6LL * 256 * (4LL * 160 + (kCap + 255) / 256);
+// Slice sums of the mixed massive passes for GPUs of up to kMaxSMs SMs (GB300 has 152).  On a
+// GPU with more, the passes find the region too small (sliced_fits) and take the
+// one-warp-per-target form instead: the same sums, slower.
+constexpr int kMaxSMs = 160;
+constexpr long long kPartWords = massive_part_words_for(kCap, kMaxSMs);
 constexpr size_t kOffPart = kOffStatus + 256;
 constexpr size_t kBytes = kOffPart + align256(sizeof(double) * kPartWords);
 
@@ -42,6 +45,17 @@ static __device__ __align__(256) unsigned char g_step_scratch[kBytes];
 // current.  In host code the symbol itself is only a host-side stand-in.
 std::mutex g_mu;
 void* g_addr[128] = {};
+// Failure-detection test hook: per device, the tile whose copy the next mixed call leaves
+// unissued (-1: none) and the bound on its waits.
+int g_lose_tile[128];
+unsigned long long g_lose_wait[128];
+bool g_hooks_init = false;
+
+void hooks_init() {
+    if (g_hooks_init) return;
+    for (int d = 0; d < 128; ++d) g_lose_tile[d] = -1, g_lose_wait[d] = 0;
+    g_hooks_init = true;
+}
 
 int scratch_address(int device, unsigned char** out) {
     if (device < 0 || device >= 128) return DDX_ERR_ARG;
@@ -52,6 +66,10 @@ int scratch_address(int device, unsigned char** out) {
             cudaGetLastError();
             return DDX_ERR_CUDA;
         }
+        // the status word starts cleared (one word, set once per device, before any step)
+        if (cudaMemset(static_cast<unsigned char*>(p) + kOffStatus, 0, sizeof(int)) != cudaSuccess ||
+            cudaDeviceSynchronize() != cudaSuccess)
+            return DDX_ERR_CUDA;
         g_addr[device] = p;
     }
     *out = static_cast<unsigned char*>(g_addr[device]);
@@ -87,7 +105,9 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
     if (p->n_planets < 0 || p->n_planets > n_grav) return DDX_ERR_ARG;
     if (n_grav > DDX_NOALLOC_MAX_GRAV || n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
-    if (cudaSetDevice(device) != cudaSuccess) return DDX_ERR_CUDA;
+    if (device < 0 || device >= 128) return DDX_ERR_ARG;
+    DeviceGuard dg(device);
+    if (!dg.ok()) return DDX_ERR_CUDA;
     unsigned char* base = nullptr;
     int r = scratch_address(device, &base);
     if (r) return r;
@@ -123,10 +143,22 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     a.mode = mode;
     a.lose_tile = -1;
     a.wait_ns = kDefaultWaitNs;
+    if (precision == DDX_PREC_MIXED) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        hooks_init();
+        if (g_lose_tile[device] >= 0) {
+            a.lose_tile = g_lose_tile[device];
+            a.wait_ns = g_lose_wait[device];
+            g_lose_tile[device] = -1;
+        }
+    }
+    a.near_eta = kDefaultNearEta;
+    a.n_grid = n_grid;
 
     // Every scratch word a step reads is written earlier in the same step (the packed bins,
     // then the stage records of bodies 0..n_grav-1), so nothing has to be cleared between
-    // calls.
+    // calls.  The status word alone carries over: kernels only set its bits, and
+    // ddx_noalloc_sync_status reads and clears it (the array starts zeroed).
     cudaStream_t st = (cudaStream_t)stream;
     pack_bins_kernel<<<(n_grid + 255) / 256, 256, 0, st>>>(bins, n_grid, beta, betasw, q);
     if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
@@ -140,4 +172,30 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     if (launch_massive_pass1(sv, a, ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (launch_massive_pass2(sv, a, ms, precision, st) != cudaSuccess) return DDX_ERR_CUDA;
     return launch_dust(sv, a, ms, bins, precision, st) == cudaSuccess ? DDX_OK : DDX_ERR_CUDA;
+}
+
+extern "C" int ddx_noalloc_sync_status(int device, void* stream) {
+    if (device < 0 || device >= 128) return DDX_ERR_ARG;
+    DeviceGuard dg(device);
+    if (!dg.ok()) return DDX_ERR_CUDA;
+    unsigned char* base = nullptr;
+    int r = scratch_address(device, &base);
+    if (r) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    int* status = reinterpret_cast<int*>(base + kOffStatus);
+    int h = 0;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return DDX_ERR_CUDA;
+    // a plain copy into a host int and a memset of the one word: no allocation
+    if (cudaMemcpy(&h, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DDX_ERR_CUDA;
+    if (h != 0 && cudaMemset(status, 0, sizeof(int)) != cudaSuccess) return DDX_ERR_CUDA;
+    return (h & kStatusTimeout) ? DDX_ERR_TIMEOUT : DDX_OK;
+}
+
+extern "C" int ddx_debug_noalloc_lose_tile_copy(int device, int tile, unsigned long long wait_ns) {
+    if (device < 0 || device >= 128 || tile < 0 || wait_ns == 0) return DDX_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_mu);
+    hooks_init();
+    g_lose_tile[device] = tile;
+    g_lose_wait[device] = wait_ns;
+    return DDX_OK;
 }

@@ -39,7 +39,8 @@ __global__ void fma64_kernel(double* out, double a, double b) {
 
 extern "C" int ddx_probe_fma_peak(int device, double* fp32_tflops, double* fp64_tflops) {
     if (!fp32_tflops || !fp64_tflops) return DDX_ERR_ARG;
-    if (cudaSetDevice(device) != cudaSuccess) return DDX_ERR_CUDA;
+    ddx::DeviceGuard dg(device);
+    if (!dg.ok()) return DDX_ERR_CUDA;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int threads = 256, blocks = sms * 8;

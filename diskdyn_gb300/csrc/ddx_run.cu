@@ -214,7 +214,7 @@ extern "C" int ddx_run(ddx_ctx* ctx, const ddx_state* s, int n_grav, int n_dust,
     if (nwavs > 0 && !wj) return DDX_ERR_ARG;
     if (!(dt > 0.0) || !(cad->t_write > 0.0) || !(cad->t_fits > 0.0) || !(cad->t_sed > 0.0)) return DDX_ERR_ARG;
     if (ddx::ctx_optics_n_wav(ctx) == 0) return DDX_ERR_STATE;
-    cudaSetDevice(ddx::ctx_device(ctx));
+    ddx::DeviceGuard dg(ddx::ctx_device(ctx));
     cudaStream_t st = (cudaStream_t)stream;
     Runner run(ctx, *s, n_grav, n_dust, precision, mode, *view, wj, nwavs, fn, user, st);
     int r = run.init();

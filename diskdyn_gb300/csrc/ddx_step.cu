@@ -31,6 +31,7 @@ constexpr float kFarAway = 1.0e18f;  // padding source position, AU (mass 0)
 __device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, int k, const float4 h,
                                                 const float4 l) {
     const int q = ms.slot ? ms.slot[k] : k;
+    if (stage == 0 && ms.slot) ms.src[q] = k;     // the inverse, for the FP64 pulls of near sources
     BodyPair* r = ms.PP + (size_t)stage * ms.pcap + (q >> 1);
     const int u = q & 1;
     r->hx[u] = h.x; r->hy[u] = h.y; r->hz[u] = h.z; r->m[u] = h.w;
@@ -107,18 +108,22 @@ __device__ __forceinline__ void pair64(const Body pi, const Body pj, double& ax,
 }
 
 // Same in FP32 on hi/lo split positions: the difference (hi_j - hi_i) + (lo_j - lo_i)
-// keeps FP32 relative precision in the separation even when |x| >> |x_j - x_i|.
-__device__ __forceinline__ void pair32(const float4 hi, const float4 li, const float4 hj,
-                                       const float4 lj, float& fx, float& fy, float& fz) {
+// keeps FP32 relative precision in the separation even when |x| >> |x_j - x_i|.  Returns
+// true, adding nothing, when the source lies within the near radius (reciprocal distance
+// above inv_near): the caller takes that pull in FP64.
+__device__ __forceinline__ bool pair32(const float4 hi, const float4 li, const float4 hj,
+                                       const float4 lj, float inv_near, float& fx, float& fy, float& fz) {
     const float dX = (hj.x - hi.x) + (lj.x - li.x);
     const float dY = (hj.y - hi.y) + (lj.y - li.y);
     const float dZ = (hj.z - hi.z) + (lj.z - li.z);
     const float RR = fmaf(dX, dX, fmaf(dY, dY, dZ * dZ));
     if (RR > 0.f) {
         const float ri = rsqrtf(RR);
+        if (ri > inv_near) return true;
         const float f = hj.w * (ri * (ri * ri));
         fx = fmaf(f, dX, fx); fy = fmaf(f, dY, fy); fz = fmaf(f, dZ, fz);
     }
+    return false;
 }
 
 // One warp per target body i, lanes stride over the sources, fixed-order butterfly
@@ -127,8 +132,8 @@ __device__ __forceinline__ void pair32(const float4 hi, const float4 li, const f
 // (sources 0..n_exact-1) stay FP64; the pulls of the planetesimals run in FP32 with a
 // per-lane Kahan sum.
 template <int PREC>
-__device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms, int ng, int n_exact, int i,
-                                                         int sa, int sb, double a_out[6]) {
+__device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms, int ng, int n_exact, float near_eta,
+                                                         int i, int sa, int sb, double a_out[6]) {
     const int lane = threadIdx.x & 31;
     double ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
     const Body pa = ms.P[sa * ms.cap + i];
@@ -144,6 +149,8 @@ __device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms
         float Sb[3] = {0.f, 0.f, 0.f}, Cb[3] = {0.f, 0.f, 0.f};
         const float4 ha = ms.Phi[sa * ms.cap + i], la = ms.Plo[sa * ms.cap + i];
         const float4 hb = ms.Phi[sb * ms.cap + i], lb = ms.Plo[sb * ms.cap + i];
+        const float inv_a = near_inv(near_eta, fmaxf(fabsf(ha.x), fmaxf(fabsf(ha.y), fabsf(ha.z))));
+        const float inv_b = near_inv(near_eta, fmaxf(fabsf(hb.x), fmaxf(fabsf(hb.y), fabsf(hb.z))));
         for (int j = lane; j < ng; j += 32) {
             if (j == i) continue;
             if (i == 0 || j < n_exact) {
@@ -151,10 +158,12 @@ __device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms
                 pair64(pb, ms.P[sb * ms.cap + j], bx, by, bz);
             } else {
                 float fx = 0.f, fy = 0.f, fz = 0.f;
-                pair32(ha, la, ms.Phi[sa * ms.cap + j], ms.Plo[sa * ms.cap + j], fx, fy, fz);
+                if (pair32(ha, la, ms.Phi[sa * ms.cap + j], ms.Plo[sa * ms.cap + j], inv_a, fx, fy, fz))
+                    pair64(pa, ms.P[sa * ms.cap + j], ax, ay, az);   // within the near radius: FP64
                 kahan_add(Sa[0], Ca[0], fx); kahan_add(Sa[1], Ca[1], fy); kahan_add(Sa[2], Ca[2], fz);
                 fx = fy = fz = 0.f;
-                pair32(hb, lb, ms.Phi[sb * ms.cap + j], ms.Plo[sb * ms.cap + j], fx, fy, fz);
+                if (pair32(hb, lb, ms.Phi[sb * ms.cap + j], ms.Plo[sb * ms.cap + j], inv_b, fx, fy, fz))
+                    pair64(pb, ms.P[sb * ms.cap + j], bx, by, bz);
                 kahan_add(Sb[0], Cb[0], fx); kahan_add(Sb[1], Cb[1], fy); kahan_add(Sb[2], Cb[2], fz);
             }
         }
@@ -205,7 +214,7 @@ __global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.n_grav) return;  // warp-uniform
     double acc[6];
-    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 0, 1, acc);
+    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, a.near_eta, i, 0, 1, acc);
     if ((threadIdx.x & 31) != 0) return;
     pass1_update(s, a, ms, i, acc, PREC);
 }
@@ -235,7 +244,7 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.n_grav) return;
     double acc[6];
-    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, i, 2, 3, acc);
+    massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, a.near_eta, i, 2, 3, acc);
     if ((threadIdx.x & 31) != 0) return;
     pass2_update(s, a, ms, i, acc);
 }
@@ -254,9 +263,7 @@ __global__ void massive_pass2_kernel(ddx_state s, StepArgs a, MassiveScratch ms)
 // whole block (a fixed-order tree sum).  massive_gather_kernel then adds the slices (a
 // fixed lane order: deterministic), adds the FP64 pulls of bodies 0..n_exact-1 and applies
 // the pass's update.
-constexpr int kSliceThreads = 256;
 constexpr int kSliceTile = 256;       // pair records per stage staged at once (16 KiB)
-constexpr int kSliceBlocksPerSM = 4;  // slices are chosen to give about this many blocks per SM
 constexpr int kMaxSlices = 64;
 
 __device__ __forceinline__ void pair_f2(const BodyPair& r, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH, f2 ZL, f2& px,
@@ -274,6 +281,64 @@ __device__ __forceinline__ void pair_f2(const BodyPair& r, f2 XH, f2 XL, f2 YH, 
     const f2 ri = f2_join(r0 > 0.f ? rsqrt_approx(r0) : 0.f, r1 > 0.f ? rsqrt_approx(r1) : 0.f);
     const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
     px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+}
+
+// pair_f2 that also raises mx to the larger reciprocal distance of the two sources (0 for
+// a coincident source, the target's own slot included, so it never counts as near).
+__device__ __forceinline__ void pair_f2_max(const BodyPair& r, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH, f2 ZL, f2& px,
+                                            f2& py, f2& pz, float& mx) {
+    const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r.hx);   // hx, hy
+    const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r.hz);   // hz, m
+    const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r.lx);   // lx, ly
+    const f2 lz = *reinterpret_cast<const f2*>(r.lz);
+    const f2 dX = add2(sub2(q0.x, XH), sub2(q2.x, XL));
+    const f2 dY = add2(sub2(q0.y, YH), sub2(q2.y, YL));
+    const f2 dZ = add2(sub2(q1.x, ZH), sub2(lz, ZL));
+    const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+    float r0, r1;
+    f2_split(RR, r0, r1);
+    const float i0 = r0 > 0.f ? rsqrt_approx(r0) : 0.f, i1 = r1 > 0.f ? rsqrt_approx(r1) : 0.f;
+    mx = fmax3(mx, i0, i1);
+    const f2 ri = f2_join(i0, i1);
+    const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
+    px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+}
+
+// One span of kPairSpan pair records (slots q0 ..) summed again for a target with a source
+// within the near radius (reciprocal FP32 distance above inv_near): the FP32 partial sum of
+// the other sources, with the same operations as pair_f2_max, and the FP64 pull of each near
+// source from the FP64 stage records (P: bodies n_exact.. of the stage; src: source of each
+// slot, null when slot q holds source q) on the target's FP64 stage position pt, added to n.
+// The target's own slot is never near (its reciprocal distance is 0).
+__device__ __forceinline__ void near_span_massive(const BodyPair* R, int q0, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH,
+                                                  f2 ZL, float inv_near, const Body pt, const Body* __restrict__ P,
+                                                  const int* __restrict__ src, f2& px, f2& py, f2& pz,
+                                                  double n[3]) {
+    px = 0; py = 0; pz = 0;
+    for (int u = 0; u < kPairSpan; ++u) {
+        const BodyPair& r = R[u];
+        const ulonglong2 q0v = *reinterpret_cast<const ulonglong2*>(r.hx);
+        const ulonglong2 q1v = *reinterpret_cast<const ulonglong2*>(r.hz);
+        const ulonglong2 q2v = *reinterpret_cast<const ulonglong2*>(r.lx);
+        const f2 lz = *reinterpret_cast<const f2*>(r.lz);
+        const f2 dX = add2(sub2(q0v.x, XH), sub2(q2v.x, XL));
+        const f2 dY = add2(sub2(q0v.y, YH), sub2(q2v.y, YL));
+        const f2 dZ = add2(sub2(q1v.x, ZH), sub2(lz, ZL));
+        const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
+        float r0, r1;
+        f2_split(RR, r0, r1);
+        const float i0 = r0 > 0.f ? rsqrt_approx(r0) : 0.f, i1 = r1 > 0.f ? rsqrt_approx(r1) : 0.f;
+        const bool n0 = i0 > inv_near, n1 = i1 > inv_near;
+        const f2 ri = f2_join(n0 ? 0.f : i0, n1 ? 0.f : i1);
+        const f2 f = mul2(mul2(q1v.y, ri), mul2(ri, ri));
+        px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!(h ? n1 : n0)) continue;
+            const int q = q0 + 2 * u + h;
+            pair64(pt, P[src ? src[q] : q], n[0], n[1], n[2]);
+        }
+    }
 }
 
 // Deterministic block sum of v (fixed tree order); the result in thread 0.
@@ -327,6 +392,10 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, dou
     const f2 XHb = f2_dup(hb.x), XLb = f2_dup(lb.x), YHb = f2_dup(hb.y), YLb = f2_dup(lb.y);
     const f2 ZHb = f2_dup(hb.z), ZLb = f2_dup(lb.z);
     f2 SA[3] = {0, 0, 0}, CA[3] = {0, 0, 0}, SB[3] = {0, 0, 0}, CB[3] = {0, 0, 0};
+    // near sources: FP64 pulls, summed apart and added to the slice's total
+    const float inv_a = near_inv(a.near_eta, fmaxf(fabsf(ha.x), fmaxf(fabsf(ha.y), fabsf(ha.z))));
+    const float inv_b = near_inv(a.near_eta, fmaxf(fabsf(hb.x), fmaxf(fabsf(hb.y), fabsf(hb.z))));
+    double NA[3] = {0.0, 0.0, 0.0}, NB[3] = {0.0, 0.0, 0.0};
     for (int t0 = r0; t0 < r1; t0 += kSliceTile) {
         const int cnt = min(kSliceTile, r1 - t0);          // a multiple of kPairSpan
         __syncthreads();                                   // the previous tile is consumed
@@ -342,19 +411,28 @@ massive_slice_kernel(StepArgs a, MassiveScratch ms, int sa, int per, int np, dou
         if (!active) continue;
         for (int u0 = 0; u0 < cnt; u0 += kPairSpan) {
             f2 ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+            float mxa = 0.f, mxb = 0.f;
 #pragma unroll 4
             for (int u = 0; u < kPairSpan; ++u) {
-                pair_f2(tile[0][u0 + u], XHa, XLa, YHa, YLa, ZHa, ZLa, ax, ay, az);
-                pair_f2(tile[1][u0 + u], XHb, XLb, YHb, YLb, ZHb, ZLb, bx, by, bz);
+                pair_f2_max(tile[0][u0 + u], XHa, XLa, YHa, YLa, ZHa, ZLa, ax, ay, az, mxa);
+                pair_f2_max(tile[1][u0 + u], XHb, XLb, YHb, YLb, ZHb, ZLb, bx, by, bz, mxb);
             }
+            if (mxa > inv_a)   // rare: a source of this span within the near radius at stage sa
+                near_span_massive(&tile[0][u0], 2 * (t0 + u0), XHa, XLa, YHa, YLa, ZHa, ZLa, inv_a, ms.P[sa * c + i],
+                                  ms.P + (size_t)sa * c + a.n_exact, ms.slot ? ms.src : nullptr, ax, ay, az, NA);
+            if (mxb > inv_b)
+                near_span_massive(&tile[1][u0], 2 * (t0 + u0), XHb, XLb, YHb, YLb, ZHb, ZLb, inv_b, ms.P[sb * c + i],
+                                  ms.P + (size_t)sb * c + a.n_exact, ms.slot ? ms.src : nullptr, bx, by, bz, NB);
             kahan2(SA[0], CA[0], ax); kahan2(SA[1], CA[1], ay); kahan2(SA[2], CA[2], az);
             kahan2(SB[0], CB[0], bx); kahan2(SB[1], CB[1], by); kahan2(SB[2], CB[2], bz);
         }
     }
     if (!active) return;
     double* o = part + (size_t)k * 6 * np + i;
-    o[0] = f2_total(SA[0], CA[0]); o[np] = f2_total(SA[1], CA[1]); o[2 * np] = f2_total(SA[2], CA[2]);
-    o[3 * np] = f2_total(SB[0], CB[0]); o[4 * np] = f2_total(SB[1], CB[1]); o[5 * np] = f2_total(SB[2], CB[2]);
+    o[0] = f2_total(SA[0], CA[0]) + NA[0]; o[np] = f2_total(SA[1], CA[1]) + NA[1];
+    o[2 * np] = f2_total(SA[2], CA[2]) + NA[2];
+    o[3 * np] = f2_total(SB[0], CB[0]) + NB[0]; o[4 * np] = f2_total(SB[1], CB[1]) + NB[1];
+    o[5 * np] = f2_total(SB[2], CB[2]) + NB[2];
 }
 
 // 32 targets per block of 8 warps.  Each warp adds the slices of 4 targets (the lanes take
@@ -482,7 +560,7 @@ dust_rk4_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __res
             vx = s.vx[t]; vy = s.vy[t]; vz = s.vz[t];
             m = s.m[t];
             const int id = s.id[t];
-            if (id >= 0) {
+            if (id >= 0 && id < a.n_grid) {
                 const SizeBin b = bins[id];
                 bet = b.beta; betsw = b.betasw; qe = b.q;
             }
@@ -613,12 +691,8 @@ int massive_slices(int n_grav, int n_exact) {
     return S < 1 ? 1 : S;
 }
 
-// S * np <= (2 SMs / groups + 1) * groups * kSliceThreads, which grows with the groups, so
-// the bound at the capacity covers every smaller system.
-long long massive_part_words(int cap) {
-    const long long groups = (cap + kSliceThreads - 1) / kSliceThreads;
-    return 6LL * kSliceThreads * ((long long)kSliceBlocksPerSM * sm_count() + groups);
-}
+// The bound grows with the groups, so the bound at the capacity covers every smaller system.
+long long massive_part_words(int cap) { return massive_part_words_for(cap, sm_count()); }
 
 cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                  int precision, cudaStream_t st) {

@@ -309,6 +309,11 @@ class Engine:
         abi.check(r, "ddx_run")
         return {k: getattr(cad, k) for k in ("time", "tlastd", "tlastf", "tlasts")}
 
+    def set_near_radius(self, eta: float) -> None:
+        """Mixed precision: planetesimals nearer to a body than eta times its largest
+        |coordinate| take the FP64 pair force (0 turns that off)."""
+        abi.check(self.lib.ddx_set_near_radius(self.ctx, C.c_double(eta)), "ddx_set_near_radius")
+
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a
         bounded device-side wait since the last call, else 0."""

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define DDX_ABI_VERSION 3
+#define DDX_ABI_VERSION 4
 
 /* Status codes.  The reference exits the process instead (src/error.cu:75-91,
  * src/ddyn.cuh:400-408). */
@@ -37,7 +37,9 @@ extern "C" {
 /* Arithmetic of the force stage. */
 #define DDX_PREC_FP64   0   /* every operation in FP64, like the reference */
 #define DDX_PREC_MIXED  1   /* FP64 state, Kepler term and stage combination; FP32
-                               body-body perturbations with compensated sums */
+                               body-body perturbations with compensated sums, except
+                               for sources within the near radius (ddx_set_near_radius),
+                               which take the FP64 pair force */
 
 /* Behaviour switch for the reference's known defects. */
 #define DDX_MODE_FIXED      0   /* defects corrected (default) */
@@ -89,8 +91,10 @@ typedef struct {
 
 typedef struct ddx_ctx ddx_ctx;
 
-/* Create a context on `device` (cudaSetDevice is called on it).  Replaces the buffer
- * ownership of Grid::allocgpu (src/init.cu:543-602); scratch grows on demand. */
+/* Create a context on `device`.  Replaces the buffer ownership of Grid::allocgpu
+ * (src/init.cu:543-602); scratch grows on demand.  Every entry point makes its device (the
+ * context's, or the `device` argument) current while it runs and makes the caller's
+ * current device current again before it returns. */
 int ddx_create(ddx_ctx **out, int device);
 int ddx_destroy(ddx_ctx *ctx);
 
@@ -160,14 +164,33 @@ int ddx_evolve(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double 
  * the rounding of the FP32 perturbations.
  *
  * The first call on a device resolves the array's device address (cudaGetSymbolAddress
- * with that device current).  Make that first call before any stream capture.  All
- * calls share the one array, so calls that overlap on the GPU (different streams,
- * different host threads) race; serialise them.  Each call writes every scratch word it
- * reads, so nothing carries over from the previous call. */
+ * with that device current) and clears its status word (a synchronous one-word memset).
+ * Make that first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU (different streams, different host threads) race;
+ * serialise them.  Each call writes every scratch word it reads, so no result carries over
+ * from the previous call, with one exception: the status word, in which a mixed-precision
+ * dust block that gave up a bounded wait (its tracers left unchanged) sets a bit.  That
+ * word collects these reports over calls until ddx_noalloc_sync_status reads and clears it.
+ * A call returns before its kernels finish, so it cannot report them itself.
+ * On a GPU with more than 160 SMs the mixed massive passes take their one-warp-per-target
+ * form here (the same sums, slower), because the fixed array holds the slice sums for 160. */
 #define DDX_NOALLOC_MAX_GRAV 8192
 int ddx_step_noalloc(int device, const ddx_state *s, int n_grav, int n_dust, double dt,
                      const ddx_phys *phys, int n_grid, const float *beta, const float *betasw,
                      const float *q, int precision, int mode, void *stream);
+
+/* Synchronises `stream` on `device` and reports whether a kernel of ddx_step_noalloc on that
+ * device gave up a bounded wait since the last call of this function: DDX_ERR_TIMEOUT if so
+ * (the tracers of the blocks concerned were left unchanged), DDX_OK otherwise.  Clears the
+ * report.  Allocates nothing: one 4-byte copy to a host variable.  No counterpart in the
+ * reference, whose kernels have no waits. */
+int ddx_noalloc_sync_status(int device, void *stream);
+
+/* Failure-detection test hook of ddx_step_noalloc (no counterpart in the reference): the
+ * next mixed-precision call on `device` leaves the TMA copy of source tile `tile` unissued
+ * and bounds its waits by wait_ns, as ddx_debug_lose_tile_copy does for a context.  Nothing
+ * faults or hangs. */
+int ddx_debug_noalloc_lose_tile_copy(int device, int tile, unsigned long long wait_ns);
 
 /* Images at the table wavelengths wj[0..n_img-1]: scattered + thermal flux of every
  * dust tracer with id >= 0, projected through `view` and summed into
@@ -313,6 +336,17 @@ int ddx_probe_fma_peak(int device, double *fp32_tflops, double *fp64_tflops);
  * blocks concerned were left unchanged), DDX_OK otherwise.  Clears the report.  No
  * counterpart in the reference, whose kernels have no waits. */
 int ddx_sync_status(ddx_ctx *ctx, void *stream);
+
+/* Near radius of DDX_PREC_MIXED (no counterpart in the reference, which is FP64 throughout).
+ * FP32 leaves about 5.6e-7 of relative error in each planetesimal pull, and a close
+ * encounter amplifies it along the trajectory.  So in the mixed step a planetesimal nearer
+ * to a body (tracer or massive) than eta times that body's largest |coordinate| at the RK4
+ * stage takes the FP64 pair force from the FP64 stage positions, as in DDX_PREC_FP64;
+ * every other planetesimal stays FP32.  The test uses the FP32 distance, so the choice is
+ * deterministic.  Default 4e-3 (0.52 AU at 130 AU); 0 turns the FP64 pulls off;
+ * 0 <= eta <= 0.25, else DDX_ERR_ARG.  Applies to later steps of this context;
+ * ddx_step_noalloc always uses the default. */
+int ddx_set_near_radius(ddx_ctx *ctx, double eta);
 
 /* Failure-detection test hook (no counterpart in the reference).  The next mixed-precision
  * dust launch of this context leaves the TMA copy of source tile `tile` (counted over the

@@ -37,7 +37,7 @@ def test_python_binding_covers_header(built_lib):
 def test_status_strings_and_version(built_lib):
     from diskdyn_gb300 import abi
     lib = abi.load()
-    assert lib.ddx_abi_version() == 3
+    assert lib.ddx_abi_version() == 4
     assert lib.ddx_status_string(0) == b"ok"
     assert lib.ddx_status_string(5) == b"size beyond limit"
     assert lib.ddx_status_string(99) == b"unknown status"
@@ -54,6 +54,10 @@ def test_argument_errors_without_gpu(built_lib):
     assert lib.ddx_set_size_table(None, 1, None, None, None, None) == 1
     assert lib.ddx_image(None, C.byref(st), 1, 0, None, None, 1, None, 0, None) == 1
     assert lib.ddx_sed(None, C.byref(st), 1, 0, None, None, 0, 0, None) == 1
+    assert lib.ddx_set_near_radius(None, C.c_double(1e-3)) == 1
+    assert lib.ddx_noalloc_sync_status(-1, None) == 1
+    assert lib.ddx_debug_noalloc_lose_tile_copy(0, -1, 1000) == 1
+    assert lib.ddx_debug_noalloc_lose_tile_copy(0, 0, 0) == 1
 
 
 def test_argument_errors_of_the_setup_and_run_calls_without_gpu(built_lib):

@@ -59,6 +59,31 @@ def test_noalloc_step_matches_ddx_step_twice(built_lib, prec, mode):
     eng.close()
 
 
+def test_noalloc_reports_a_wait_that_ran_out(built_lib):
+    """A mixed call whose bounded wait runs out (the test hook leaves one tile's copy
+    unissued and bounds the waits by 20 ms) leaves every tracer unchanged and is reported
+    once by ddx_noalloc_sync_status; the next call steps normally and reports nothing."""
+    lib = abi.load()
+    sysm = synth.dusty_ring(n_dust=2048, n_plsml=256, seed=7, n_steps=2)
+    tab = {k: torch.tensor(np.asarray(sysm.size_table[k], np.float32), device="cuda")
+           for k in ("beta", "betasw", "q")}
+    st = DeviceState.from_numpy(sysm.state)
+    h = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib.ddx_noalloc_sync_status(0, h)                      # nothing pending from earlier calls
+    ng = sysm.n_grav
+    before = st.to_numpy()
+    abi.check(lib.ddx_debug_noalloc_lose_tile_copy(0, 1, 20_000_000), "inject")
+    noalloc_step(lib, st, sysm, tab, abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)
+    assert lib.ddx_noalloc_sync_status(0, h) == abi.DDX_ERR_TIMEOUT
+    after = st.to_numpy()
+    for f in ("x", "y", "z", "vx", "vy", "vz", "N"):
+        assert np.array_equal(after[f][ng:], before[f][ng:]), f
+    assert lib.ddx_noalloc_sync_status(0, h) == abi.DDX_OK   # the report was cleared
+    noalloc_step(lib, st, sysm, tab, abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)
+    assert lib.ddx_noalloc_sync_status(0, h) == abi.DDX_OK
+    assert not np.array_equal(st.to_numpy()["x"][ng:], before["x"][ng:])
+
+
 def test_noalloc_rejects_sizes_beyond_its_limit(built_lib):
     lib = abi.load()
     sysm = synth.solar_like(n_dust=8)
