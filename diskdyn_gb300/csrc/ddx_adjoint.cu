@@ -532,7 +532,7 @@ __device__ __forceinline__ void tracer_geometry(double x, double y, double z, in
     const double num = x1 * x1 + y1 * y1 + z * z - y1 * v.ly0 - z * v.lz0;
     double c = num / (R * L);
     g.clamped = false;
-    if (c < -1) { c = -1.0; g.clamped = true; }
+    if (!(c >= -1)) { c = -1.0; g.clamped = true; }   // NaN too: the table index stays in range
     if (c >= 1.0 - 2.0 / v.ntheta) { c = 1.0 - 2.0 / v.ntheta; g.clamped = true; }
     g.cossc = c;
     const double p[3] = {x1, y1, z}, l0[3] = {0.0, v.ly0, v.lz0}, q[3] = {qx, qy, qz};
@@ -557,13 +557,14 @@ __device__ __forceinline__ void tracer_geometry(double x, double y, double z, in
     g.dw[2] = dYdz / v.psca;
     // temperature (log-log in R on the nR grid) and its slope
     const double* Td = o.Td + (size_t)id * kNR;
-    if (R <= o.Rmin) { g.T = Td[0]; g.dTdR = 0.0; }
+    if (!(R > o.Rmin)) { g.T = Td[0]; g.dTdR = 0.0; }   // R <= Rmin, or NaN: no table index from it
     else if (R >= o.Rmax) { g.T = Td[kNR - 1]; g.dTdR = 0.0; }
     else {
         const double* lT = o.lTd + (size_t)id * kNR;
         const double lr = log(R / o.Rmin);
         int k = (int)(lr / o.fR) + 1;
         if (k > kNR - 1) k = kNR - 1;
+        if (k < 1) k = 1;
         const double frac = (lr - (k - 1) * o.fR) / o.fR;
         g.T = exp(lT[k - 1] + (lT[k] - lT[k - 1]) * frac);
         g.dTdR = g.T * (lT[k] - lT[k - 1]) / (o.fR * R);

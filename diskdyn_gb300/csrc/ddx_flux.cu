@@ -112,7 +112,7 @@ __device__ __forceinline__ double scatter_cos(double x1, double y1, double z, do
     const double ly = v.ly0 - y1;
     const double lz = v.lz0 - z;
     double cossc = (x1 * x1 + (-y1) * ly + (-z) * lz) / R / sqrt(x1 * x1 + ly * ly + lz * lz);
-    if (cossc < -1) cossc = -1.0;
+    if (!(cossc >= -1)) cossc = -1.0;            // also a NaN cosine: a table index from it stays in range
     if (cossc >= 1.0 - 2.0 / v.ntheta) cossc = 1.0 - 2.0 / v.ntheta;
     return cossc;
 }
@@ -121,12 +121,13 @@ __device__ __forceinline__ double scatter_cos(double x1, double y1, double z, do
 // (src/gpu_functions.cu:1049-1063), using the table of log T built at set-up.
 __device__ __forceinline__ double dust_temperature(double R, int id, const OpticsDev& o) {
     const double* Td = o.Td + (size_t)id * kNR;
-    if (R <= o.Rmin) return Td[0];
+    if (!(R > o.Rmin)) return Td[0];             // R <= Rmin, or NaN: no table index from it
     if (R >= o.Rmax) return Td[kNR - 1];
     const double* lTd = o.lTd + (size_t)id * kNR;
     const double lr = log(R / o.Rmin);
     int Rid = (int)(lr / o.fR) + 1;
     if (Rid > kNR - 1) Rid = kNR - 1;
+    if (Rid < 1) Rid = 1;
     const double frac = (lr - (Rid - 1) * o.fR) / o.fR;
     return exp(lTd[Rid - 1] + (lTd[Rid] - lTd[Rid - 1]) * frac);
 }

@@ -13,7 +13,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
-REFSRC = Path("/root/reference/src")
+from .paths import SRC as REFSRC
 EXE = OUT / "param_dump"
 OPTICS_EXE = OUT / "optics_dump"
 UNITS = ("read_in", "functions", "ran3", "error", "print", "getMemorySize")

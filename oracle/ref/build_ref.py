@@ -17,7 +17,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
-REFSRC = Path("/root/reference/src")
+from .paths import SRC as REFSRC
 CUBIN = OUT / "ddyn_ref_sm103a.cubin"
 RUNNER = OUT / "libref_runner.so"
 

@@ -63,7 +63,8 @@ CASES = {
 
 def usage_messages() -> list[str]:
     """errmsg[] of the reference (src/error.cu), to name the code of an exit message."""
-    txt = Path("/root/reference/src/error.cu").read_text()
+    from oracle.ref.paths import SRC
+    txt = (SRC / "error.cu").read_text()
     body = txt[txt.index("errmsg"):]
     body = body[body.index("{") + 1: body.index("};")]
     return [m.replace("\\n", "").strip() for m in re.findall(r'"((?:[^"\\]|\\.)*)"', body)]

@@ -1,0 +1,119 @@
+"""Parity at the benchmark configurations' own sizes, through the C ABI.
+
+- Solar-system run: 9 massive bodies + 16,384 tracers, all 1,000 FP64 steps (dt 0.05 yr)
+  against the FP64 oracle.
+- Dusty ring: the full massive set (star, 2 planets, 4,096 gravitating planetesimals, so
+  the mixed step orders its sources and tracers in space and takes far spans) with a
+  4,096-grain shard: mixed precision against the oracle over 5 steps, and the FP64 step
+  in the reference's arithmetic against the reference's own kernels over 3 steps.
+- Imaging: all 4,194,304 tracers at 1024 x 1024 and 10 wavelengths.  The FP64 image
+  against the reference's own flux kernel (1e-11 per pixel, the same lit pixels: every
+  tracer adds a positive flux, so a tracer binned to another pixel would change two
+  pixels by far more than 1e-11), the pixel indices against the oracle's, the fluxes
+  against the oracle, and the mixed image against the FP64 one.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle.cpu as oc
+from diskdyn_gb300 import abi, synth
+from diskdyn_gb300.engine import DeviceState, make_phys, make_view
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(engine, s, n_steps, precision, mode=abi.DDX_MODE_FIXED):
+    st = DeviceState.from_numpy(s.state)
+    engine.set_size_table(**s.size_table)
+    engine.evolve(st, s.n_grav, s.dt, n_steps, make_phys(**s.phys), precision, mode)
+    torch.cuda.synchronize()
+    return st.to_numpy()
+
+
+def rel_err(a, b, sl=slice(None)):
+    pa = np.stack([a[f][sl] for f in ("x", "y", "z")])
+    pb = np.stack([b[f][sl] for f in ("x", "y", "z")])
+    return np.linalg.norm(pa - pb, axis=0) / np.linalg.norm(pb, axis=0)
+
+
+def test_solar_thousand_fp64_steps_match_oracle(engine):
+    """The two inner planets (0.4 and 0.7 AU) get about 5 and 12 steps per orbit at dt = 0.05
+    yr, so the step integrates them far from convergence and rounding differences grow by
+    orders of magnitude there (4e-6 relative for the second planet after 1,000 steps, the
+    star 1e-8 near the origin); the outer planets and the tracers stay close."""
+    s = synth.solar_like(n_dust=16384)
+    g = run_gpu(engine, s, 1000, abi.DDX_PREC_FP64)
+    o = oc.step(s.state, s.n_grav, s.dt, s.size_table, s.phys, 1000)
+    np.testing.assert_array_equal(g["N"], o["N"])
+    ep = rel_err(g, o, slice(0, s.n_grav))
+    ed = rel_err(g, o, slice(s.n_grav, None))
+    print(f"solar 1000 steps: bodies {np.array2string(ep, precision=2)}; tracers median {np.median(ed):.3e} "
+          f"p99 {np.quantile(ed, .99):.3e} max {ed.max():.3e}")
+    assert ep[3:].max() < 1e-8 and ep.max() < 1e-4
+    assert np.median(ed) < 1e-12 and np.quantile(ed, 0.99) < 1e-10 and ed.max() < 1e-6
+
+
+@pytest.fixture(scope="module")
+def ring_full():
+    return synth.dusty_ring(n_dust=4096, n_plsml=4096, seed=77, n_steps=5)
+
+
+def test_ring_full_massive_set_mixed_matches_oracle(engine, ring_full):
+    s = ring_full
+    m = run_gpu(engine, s, 5, abi.DDX_PREC_MIXED)
+    o = oc.step(s.state, s.n_grav, s.dt, s.size_table, s.phys, 5)
+    np.testing.assert_array_equal(m["N"] != 0, o["N"] != 0)
+    live = o["N"][s.n_grav:] != 0
+    ed = rel_err(m, o, slice(s.n_grav, None))[live]
+    em = rel_err(m, o, slice(0, s.n_grav))
+    print(f"ring mixed vs oracle, 5 steps: dust median {np.median(ed):.3e} p99 {np.quantile(ed, .99):.3e} "
+          f"max {ed.max():.3e}; massive max {em.max():.3e}")
+    assert np.median(ed) < 1e-13 and np.quantile(ed, 0.99) < 1e-12 and ed.max() < 1e-10
+    assert em.max() < 1e-11
+
+
+def test_ring_full_massive_set_fp64_matches_reference_kernels(engine, refk, ring_full):
+    s = ring_full
+    g = run_gpu(engine, s, 3, abi.DDX_PREC_FP64, abi.DDX_MODE_REFERENCE)
+    r = refk.step(s.state, s.n_grav, s.dt, s.size_table, s.phys, 3)
+    np.testing.assert_array_equal(g["N"] != 0, r["N"] != 0)
+    assert rel_err(g, r, slice(0, s.n_grav)).max() < 1e-12
+    live = r["N"][s.n_grav:] != 0
+    assert rel_err(g, r, slice(s.n_grav, None))[live].max() < 1e-10
+
+
+@pytest.fixture(scope="module")
+def imaging_full():
+    return synth.imaging(n_dust=4194304, xsize=1024, ysize=1024, n_img=10)
+
+
+def set_optics(engine, s):
+    engine.set_size_table(**s.size_table)
+    o = s.optics
+    engine.set_optics(o["w"], o["in"], o["Qabs"], o["Qsca"], o["Qpfunc"], o["Td"], o["Rmin"], o["Rmax"])
+
+
+def test_imaging_full_size_matches_reference_kernel_and_oracle(engine, refk, imaging_full):
+    s = imaging_full
+    set_optics(engine, s)
+    st = DeviceState.from_numpy(s.state)
+    view = make_view(**s.view)
+    F = engine.image(st, s.n_grav, view, s.image_wj).cpu().numpy()
+    Fm = engine.image(st, s.n_grav, view, s.image_wj, precision=abi.DDX_PREC_MIXED).cpu().numpy()
+    pix, _ = engine.pixels(st, s.n_grav, view)
+    pix = pix.cpu().numpy()
+    Fr = refk.image(s.state, s.n_grav, s.optics, s.size_table["size"], s.view, s.image_wj)
+    assert np.array_equal(F != 0, Fr != 0)
+    np.testing.assert_allclose(F, Fr, rtol=1e-11, atol=0)
+    Fo, pix_o = oc.image(s.state, s.n_grav, s.optics, s.size_table["size"], s.view, s.image_wj)
+    # libm (oracle) and the CUDA math library (reference kernel, ours) may round a tracer
+    # within ~1e-9 pixel of an edge differently: at most a handful of 4M
+    assert int((pix != pix_o).sum()) <= 2
+    lit = Fo != 0
+    if int((pix != pix_o).sum()) == 0:
+        np.testing.assert_allclose(F, Fo, rtol=1e-11, atol=0)
+    else:
+        assert np.quantile(np.abs(F[lit] / Fo[lit] - 1.0), 0.999) < 1e-11
+    assert np.array_equal(F != 0, Fm != 0)
+    assert np.max(np.abs(Fm[F != 0] / F[F != 0] - 1.0)) < 1e-5

@@ -115,8 +115,9 @@ def reference_parser():
         return None
 
 
-@pytest.mark.skipif(not Path("/root/reference/src/read_in.cu").exists(), reason="reference sources absent")
 def test_reference_reads_our_data_file_header_identically(tmp_path):
+    from oracle.ref import paths
+    paths.require(paths.SRC / "read_in.cu")
     exe = reference_parser()
     if exe is None:
         pytest.skip("the reference parser could not be built")

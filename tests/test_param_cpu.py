@@ -15,7 +15,7 @@ import pytest
 from diskdyn_gb300 import formats
 
 GOLD = Path(__file__).resolve().parent / "golden" / "params"
-REF_TESTS = Path("/root/reference/tests")
+from oracle.ref.paths import TESTS as REF_TESTS  # noqa: E402
 
 
 def as_float(v):
@@ -70,6 +70,11 @@ def reference_parser():
         return bp.build()
     except RuntimeError:
         return None
+
+
+def test_reference_test_systems_present():
+    from oracle.ref import paths
+    paths.require(REF_TESTS, "the reference's test systems")
 
 
 @pytest.mark.skipif(not REF_TESTS.exists(), reason="the reference's test systems are not on this machine")

@@ -148,12 +148,16 @@ def test_counter_based_draws_are_per_body(built_lib):
     assert not np.any(np.all(other == full, axis=1))       # (collision blobs keep x, not v)
 
 
-REF_SRC = Path("/root/reference/src/read_in.cu")
+from oracle.ref.paths import SRC as _REF_SRC  # noqa: E402
+
+REF_SRC = _REF_SRC / "read_in.cu"
 
 
-@pytest.mark.skipif(not REF_SRC.exists() or shutil.which("nvcc") is None, reason="reference sources absent")
+@pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc absent")
 @pytest.mark.parametrize("case", CASES)
 def test_reference_reproduces_fixtures(tmp_path, case):
+    from oracle.ref import paths
+    paths.require(REF_SRC)
     spec = importlib.util.spec_from_file_location("msg", Path(__file__).parent / "golden" / "make_setup_golden.py")
     msg = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(msg)

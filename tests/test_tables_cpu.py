@@ -168,12 +168,16 @@ def test_spectrum_reader_skips_comments_and_partial_lines(built_lib, tmp_path):
     np.testing.assert_array_equal(F, [2.0, 4.0])
 
 
-REF_SRC = Path("/root/reference/src/read_in.cu")
+from oracle.ref.paths import SRC as _REF_SRC  # noqa: E402
+
+REF_SRC = _REF_SRC / "read_in.cu"
 
 
-@pytest.mark.skipif(not REF_SRC.exists() or shutil.which("nvcc") is None, reason="reference sources absent")
+@pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc absent")
 @pytest.mark.parametrize("case", CASES)
 def test_reference_reproduces_fixtures(tmp_path, case):
+    from oracle.ref import paths
+    paths.require(REF_SRC)
     spec = importlib.util.spec_from_file_location("mog", Path(__file__).parent / "golden" / "make_optics_golden.py")
     mog = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mog)
