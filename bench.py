@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--n-dust", type=int, default=1048576)
     p.add_argument("--n-plsml", type=int, default=4096)
     p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--comp-steps", type=int, default=5)
     p.add_argument("--err-steps", type=int, default=1000)
     p.add_argument("--err-dust", type=int, default=16384)
     p.add_argument("--cpu-sample", type=int, default=262144)
@@ -285,6 +286,29 @@ def run_ours(args, world, rank, local):
         err_short = {"steps": args.fp64_steps, "dust_rel_pos_err_median": float(np.median(e_short)),
                      "dust_rel_pos_err_max": float(e_short.max())}
 
+    # the compensated step (massive set FP64, float-float planetesimal pulls within half the
+    # tracer's largest coordinate, FP64 within 1.6e-2 of it) on the full workload
+    comp = None
+    if args.comp_steps > 0:
+        COMP = abi.DDX_PREC_COMPENSATED
+        st = st0.clone()
+        one_step(COMP)
+        c_evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.comp_steps)]
+        torch.cuda.synchronize()
+        for k in range(args.comp_steps):
+            flush.zero_()
+            one_step(COMP, c_evs[k])
+        torch.cuda.synchronize()
+        c_ms = [e[0].elapsed_time(e[3]) for e in c_evs]
+        c_value = allsum((ng + alive0) * args.comp_steps) / allmax(sum(c_ms) / 1e3)
+        comp = {"value": c_value, "unit": UNIT, "ms_per_step": statistics.mean(c_ms), "steps": args.comp_steps,
+                "dust_kernel_ms": statistics.mean(e[1].elapsed_time(e[2]) for e in c_evs),
+                "massive_ms": statistics.mean(e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3]) for e in c_evs),
+                "over_fp64": c_value / fp64["value"] if fp64 else None,
+                "what": "DDX_PREC_COMPENSATED: FP64 massive set, float-float planetesimal pulls for spans within "
+                        "0.5 x the tracer's largest coordinate, FP32 beyond, FP64 within 1.6e-2 of it; the RK4 "
+                        "step only (no collisions)"}
+
     # long-horizon error: err_steps steps of a smaller shard, mixed vs FP64
     err_long = None
     if args.err_steps > 0 and rank == 0:
@@ -338,7 +362,8 @@ def run_ours(args, world, rank, local):
         "rk4_only": {"value": value_rk4, "unit": UNIT, "ms_per_step": statistics.mean(rk4_ms),
                      "what": "the same timed steps without the collision call"},
         "fp64": fp64,
-        "mixed_over_fp64": value / fp64["value"] if fp64 else None,
+        "mixed_over_fp64": value_rk4 / fp64["value"] if fp64 else None,
+        "compensated": comp,
         "error_vs_fp64": err_short,
         "error_vs_fp64_long": err_long,
         "collide": collide,
@@ -434,7 +459,8 @@ def long_error_leg(eng, phys, args, n_plsml=None, seed=None, n_steps=None, floor
     small = synth.ring_imaging(synth.dusty_ring(n_dust=args.err_dust, n_plsml=n_plsml, seed=seed))
     ng = small.n_grav
     runs = {}
-    forms = [("fp64", abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED), ("mixed", abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)]
+    forms = [("fp64", abi.DDX_PREC_FP64, abi.DDX_MODE_FIXED), ("mixed", abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED),
+             ("compensated", abi.DDX_PREC_COMPENSATED, abi.DDX_MODE_FIXED)]
     if floor:
         forms.append(("fp64_ref_expr", abi.DDX_PREC_FP64, abi.DDX_MODE_REFERENCE))
     for name, prec, mode in forms:
@@ -481,6 +507,7 @@ def long_error_leg(eng, phys, args, n_plsml=None, seed=None, n_steps=None, floor
     out = {"steps": n_steps, "n_dust": args.err_dust, "n_grav": ng, "n_planets": small.phys["n_planets"],
            "fp64_massive_energy_drift": runs["fp64"][1],
            "mixed_vs_fp64": compare("mixed"),
+           "compensated_vs_fp64": compare("compensated"),
            "profile_error_definition": "max over bins of |profile - FP64 profile| / max FP64 profile; "
                                        "48 annuli to the frame half-width, 36 sectors"}
     if floor:
@@ -564,6 +591,30 @@ def run_accuracy(args, world, rank, local):
         m = evolve(small, MIX, n_steps, eta)
         sweep.append({"eta": eta, "near_radius_at_130AU": eta * 130.0, "ms_per_step": ms,
                       "body_steps_per_s": (ng + full.n_dust) / (ms / 1e3), "error_vs_fp64": errs(m, ref, sng)})
+    comp_sweep = []
+    for ceta, neta in ((0.25, 4e-3), (0.5, 4e-3), (0.5, 1.6e-2), (0.5, 3.2e-2), (1.0, 1.6e-2),
+                       (float("inf"), 1.6e-2)):
+        eng.set_size_table(**full.size_table)
+        eng.set_compensated_radius(ceta)
+        eng.set_near_radius(neta)
+        st = st0.clone()
+        for _ in range(2):
+            eng.step(st, ng, full.dt, phys, abi.DDX_PREC_COMPENSATED)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        torch.cuda.synchronize()
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            eng.step(st, ng, full.dt, phys, abi.DDX_PREC_COMPENSATED)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+        eng.set_compensated_radius(ceta)
+        c = evolve(small, abi.DDX_PREC_COMPENSATED, n_steps, neta)
+        comp_sweep.append({"comp_eta": ceta if math.isfinite(ceta) else "inf", "near_eta": neta, "ms_per_step": ms,
+                           "body_steps_per_s": (ng + full.n_dust) / (ms / 1e3), "error_vs_fp64": errs(c, ref, sng)})
+    eng.set_compensated_radius(0.5)
+    eng.set_near_radius(-1.0)
     worker.join()
     vs_oracle = None
     if "state" in oracle_out:
@@ -574,11 +625,13 @@ def run_accuracy(args, world, rank, local):
         vs_oracle = {"steps": n_steps, "n_dust": 2048, "n_grav": osys.n_grav, "oracle_s": oracle_out["s"],
                      "oracle_cores": os.cpu_count(),
                      "fp64_gpu_vs_oracle": errs(f, ost, osys.n_grav),
-                     "mixed_gpu_vs_oracle": errs(m, ost, osys.n_grav)}
+                     "mixed_gpu_vs_oracle": errs(m, ost, osys.n_grav),
+                     "compensated_gpu_vs_oracle": errs(evolve(osys, abi.DDX_PREC_COMPENSATED, n_steps, -1.0),
+                                                       ost, osys.n_grav)}
     line = {"metric": "near radius vs step time and 1,000-step error (mixed precision)", "workload": "accuracy",
             "n_grav": ng, "n_dust": full.n_dust, "err_dust": args.err_dust, "err_steps": n_steps,
             "error_definition": "|x - x_ref| / |x_ref| per body after err_steps steps from the same state",
-            "sweep": sweep, "vs_oracle": vs_oracle}
+            "sweep": sweep, "compensated_sweep": comp_sweep, "vs_oracle": vs_oracle}
     eng.close()
     print(json.dumps(line), flush=True)
 

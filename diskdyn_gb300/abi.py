@@ -16,6 +16,7 @@ DDX_OK = 0
 DDX_ERR_ARG, DDX_ERR_CUDA, DDX_ERR_NOMEM, DDX_ERR_STATE, DDX_ERR_RANGE, DDX_ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
 DDX_PREC_FP64 = 0
 DDX_PREC_MIXED = 1
+DDX_PREC_COMPENSATED = 2
 DDX_MODE_FIXED = 0
 DDX_MODE_REFERENCE = 1
 DDX_MAX_SIZE_BINS = 2700
@@ -156,6 +157,7 @@ SIGNATURES = [
     ("ddx_noalloc_sync_status", C.c_int, [C.c_int, C.c_void_p]),
     ("ddx_debug_noalloc_lose_tile_copy", C.c_int, [C.c_int, C.c_int, C.c_ulonglong]),
     ("ddx_set_near_radius", C.c_int, [C.c_void_p, C.c_double]),
+    ("ddx_set_compensated_radius", C.c_int, [C.c_void_p, C.c_double]),
     ("ddx_probe_fma_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
 

@@ -31,7 +31,8 @@ struct ddx_ctx {
     int sed_partial_cap = 0;
     unsigned long long* counters = nullptr;   // [0]: tracers that took the exact pixel path
     int* status = nullptr;                      // kStatus* bits set by kernels (device)
-    float near_eta = kDefaultNearEta;           // mixed path: FP64 pulls within near_eta * |coordinate|
+    float near_eta = -1.f;                      // FP64 pulls within near_eta * |coordinate| (< 0: defaults)
+    float comp_eta = kDefaultCompEta;           // compensated path: float-float spans within comp_eta * |coordinate|
     int inject_lose_tile = -1;                  // one-shot test hook for the next mixed dust launch
     unsigned long long inject_wait_ns = 0;
     CollideScratch* collide = nullptr;          // spatial-hash buffers, grown on demand
@@ -66,7 +67,8 @@ cudaError_t dalloc(T** p, size_t n) {
 }
 
 void free_massive(MassiveScratch& ms) {
-    cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.PP); cudaFree(ms.A); cudaFree(ms.R);
+    cudaFree(ms.P); cudaFree(ms.Phi); cudaFree(ms.Plo); cudaFree(ms.PP); cudaFree(ms.PM); cudaFree(ms.A);
+    cudaFree(ms.R);
     cudaFree(ms.part); cudaFree(ms.slot); cudaFree(ms.src);
     order_free(ms.src_order);
     order_free(ms.dust_order);
@@ -82,7 +84,7 @@ int ensure_massive(ddx_ctx* c, int n_grav, int n_dust, int precision) {
         const int r = alloc_massive(c, n_grav);
         if (r) return r;
     }
-    if (precision == DDX_PREC_MIXED && c->ms.dust_order.cap < n_dust) {
+    if (precision != DDX_PREC_FP64 && c->ms.dust_order.cap < n_dust) {
         if (order_alloc(c->ms.dust_order, n_dust, false) != cudaSuccess) {
             cudaGetLastError();
             return DDX_ERR_NOMEM;
@@ -102,6 +104,7 @@ int alloc_massive(ddx_ctx* c, int n_grav) {
     ms.part_words = massive_part_words(cap);
     if (dalloc(&ms.P, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.Phi, (size_t)4 * cap) != cudaSuccess ||
         dalloc(&ms.Plo, (size_t)4 * cap) != cudaSuccess || dalloc(&ms.PP, (size_t)4 * ms.pcap) != cudaSuccess ||
+        dalloc(&ms.PM, (size_t)4 * ms.pcap) != cudaSuccess ||
         dalloc(&ms.A, (size_t)12 * cap) != cudaSuccess || dalloc(&ms.R, (size_t)9 * cap) != cudaSuccess ||
         dalloc(&ms.part, (size_t)ms.part_words) != cudaSuccess || dalloc(&ms.slot, (size_t)cap) != cudaSuccess ||
         dalloc(&ms.src, (size_t)cap) != cudaSuccess ||
@@ -119,9 +122,11 @@ bool state_ok(const ddx_state* s) {
     return s && s->x && s->y && s->z && s->vx && s->vy && s->vz && s->m && s->N && s->id;
 }
 
-int make_step_args(const ddx_ctx* c, const ddx_phys* p, int n_grav, int n_dust, double dt, int mode, StepArgs& a) {
+int make_step_args(const ddx_ctx* c, const ddx_phys* p, int n_grav, int n_dust, double dt, int mode, StepArgs& a,
+                   int precision = DDX_PREC_MIXED) {
     if (!p || n_grav < 1 || n_dust < 0) return DDX_ERR_ARG;
-    a.near_eta = c->near_eta;
+    a.near_eta = c->near_eta >= 0.f ? c->near_eta : default_near_eta(precision);
+    a.comp_eta = c->comp_eta;
     a.n_grid = c->n_grid;
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
     if (p->n_planets < 0 || p->n_planets > n_grav) return DDX_ERR_ARG;
@@ -378,12 +383,12 @@ int ddx_step(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
 int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, const ddx_state* s, int n_grav,
                   int n_dust, double dt, const ddx_phys* phys, int precision, int mode, void* stream) {
     if (!c || !state_ok(s) || n_grav < 1 || n_dust < 0) return DDX_ERR_ARG;
-    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (!step_precision_ok(precision)) return DDX_ERR_ARG;
     const long long n_all = (long long)n_grav + n_dust;
     if (!host_state_ok(in, n_all) || !host_state_ok(out, n_all)) return DDX_ERR_ARG;
     if (!c->bins) return DDX_ERR_STATE;
     StepArgs a;
-    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a, precision);
     if (r) return r;
     DeviceGuard dg(c->device);
     if ((r = ensure_massive(c, n_grav, n_dust, precision)) || (r = ensure_pipeline(c))) return r;
@@ -401,7 +406,7 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
     // the span boxes.  Measured on the dusty ring, three chunks cost more (10.2 ms a step)
     // than the copies they hide: one chunk has its copy in overlapped with the massive set's
     // work and only the copy out exposed (0.3 ms).
-    const bool ordered = precision == DDX_PREC_MIXED && spatial_order_on(a);
+    const bool ordered = precision != DDX_PREC_FP64 && spatial_order_on(a);
     const std::vector<int> chunks =
         a.mode == DDX_MODE_REFERENCE || ordered ? std::vector<int>{n_dust} : dust_chunks(n_dust);
     int o = 0;
@@ -427,10 +432,10 @@ int ddx_step_host(ddx_ctx* c, const ddx_host_state* in, ddx_host_state* out, con
 int ddx_evolve(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt, int n_steps,
                const ddx_phys* phys, int precision, int mode, void* stream) {
     if (!c || !state_ok(s) || n_steps < 0) return DDX_ERR_ARG;
-    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (!step_precision_ok(precision)) return DDX_ERR_ARG;
     if (!c->bins) return DDX_ERR_STATE;
     StepArgs a;
-    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a, precision);
     if (r) return r;
     DeviceGuard dg(c->device);
     if ((r = ensure_massive(c, n_grav, n_dust, precision))) return r;
@@ -444,9 +449,9 @@ namespace {
 int prepare_call(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, double dt,
                  const ddx_phys* phys, int precision, int mode, StepArgs& a) {
     if (!c || !state_ok(s)) return DDX_ERR_ARG;
-    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (!step_precision_ok(precision)) return DDX_ERR_ARG;
     if (!c->bins) return DDX_ERR_STATE;
-    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a);
+    int r = make_step_args(c, phys, n_grav, n_dust, dt, mode, a, precision);
     if (r) return r;
     return ensure_massive(c, n_grav, n_dust, precision);   // the caller made c's device current
 }
@@ -592,8 +597,14 @@ int ddx_adjoint_backward(ddx_ctx* c, const double* dL_dimage, double* grad_state
 }
 
 int ddx_set_near_radius(ddx_ctx* c, double eta) {
-    if (!c || !(eta >= 0.0) || eta > (double)kMaxNearEta) return DDX_ERR_ARG;
-    c->near_eta = (float)eta;
+    if (!c || eta != eta || eta > (double)kMaxNearEta) return DDX_ERR_ARG;
+    c->near_eta = eta < 0.0 ? -1.f : (float)eta;   // negative: the defaults of each precision
+    return DDX_OK;
+}
+
+int ddx_set_compensated_radius(ddx_ctx* c, double eta) {
+    if (!c || !(eta >= 0.0)) return DDX_ERR_ARG;   // +inf: every span
+    c->comp_eta = (float)eta;
     return DDX_OK;
 }
 

@@ -45,6 +45,20 @@
 // record); a span whose largest exceeds 1 / (near_eta own) is summed again without its
 // near sources, which are added in FP64.  Far spans never hold a near source (near_eta is
 // at most a quarter, far spans start at a half).
+//
+// Compensated variant (DDX_PREC_COMPENSATED).  The near radius does not bound the largest
+// errors: in this chaotic system a grain amplifies the FP32 rounding of every planetesimal
+// pull within tens of AU by three to four orders of magnitude over 1,000 steps.  So spans
+// nearer to the tracer than comp_eta times its largest |coordinate| are evaluated in
+// float-float arithmetic: each quantity is an unevaluated sum hi + lo of two FP32 numbers,
+// carried through error-free transformations (TwoSum; products split by FMA) and one
+// Newton step of the reciprocal square root on the float-float square distance, with the
+// masses in two parts as well.  That keeps about 44 bits of each pull, against 22 or so in
+// FP32, for about ten times the FP32 operations of a pair; farther spans take the FP32
+// forms.  The hi + lo positions themselves hold 48 bits, so sources within the near radius
+// still take the exact FP64 pull inside those spans.  The per-span choice is made like the
+// far-span choice (block box first, then per tracer), so a tracer's result again depends
+// only on its own state and the massive set.
 #include "ddx_internal.cuh"
 #include "ddx_f32x2.cuh"
 
@@ -86,6 +100,102 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, unsigned parity, unsigned
     while (!mbar_try(mb, parity))
         if (global_ns() - t0 > limit_ns) return false;
     return true;
+}
+
+// ---- float-float pulls (compensated variant) -------------------------------------------
+__device__ __forceinline__ f2 neg2(f2 a) { return a ^ 0x8000000080000000ull; }
+// s + e == a + b exactly (Knuth's TwoSum, no ordering needed)
+__device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
+    s = add2(a, b);
+    const f2 v = sub2(s, a);
+    e = add2(sub2(a, sub2(s, v)), sub2(b, v));
+}
+// One coordinate of source - tracer as an unnormalised pair h + l: h = fp32(a - A), l = the
+// rounding error of that difference (TwoSum) plus the difference of the low parts.
+__device__ __forceinline__ void sep_ff(f2 a, f2 la, f2 A, f2 LA, f2& h, f2& l) {
+    h = sub2(a, A);
+    const f2 v = sub2(h, a);
+    l = add2(sub2(la, LA), sub2(sub2(a, sub2(h, v)), add2(A, v)));
+}
+// (h + l)^2 = p + e: p = fp32(h^2), e = (h^2 - p) + 2 h l + l^2
+__device__ __forceinline__ void sq_ff(f2 h, f2 l, f2& p, f2& e) {
+    p = mul2(h, h);
+    e = fma2(h, h, neg2(p));
+    e = fma2(add2(h, h), l, e);
+    e = fma2(l, l, e);
+}
+// (S, L) += (fh + fl)(dh + dl): the product's rounding error and cross terms into L, the
+// sum's rounding error (TwoSum) into L.
+__device__ __forceinline__ void acc_ff(f2 fh, f2 fl, f2 dh, f2 dl, f2& S, f2& L) {
+    const f2 ph = mul2(fh, dh);
+    f2 pl = fma2(fh, dh, neg2(ph));
+    pl = fma2(fh, dl, pl);
+    pl = fma2(fl, dh, pl);
+    f2 t, e;
+    two_sum2(S, ph, t, e);
+    S = t;
+    L = add2(L, add2(e, pl));
+}
+// Pulls of the two sources of pair record r on one tracer (hi/lo parts XH..ZL) in
+// float-float, added to the span sums (SH, SL) per axis.  ml: the low parts of the two
+// masses.  y0, y1: the two FP32 reciprocal distances (rsqrt.approx of the high part of the
+// square distance), which decide the near sources.  SKIP: a source whose reciprocal distance
+// exceeds inv_near adds nothing (the caller takes its pull in FP64).  A coincident source
+// (zero distance) makes the sums non-finite, which removes the tracer as in the other
+// variants.
+template <bool SKIP>
+__device__ __forceinline__ void pair_ff(const BodyPair* r, f2 ml, f2 XH, f2 XL, f2 YH, f2 YL, f2 ZH, f2 ZL,
+                                        f2 SH[3], f2 SL[3], float inv_near, float& y0, float& y1) {
+    const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);  // hx, hy
+    const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);  // hz, m
+    const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r->lx);  // lx, ly
+    const f2 lz = *reinterpret_cast<const f2*>(r->lz);
+    f2 dxh, dxl, dyh, dyl, dzh, dzl;
+    sep_ff(q0.x, q2.x, XH, XL, dxh, dxl);
+    sep_ff(q0.y, q2.y, YH, YL, dyh, dyl);
+    sep_ff(q1.x, lz, ZH, ZL, dzh, dzl);
+    f2 px, ex, py, ey, pz, ez;
+    sq_ff(dxh, dxl, px, ex);
+    sq_ff(dyh, dyl, py, ey);
+    sq_ff(dzh, dzl, pz, ez);
+    f2 a1, t1, a2, t2;
+    two_sum2(px, py, a1, t1);
+    two_sum2(a1, pz, a2, t2);
+    const f2 lo = add2(add2(add2(ex, ey), add2(ez, t1)), t2);
+    const f2 RRh = add2(a2, lo);                       // |a2| >> |lo|: Fast2Sum
+    const f2 RRl = sub2(lo, sub2(RRh, a2));
+    // 1/sqrt(RR) = y + yl: y from rsqrt.approx, yl = y (1 - RR y^2) / 2 (one Newton step),
+    // with y^2 = u + eu and RRh u = v + ev exact
+    float r0, r1;
+    f2_split(RRh, r0, r1);
+    y0 = rsqrt_approx(r0);
+    y1 = rsqrt_approx(r1);
+    const f2 y = f2_join(y0, y1);
+    const f2 u = mul2(y, y), eu = fma2(y, y, neg2(u));
+    const f2 v = mul2(RRh, u), ev = fma2(RRh, u, neg2(v));
+    constexpr f2 kOne2 = 0x3F8000003F800000ull, kHalf2 = 0x3F0000003F000000ull;
+    f2 rr = sub2(sub2(kOne2, v), ev);
+    rr = fma2(neg2(RRh), eu, rr);
+    rr = fma2(neg2(RRl), u, rr);
+    const f2 yl = mul2(mul2(y, kHalf2), rr);
+    // ri^3 = h3 + l3 from ri^2 = u + (eu + 2 y yl); then f = m ri^3 = fh + fl
+    const f2 c2l = fma2(add2(y, y), yl, eu);
+    const f2 h3 = mul2(u, y);
+    f2 l3 = fma2(u, y, neg2(h3));
+    l3 = fma2(u, yl, l3);
+    l3 = fma2(c2l, y, l3);
+    f2 fh = mul2(q1.y, h3);
+    f2 fl = fma2(q1.y, h3, neg2(fh));
+    fl = fma2(q1.y, l3, fl);
+    fl = fma2(ml, h3, fl);
+    if (SKIP) {   // zero pull (exactly) for the near sources
+        const unsigned long long keep = (y0 > inv_near ? 0ull : 0xFFFFFFFFull) | (y1 > inv_near ? 0ull : 0xFFFFFFFF00000000ull);
+        fh &= keep;
+        fl &= keep;
+    }
+    acc_ff(fh, fl, dxh, dxl, SH[0], SL[0]);
+    acc_ff(fh, fl, dyh, dyl, SH[1], SL[1]);
+    acc_ff(fh, fl, dzh, dzl, SH[2], SL[2]);
 }
 
 // Box of every span's sources (high parts, padding slots left out) at every stage, written
@@ -156,18 +266,27 @@ __device__ __forceinline__ bool lane_far(float2 bx, float2 by, float2 bz, float 
 // b is nearer than kFar xm.  Each rounded step is monotone, so these imply lane_far's
 // outcome for any tracer inside b.
 __device__ __forceinline__ void block_far(float2 bx, float2 by, float2 bz, float xm, const float* b, bool& all_far,
-                                          bool& all_near) {
+                                          bool& all_near, float& dn, float& df) {
     const float nx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, b[1]), __fsub_rn(b[0], bx.y)));
     const float ny = fmaxf(0.f, fmaxf(__fsub_rn(by.x, b[3]), __fsub_rn(b[2], by.y)));
     const float nz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, b[5]), __fsub_rn(b[4], bz.y)));
     const float fx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, b[0]), __fsub_rn(b[1], bx.y)));
     const float fy = fmaxf(0.f, fmaxf(__fsub_rn(by.x, b[2]), __fsub_rn(b[3], by.y)));
     const float fz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, b[4]), __fsub_rn(b[5], bz.y)));
-    const float dn = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
-    const float df = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+    dn = __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
+    df = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
     const float X = kFar * fmaxf(xm, b[6]), Xn = kFar * xm;
     all_far = xm == xm && dn >= __fmul_rn(X, X);
     all_near = !(xm == xm) || df < __fmul_rn(Xn, Xn);
+}
+
+// Squared distance from a tracer's point to a span box (rounded operations only, like
+// lane_far, so the block tests imply its outcome).
+__device__ __forceinline__ float lane_dist2(float2 bx, float2 by, float2 bz, float xh, float yh, float zh) {
+    const float gx = fmaxf(0.f, fmaxf(__fsub_rn(bx.x, xh), __fsub_rn(xh, bx.y)));
+    const float gy = fmaxf(0.f, fmaxf(__fsub_rn(by.x, yh), __fsub_rn(yh, by.y)));
+    const float gz = fmaxf(0.f, fmaxf(__fsub_rn(bz.x, zh), __fsub_rn(zh, bz.y)));
+    return __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
 }
 
 __device__ __forceinline__ void span_box(const BodyPair* R, float2& bx, float2& by, float2& bz, float& xm) {
@@ -234,6 +353,33 @@ __device__ __forceinline__ void near_span(const BodyPair* R, int q0, f2 XH, f2 X
     }
 }
 
+// One float-float span summed again for a tracer with a near source among its pair records:
+// the float-float sums of the other sources into (SH, SL), and the FP64 pull of each near
+// source (reciprocal FP32 distance above inv_near) from its FP64 stage record, added to k
+// (as near_span does for the FP32 forms).
+__device__ __forceinline__ void near_span_ff(const BodyPair* R, const f2* ML, int q0, f2 XH, f2 XL, f2 YH, f2 YL,
+                                             f2 ZH, f2 ZL, float xr, float yr, float zr, float inv_near,
+                                             const Body* __restrict__ P, const int* __restrict__ src, f2 SH[3],
+                                             f2 SL[3], double& kx, double& ky, double& kz) {
+    const double xt = join3(XH, XL, xr), yt = join3(YH, YL, yr), zt = join3(ZH, ZL, zr);
+    for (int c = 0; c < 3; ++c) SH[c] = SL[c] = 0;
+    for (int u = 0; u < kPairSpan; ++u) {
+        float y0, y1;
+        pair_ff<true>(R + u, __ldg(ML + u), XH, XL, YH, YL, ZH, ZL, SH, SL, inv_near, y0, y1);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!((h ? y1 : y0) > inv_near)) continue;
+            const int q = q0 + 2 * u + h;
+            const Body p = P[src ? src[q] : q];
+            const double ex = p.x - xt, ey = p.y - yt, ez = p.z - zt;
+            const double rr = ex * ex + ey * ey + ez * ez;
+            const double ri64 = rsqrt(rr);
+            const double f64 = p.m * (ri64 * ri64 * ri64);
+            kx = fma(f64, ex, kx); ky = fma(f64, ey, ky); kz = fma(f64, ez, kz);
+        }
+    }
+}
+
 // Spans with one bit per block test (all far, all near) in shared memory, per stage; beyond
 // this many spans every tracer tests every span itself.
 constexpr int kFlagSpans = 4096;
@@ -253,14 +399,19 @@ __device__ __forceinline__ uint32_t span_bits(const uint32_t* w, int j0, int n) 
 // Measured on the dusty ring (dust kernel): 3 blocks (80 registers, 32 KiB tiles) 8.50 ms,
 // 4 blocks 8.34 ms, 5 blocks (48 registers, 20 KiB tiles) 8.41 ms; two blocks without
 // spills were slower than three.
-__global__ void __launch_bounds__(kThreads, 4)
+// COMP: the compensated variant, two blocks per SM (its float-float pair needs more
+// registers than 64).
+template <bool COMP>
+__global__ void __launch_bounds__(kThreads, COMP ? 2 : 4)
 dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins,
                       const int* __restrict__ perm, bool boxes, const int* __restrict__ src) {
+    constexpr int NB = COMP ? 8 : 7;              // box values: 3 x (min, max), largest own[, smallest own]
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar[2];
-    __shared__ float bred[kThreads / 32][7];
-    __shared__ float bbox[7];                     // the block's box at the current stage, largest own
+    __shared__ float bred[kThreads / 32][NB];
+    __shared__ float bbox[NB];                    // the block's box at the current stage, largest own
     __shared__ uint32_t allfar[kFlagSpans / 32], allnear[kFlagSpans / 32];
+    __shared__ uint32_t allcomp[COMP ? kFlagSpans / 32 : 1], nocomp[COMP ? kFlagSpans / 32 : 1];
     BodyPair* const tiles = reinterpret_cast<BodyPair*>(smem);
     const int tid = threadIdx.x;
     const int slot = blockIdx.x * blockDim.x + tid;   // position in the visiting order
@@ -359,16 +510,17 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
         const f2 ZH = f2_dup(zh), ZL = f2_dup(zl);
         const float own = fmaxf(fabsf(xh), fmaxf(fabsf(yh), fabsf(zh)));   // largest |coordinate|
         const float inv_near = near_inv(a.near_eta, own);
+        const float Dc = a.comp_eta * own;                                 // compensated spans: nearer than this
         const Body* const Pn = ms.P + (size_t)st * ms.cap + a.n_exact;     // FP64 records of the sources
         // per stage: the block's box (live tracers) and, per span, whether the box settles
         // every tracer's choice (bits in shared memory); spans left open are tested per tracer
         const int nspans = npairs / kPairSpan;
         const bool flags = boxes && nspans <= kFlagSpans;
         if (flags) {
-            const float v[7] = {xh, xh, yh, yh, zh, zh, own};
+            const float v[8] = {xh, xh, yh, yh, zh, zh, own, own};
 #pragma unroll
-            for (int q = 0; q < 7; ++q) {
-                const bool mx = (q & 1) || q == 6;
+            for (int q = 0; q < NB; ++q) {
+                const bool mx = q < 7 && ((q & 1) || q == 6);
                 float w = alive ? v[q] : (mx ? -INFINITY : INFINITY);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
@@ -378,28 +530,39 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
                 if ((tid & 31) == 0) bred[tid >> 5][q] = w;
             }
             __syncthreads();
-            if (tid < 7) {
-                const bool mx = (tid & 1) || tid == 6;
+            if (tid < NB) {
+                const bool mx = tid < 7 && ((tid & 1) || tid == 6);
                 float w = bred[0][tid];
                 for (int k = 1; k < (int)(blockDim.x >> 5); ++k) w = mx ? fmaxf(w, bred[k][tid]) : fminf(w, bred[k][tid]);
-                bbox[tid] = tid == 6 ? fmaxf(w, 0.f) : w;
+                bbox[tid] = tid >= 6 ? fmaxf(w, 0.f) : w;
             }
             __syncthreads();
-            float b[7];
+            float b[NB];
 #pragma unroll
-            for (int q = 0; q < 7; ++q) b[q] = bbox[q];
+            for (int q = 0; q < NB; ++q) b[q] = bbox[q];
             const BodyPair* PPs = ms.PP + (size_t)st * ms.pcap;
             for (int j0 = 0; j0 < nspans; j0 += blockDim.x) {   // uniform trip count: ballots below
                 const int j = j0 + tid;
-                bool f = false, nr = false;
+                bool f = false, nr = false, ca = false, cn = false;
                 if (j < nspans) {
                     float2 bx, by, bz;
-                    float xm;
+                    float xm, dn, df;
                     span_box(PPs + (size_t)j * kPairSpan, bx, by, bz, xm);
-                    block_far(bx, by, bz, xm, b, f, nr);
+                    block_far(bx, by, bz, xm, b, f, nr, dn, df);
+                    if constexpr (COMP) {
+                        // every tracer within comp_eta own of the box / none (b[6], b[7]: the
+                        // largest and smallest own); monotone like the far tests
+                        const float lo = a.comp_eta * b[7], hi = a.comp_eta * b[6];
+                        ca = df < __fmul_rn(lo, lo);
+                        cn = !(dn < __fmul_rn(hi, hi));
+                    }
                 }
                 const uint32_t wf = __ballot_sync(0xffffffffu, f), wn = __ballot_sync(0xffffffffu, nr);
                 if ((tid & 31) == 0 && j < nspans) { allfar[j >> 5] = wf; allnear[j >> 5] = wn; }   // lane 0: j = 32 w
+                if constexpr (COMP) {
+                    const uint32_t wa = __ballot_sync(0xffffffffu, ca), wc = __ballot_sync(0xffffffffu, cn);
+                    if ((tid & 31) == 0 && j < nspans) { allcomp[j >> 5] = wa; nocomp[j >> 5] = wc; }
+                }
             }
             __syncthreads();
         }
@@ -414,15 +577,36 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
             const BodyPair* T = tiles + (g & 1) * kTilePairs;
             const int cnt = min(kTilePairs, npairs - tt * kTilePairs);   // a multiple of kPairSpan
             static_assert(kTilePairs / kPairSpan <= 32, "one mask bit per span of a tile");
-            uint32_t fm = 0u;
+            uint32_t fm = 0u, cm = 0u;   // far spans, compensated spans (compensated wins)
+            const uint32_t all = cnt / kPairSpan == 32 ? 0xFFFFFFFFu : (1u << (cnt / kPairSpan)) - 1u;
+            if (COMP) {
+                if (!boxes) {
+                    cm = all;              // no spatial order: every span compensated
+                } else {
+                    uint32_t open = all;
+                    if (flags) {
+                        const int j0 = tt * (kTilePairs / kPairSpan);
+                        const uint32_t ac = span_bits(allcomp, j0, cnt / kPairSpan);
+                        cm = ac;
+                        open = all & ~(ac | span_bits(nocomp, j0, cnt / kPairSpan));
+                    }
+                    while (open) {
+                        const int j = __ffs(open) - 1;
+                        open &= open - 1;
+                        float2 bx, by, bz;
+                        float xm;
+                        span_box(T + j * kPairSpan, bx, by, bz, xm);
+                        if (lane_dist2(bx, by, bz, xh, yh, zh) < __fmul_rn(Dc, Dc)) cm |= 1u << j;
+                    }
+                }
+            }
             if (boxes) {
-                const uint32_t all = cnt / kPairSpan == 32 ? 0xFFFFFFFFu : (1u << (cnt / kPairSpan)) - 1u;
-                uint32_t open = all;
+                uint32_t open = all & ~cm;
                 if (flags) {
                     const int j0 = tt * (kTilePairs / kPairSpan);   // the tile's first span
                     const uint32_t af = span_bits(allfar, j0, cnt / kPairSpan);
-                    fm = af;
-                    open = all & ~(af | span_bits(allnear, j0, cnt / kPairSpan));
+                    fm = af & ~cm;
+                    open = all & ~cm & ~(af | span_bits(allnear, j0, cnt / kPairSpan));
                 }
                 while (open) {   // the same mask in every lane: no divergence here
                     const int j = __ffs(open) - 1;
@@ -435,6 +619,25 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
             }
             for (int k = 0; k < cnt; k += kPairSpan) {
                 f2 px = 0, py = 0, pz = 0;
+                if (COMP && ((cm >> (k / kPairSpan)) & 1u)) {
+                    // float-float span sums, folded into the compensated running sums: the
+                    // high parts through kahan2, the low parts straight into its compensation
+                    f2 SH[3] = {0, 0, 0}, SL[3] = {0, 0, 0};
+                    const f2* ML = reinterpret_cast<const f2*>(ms.PM + (size_t)st * ms.pcap + tt * kTilePairs + k);
+                    float mx = 0.f;
+#pragma unroll 2
+                    for (int u = 0; u < kPairSpan; ++u) {
+                        float y0, y1;
+                        pair_ff<false>(T + k + u, __ldg(ML + u), XH, XL, YH, YL, ZH, ZL, SH, SL, inv_near, y0, y1);
+                        mx = fmax3(mx, y0, y1);
+                    }
+                    if (mx > inv_near)   // a source within the near radius: its pull in FP64
+                        near_span_ff(T + k, ML, 2 * (tt * kTilePairs + k), XH, XL, YH, YL, ZH, ZL, xr, yr, zr,
+                                     inv_near, Pn, src, SH, SL, kx, ky, kz);
+                    kahan2(Sx, Cx, SH[0]); kahan2(Sy, Cy, SH[1]); kahan2(Sz, Cz, SH[2]);
+                    Cx = sub2(Cx, SL[0]); Cy = sub2(Cy, SL[1]); Cz = sub2(Cz, SL[2]);
+                    continue;
+                }
                 if ((fm >> (k / kPairSpan)) & 1u) {
 #pragma unroll
                     for (int u = 0; u < kPairSpan; ++u) {
@@ -516,16 +719,20 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
 }  // namespace
 
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
-                              const SizeBin* bins, cudaStream_t st) {
+                              const SizeBin* bins, int precision, cudaStream_t st) {
     if (a.n_dust <= 0) return cudaSuccess;
+    const bool comp = precision == DDX_PREC_COMPENSATED;
     const size_t smem = 2 * (size_t)kTilePairs * sizeof(BodyPair);
-    static bool attr_set[128] = {};   // the attribute is set once per device
+    static bool attr_set[128] = {};   // the attributes are set once per device
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
     if (!attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(dust_rk4_mixed_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(dust_rk4_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dust_rk4_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
@@ -546,7 +753,8 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
     // the source of each pair slot, for the FP64 pulls of near sources: the sources sit in
     // cell order when the step ordered them (massive_prepare), else slot q holds source q
     const int* src = ms.slot && spatial_order_on(a) ? ms.src : nullptr;
-    dust_rk4_mixed_kernel<<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes, src);
+    if (comp) dust_rk4_mixed_kernel<true><<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes, src);
+    else dust_rk4_mixed_kernel<false><<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes, src);
     return cudaGetLastError();
 }
 

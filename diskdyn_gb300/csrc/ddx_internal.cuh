@@ -39,10 +39,23 @@ struct StepArgs {
     unsigned long long wait_ns;   // bound on any one device-side wait
     float  near_eta;        // mixed path: an FP32 source nearer to a body than near_eta times the
                             // body's largest |coordinate| takes the FP64 pair force instead (0: none)
+    float  comp_eta;        // compensated path: spans nearer to a tracer than comp_eta times its
+                            // largest |coordinate| take the float-float pull
 };
 
-// Default near radius of the mixed path, relative to the body's largest |coordinate|.
+// Default near radius of the mixed path, relative to the body's largest |coordinate|, and
+// of the compensated path, whose float-float pulls leave the 48-bit positions' rounding
+// (about 2^-48 of a coordinate) as the largest error of a close pull: exact FP64 pulls out
+// to 1.6e-2 of the coordinate bring the worst 1,000-step grain of the dusty ring from 8.6e-10
+// to 5.0e-10 of its FP64 position for 5 % more time.
 constexpr float kDefaultNearEta = 4.0e-3f;
+constexpr float kDefaultCompNearEta = 1.6e-2f;
+__host__ __device__ inline float default_near_eta(int precision) {
+    return precision == DDX_PREC_COMPENSATED ? kDefaultCompNearEta : kDefaultNearEta;
+}
+// Default radius of the float-float spans of DDX_PREC_COMPENSATED, relative to the tracer's
+// largest |coordinate|.
+constexpr float kDefaultCompEta = 0.5f;
 // Largest accepted near radius: far spans (dust kernel) start at half the largest coordinate,
 // so a near source can never sit in a far span.
 constexpr float kMaxNearEta = 0.25f;
@@ -130,6 +143,7 @@ struct MassiveScratch {
     float4   *Phi;    // [4][cap] fp32 hi part, m in .w
     float4   *Plo;    // [4][cap] fp32 lo part
     BodyPair *PP;     // [4][pcap] pair records of sources 1..n_grav-1
+    float2   *PM;     // [4][pcap] low parts of the two masses of each pair record (m - fp32(m))
     double   *A;      // [4][3][cap] stage accelerations A1..A4
     double   *R;      // [3][3][cap] stage velocities R2..R4
     int      *status; // device status word: DDX_STATUS_* bits set by kernels
@@ -174,6 +188,11 @@ constexpr int kSliceThreads = 256;
 constexpr int kSliceBlocksPerSM = 4;
 constexpr long long massive_part_words_for(int cap, int sms) {
     return 6LL * kSliceThreads * ((long long)kSliceBlocksPerSM * sms + (cap + kSliceThreads - 1) / kSliceThreads);
+}
+
+// Precisions the step entry points take.
+inline bool step_precision_ok(int p) {
+    return p == DDX_PREC_FP64 || p == DDX_PREC_MIXED || p == DDX_PREC_COMPENSATED;
 }
 
 // Bits of the device status word.
@@ -247,7 +266,7 @@ cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScra
 int massive_slices(int n_grav, int n_exact);
 long long massive_part_words(int cap);
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
-                              const SizeBin* bins, cudaStream_t st);
+                              const SizeBin* bins, int precision, cudaStream_t st);
 
 struct CollideScratch;   // ddx_collide.cu
 int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double h, int2* pairs,

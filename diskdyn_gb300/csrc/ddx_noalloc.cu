@@ -27,7 +27,8 @@ constexpr size_t kOffPhi = kOffP + align256(sizeof(Body) * 4 * kCap);
 constexpr size_t kOffPlo = kOffPhi + align256(sizeof(float4) * 4 * kCap);
 constexpr int kPcap = pair_count(kCap) + kPairSpan;
 constexpr size_t kOffPP = kOffPlo + align256(sizeof(float4) * 4 * kCap);
-constexpr size_t kOffA = kOffPP + align256(sizeof(BodyPair) * 4 * kPcap);
+constexpr size_t kOffPM = kOffPP + align256(sizeof(BodyPair) * 4 * kPcap);
+constexpr size_t kOffA = kOffPM + align256(sizeof(float2) * 4 * kPcap);
 constexpr size_t kOffR = kOffA + align256(sizeof(double) * 12 * kCap);
 constexpr size_t kOffBins = kOffR + align256(sizeof(double) * 9 * kCap);
 constexpr size_t kOffStatus = kOffBins + align256(sizeof(SizeBin) * DDX_MAX_SIZE_BINS);
@@ -101,7 +102,7 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     if (!s || !s->x || !s->y || !s->z || !s->vx || !s->vy || !s->vz || !s->m || !s->N || !s->id || !p)
         return DDX_ERR_ARG;
     if (n_grav < 1 || n_dust < 0 || n_grid < 1 || !beta || !betasw || !q) return DDX_ERR_ARG;
-    if (precision != DDX_PREC_FP64 && precision != DDX_PREC_MIXED) return DDX_ERR_ARG;
+    if (!step_precision_ok(precision)) return DDX_ERR_ARG;
     if (mode != DDX_MODE_FIXED && mode != DDX_MODE_REFERENCE) return DDX_ERR_ARG;
     if (p->n_planets < 0 || p->n_planets > n_grav) return DDX_ERR_ARG;
     if (n_grav > DDX_NOALLOC_MAX_GRAV || n_grid > DDX_MAX_SIZE_BINS) return DDX_ERR_RANGE;
@@ -119,6 +120,7 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     ms.A = reinterpret_cast<double*>(base + kOffA);
     ms.R = reinterpret_cast<double*>(base + kOffR);
     ms.PP = reinterpret_cast<BodyPair*>(base + kOffPP);
+    ms.PM = reinterpret_cast<float2*>(base + kOffPM);
     ms.status = reinterpret_cast<int*>(base + kOffStatus);
     ms.cap = kCap;
     ms.pcap = kPcap;
@@ -143,7 +145,7 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
     a.mode = mode;
     a.lose_tile = -1;
     a.wait_ns = kDefaultWaitNs;
-    if (precision == DDX_PREC_MIXED) {
+    if (precision != DDX_PREC_FP64) {
         std::lock_guard<std::mutex> lk(g_mu);
         hooks_init();
         if (g_lose_tile[device] >= 0) {
@@ -152,7 +154,8 @@ extern "C" int ddx_step_noalloc(int device, const ddx_state* s, int n_grav, int 
             g_lose_tile[device] = -1;
         }
     }
-    a.near_eta = kDefaultNearEta;
+    a.near_eta = default_near_eta(precision);
+    a.comp_eta = kDefaultCompEta;
     a.n_grid = n_grid;
 
     // Every scratch word a step reads is written earlier in the same step (the packed bins,

@@ -36,6 +36,8 @@ __device__ __forceinline__ void store_pair_slot(MassiveScratch& ms, int stage, i
     const int u = q & 1;
     r->hx[u] = h.x; r->hy[u] = h.y; r->hz[u] = h.z; r->m[u] = h.w;
     r->lx[u] = l.x; r->ly[u] = l.y; r->lz[u] = l.z; r->pad[u] = 0.f;
+    float2& pm = ms.PM[(size_t)stage * ms.pcap + (q >> 1)];
+    if (u) pm.y = l.w; else pm.x = l.w;           // the mass's low part
 }
 
 // Zero-mass, far-away filler for the slots past the last FP32 source, so the dust kernel
@@ -48,6 +50,8 @@ __device__ __forceinline__ void store_pair_padding(MassiveScratch& ms, int n_src
             const int k = q & 1;
             r->hx[k] = kFarAway; r->hy[k] = kFarAway; r->hz[k] = kFarAway; r->m[k] = 0.f;
             r->lx[k] = 0.f; r->ly[k] = 0.f; r->lz[k] = 0.f; r->pad[k] = 0.f;
+            float2& pm = ms.PM[(size_t)stage * ms.pcap + (q >> 1)];
+            if (k) pm.y = 0.f; else pm.x = 0.f;
         }
 }
 
@@ -68,10 +72,10 @@ __global__ void massive_prepare_kernel(ddx_state s, StepArgs a, MassiveScratch m
     const double x2 = x + vx * a.dt2, y2 = y + vy * a.dt2, z2 = z + vz * a.dt2;
     ms.P[0 * ms.cap + i] = make_body(x, y, z, m);
     ms.P[1 * ms.cap + i] = make_body(x2, y2, z2, m);
-    if (prec == DDX_PREC_MIXED) {
+    if (prec != DDX_PREC_FP64) {   // the FP32 records of the mixed and compensated dust kernels
         float4 h, l;
         split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
-        h.w = (float)m; l.w = 0.f;
+        split_hilo(m, h.w, l.w);
         ms.Phi[0 * ms.cap + i] = h; ms.Plo[0 * ms.cap + i] = l;
         if (i >= a.n_exact) store_pair_slot(ms, 0, i - a.n_exact, h, l);
         split_hilo(x2, h.x, l.x); split_hilo(y2, h.y, l.y); split_hilo(z2, h.z, l.z);
@@ -179,10 +183,10 @@ __device__ __forceinline__ void massive_two_stage_accel(const MassiveScratch& ms
 __device__ __forceinline__ void store_stage_pos(MassiveScratch& ms, int stage, int i, double x,
                                                 double y, double z, double m, int prec, int n_exact) {
     ms.P[stage * ms.cap + i] = make_body(x, y, z, m);
-    if (prec == DDX_PREC_MIXED) {
+    if (prec != DDX_PREC_FP64) {
         float4 h, l;
         split_hilo(x, h.x, l.x); split_hilo(y, h.y, l.y); split_hilo(z, h.z, l.z);
-        h.w = (float)m; l.w = 0.f;
+        split_hilo(m, h.w, l.w);
         ms.Phi[stage * ms.cap + i] = h; ms.Plo[stage * ms.cap + i] = l;
         if (i >= n_exact) store_pair_slot(ms, stage, i - n_exact, h, l);
     }
@@ -209,14 +213,17 @@ __device__ __forceinline__ void pass1_update(const ddx_state& s, const StepArgs&
     store_stage_pos(ms, 3, i, k4x, k4y, k4z, m, prec, a.n_exact);
 }
 
-template <int PREC>
+// PREC: the arithmetic of the accelerations; STORE: the precision whose stage records
+// pass 1 writes (the compensated step integrates the massive set in FP64 and writes the
+// FP32 records its dust kernel reads).
+template <int PREC, int STORE = PREC>
 __global__ void massive_pass1_kernel(ddx_state s, StepArgs a, MassiveScratch ms) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.n_grav) return;  // warp-uniform
     double acc[6];
     massive_two_stage_accel<PREC>(ms, a.n_grav, a.n_exact, a.near_eta, i, 0, 1, acc);
     if ((threadIdx.x & 31) != 0) return;
-    pass1_update(s, a, ms, i, acc, PREC);
+    pass1_update(s, a, ms, i, acc, STORE);
 }
 
 // Pass 2: A3 at P3, A4 at P4; R4; final combination (src/gpu_functions.cu:613-625).
@@ -633,7 +640,7 @@ dust_rk4_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __res
 cudaError_t launch_massive_prepare(const ddx_state& s, const StepArgs& a, MassiveScratch& ms,
                                    int precision, cudaStream_t st) {
     // the FP32 sources' pair slots in cell order, from their positions at the start of the step
-    if (precision == DDX_PREC_MIXED && ms.slot && spatial_order_on(a)) {
+    if (precision != DDX_PREC_FP64 && ms.slot && spatial_order_on(a)) {
         const cudaError_t e =
             order_bodies(s, a.n_exact, a.n_grav - a.n_exact, false, ms.src_order, nullptr, ms.slot, st);
         if (e != cudaSuccess) return e;
@@ -699,7 +706,9 @@ cudaError_t launch_massive_pass1(const ddx_state& s, const StepArgs& a, MassiveS
     if (precision == DDX_PREC_MIXED && sliced_fits(a, ms)) return launch_sliced<1>(s, a, ms, st);
     const int threads = 128;  // 4 targets per block
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
-    if (precision == DDX_PREC_MIXED)
+    if (precision == DDX_PREC_COMPENSATED)   // the massive set in FP64
+        massive_pass1_kernel<DDX_PREC_FP64, DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, slotted(ms, a));
+    else if (precision == DDX_PREC_MIXED)
         massive_pass1_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, slotted(ms, a));
     else massive_pass1_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
     return cudaGetLastError();
@@ -710,7 +719,9 @@ cudaError_t launch_massive_pass2(const ddx_state& s, const StepArgs& a, MassiveS
     if (precision == DDX_PREC_MIXED && sliced_fits(a, ms)) return launch_sliced<2>(s, a, ms, st);
     const int threads = 128;
     const int blocks = (a.n_grav * 32 + threads - 1) / threads;
-    if (precision == DDX_PREC_MIXED)
+    if (precision == DDX_PREC_COMPENSATED)
+        massive_pass2_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
+    else if (precision == DDX_PREC_MIXED)
         massive_pass2_kernel<DDX_PREC_MIXED><<<blocks, threads, 0, st>>>(s, a, slotted(ms, a));
     else massive_pass2_kernel<DDX_PREC_FP64><<<blocks, threads, 0, st>>>(s, a, ms);
     return cudaGetLastError();
@@ -737,8 +748,8 @@ cudaError_t launch_dust(const ddx_state& s, const StepArgs& a, const MassiveScra
     const int threads = dust_block_threads(a.n_dust);
     const int blocks = (a.n_dust + threads - 1) / threads;
     const size_t smem = (size_t)kDustTile * 32;
-    if (precision == DDX_PREC_MIXED) {
-        return launch_dust_mixed(s, a, ms, bins, st);
+    if (precision == DDX_PREC_MIXED || precision == DDX_PREC_COMPENSATED) {
+        return launch_dust_mixed(s, a, ms, bins, precision, st);
     } else if (a.mode == DDX_MODE_REFERENCE) {
         dust_rk4_kernel<kDustFP64Exact><<<blocks, threads, smem, st>>>(s, a, ms, bins);
     } else {

@@ -310,9 +310,15 @@ class Engine:
         return {k: getattr(cad, k) for k in ("time", "tlastd", "tlastf", "tlasts")}
 
     def set_near_radius(self, eta: float) -> None:
-        """Mixed precision: planetesimals nearer to a body than eta times its largest
-        |coordinate| take the FP64 pair force (0 turns that off)."""
+        """Mixed and compensated precision: planetesimals nearer to a body than eta times its
+        largest |coordinate| take the FP64 pair force (0 turns that off, a negative eta
+        restores the defaults of each precision)."""
         abi.check(self.lib.ddx_set_near_radius(self.ctx, C.c_double(eta)), "ddx_set_near_radius")
+
+    def set_compensated_radius(self, eta: float) -> None:
+        """DDX_PREC_COMPENSATED: spans of planetesimals nearer to a tracer than eta times its
+        largest |coordinate| take the float-float pull (inf: every span)."""
+        abi.check(self.lib.ddx_set_compensated_radius(self.ctx, C.c_double(eta)), "ddx_set_compensated_radius")
 
     def sync_status(self, stream=None) -> int:
         """Synchronise the stream; DDX_ERR_TIMEOUT (6) if a kernel of this context gave up a

@@ -41,6 +41,15 @@ extern "C" {
                                for sources within the near radius (ddx_set_near_radius),
                                which take the FP64 pair force */
 
+#define DDX_PREC_COMPENSATED 2 /* FP64 state, Kepler term, stage combination, planets and
+                               massive-set gravity; the planetesimals' pull on each tracer
+                               in float-float (pairs of FP32 numbers carried through
+                               error-free transformations, about 44 bits) for every span of
+                               planetesimals nearer than ddx_set_compensated_radius, in FP32
+                               beyond, in FP64 within the near radius.  For runs that need
+                               errors near FP64's at several times FP64's throughput;
+                               ddx_step and its variants only */
+
 /* Behaviour switch for the reference's known defects. */
 #define DDX_MODE_FIXED      0   /* defects corrected (default) */
 #define DDX_MODE_REFERENCE  1   /* defects reproduced where they are deterministic */
@@ -343,10 +352,19 @@ int ddx_sync_status(ddx_ctx *ctx, void *stream);
  * to a body (tracer or massive) than eta times that body's largest |coordinate| at the RK4
  * stage takes the FP64 pair force from the FP64 stage positions, as in DDX_PREC_FP64;
  * every other planetesimal stays FP32.  The test uses the FP32 distance, so the choice is
- * deterministic.  Default 4e-3 (0.52 AU at 130 AU); 0 turns the FP64 pulls off;
- * 0 <= eta <= 0.25, else DDX_ERR_ARG.  Applies to later steps of this context;
- * ddx_step_noalloc always uses the default. */
+ * deterministic.  DDX_PREC_COMPENSATED applies the same rule inside its float-float spans.
+ * Defaults: 4e-3 for DDX_PREC_MIXED (0.52 AU at 130 AU) and 1.6e-2 for
+ * DDX_PREC_COMPENSATED; a value set here applies to both, a negative one restores the
+ * defaults; 0 turns the FP64 pulls off; eta <= 0.25 and not NaN, else DDX_ERR_ARG.  Applies
+ * to later steps of this context; ddx_step_noalloc always uses the defaults. */
 int ddx_set_near_radius(ddx_ctx *ctx, double eta);
+
+/* Radius of the float-float spans of DDX_PREC_COMPENSATED (no counterpart in the
+ * reference).  A span of 32 planetesimals whose box lies nearer to a tracer than eta times
+ * the tracer's largest |coordinate| at the RK4 stage takes the float-float pull; farther
+ * spans take the FP32 forms of DDX_PREC_MIXED.  Default 0.5; +infinity makes every span
+ * float-float; eta >= 0, else DDX_ERR_ARG.  ddx_step_noalloc uses the default. */
+int ddx_set_compensated_radius(ddx_ctx *ctx, double eta);
 
 /* Failure-detection test hook (no counterpart in the reference).  The next mixed-precision
  * dust launch of this context leaves the TMA copy of source tile `tile` (counted over the

@@ -55,6 +55,7 @@ def test_argument_errors_without_gpu(built_lib):
     assert lib.ddx_image(None, C.byref(st), 1, 0, None, None, 1, None, 0, None) == 1
     assert lib.ddx_sed(None, C.byref(st), 1, 0, None, None, 0, 0, None) == 1
     assert lib.ddx_set_near_radius(None, C.c_double(1e-3)) == 1
+    assert lib.ddx_set_compensated_radius(None, C.c_double(0.5)) == 1
     assert lib.ddx_noalloc_sync_status(-1, None) == 1
     assert lib.ddx_debug_noalloc_lose_tile_copy(0, -1, 1000) == 1
     assert lib.ddx_debug_noalloc_lose_tile_copy(0, 0, 0) == 1

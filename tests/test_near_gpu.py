@@ -55,11 +55,11 @@ def planted(n_plsml, n_dust=4096, n_grain_pairs=64, n_body_pairs=16, seed=41):
 
 def run(engine, s, prec, eta=None, n_steps=5):
     engine.set_size_table(**s.size_table)
-    engine.set_near_radius(4e-3 if eta is None else eta)
+    engine.set_near_radius(-1.0 if eta is None else eta)
     st = DeviceState.from_numpy(s.state)
     engine.evolve(st, s.n_grav, s.dt, n_steps, make_phys(**s.phys), prec, abi.DDX_MODE_FIXED)
     torch.cuda.synchronize()
-    engine.set_near_radius(4e-3)
+    engine.set_near_radius(-1.0)      # back to the defaults
     return st.to_numpy()
 
 
@@ -98,8 +98,7 @@ def test_near_radius_zero_is_the_plain_fp32_step(engine):
 def test_near_radius_argument_checks(engine):
     lib = engine.lib
     import ctypes as C
-    assert lib.ddx_set_near_radius(engine.ctx, C.c_double(-1e-3)) == abi.DDX_ERR_ARG
     assert lib.ddx_set_near_radius(engine.ctx, C.c_double(0.3)) == abi.DDX_ERR_ARG
     assert lib.ddx_set_near_radius(engine.ctx, C.c_double(float("nan"))) == abi.DDX_ERR_ARG
     assert lib.ddx_set_near_radius(engine.ctx, C.c_double(0.25)) == abi.DDX_OK
-    assert lib.ddx_set_near_radius(engine.ctx, C.c_double(4e-3)) == abi.DDX_OK
+    assert lib.ddx_set_near_radius(engine.ctx, C.c_double(-1.0)) == abi.DDX_OK   # the defaults again
