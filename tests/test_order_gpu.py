@@ -125,3 +125,23 @@ def test_ordered_step_with_removed_non_finite_and_distant_tracers(engine, n_dust
     pm = np.stack([m[k][g:][ok] for k in ("x", "y", "z")])
     e = np.linalg.norm(pm - pf, axis=0) / np.linalg.norm(pf, axis=0)
     assert e.max() < 1e-12
+
+
+@pytest.mark.parametrize("n_plsml", [1100, 9000])
+def test_two_tracers_per_thread_identical_to_one(engine, n_plsml):
+    """From two blocks of 512 grains per SM on, the mixed step carries two tracers per thread
+    (adjacent in the visiting order).  A tracer's result depends only on its own state and
+    the massive set, so the first 20,000 grains of a 400,000-grain system step to the same
+    bits as those 20,000 grains alone, which take one tracer per thread."""
+    s = synth.dusty_ring(n_dust=400_000, n_plsml=n_plsml, seed=23, n_steps=2)
+    ng = s.n_grav
+    sub = {k: np.asarray(v)[:ng + 20000].copy() for k, v in s.state.items()}
+    engine.set_size_table(**s.size_table)
+    phys = make_phys(**s.phys)
+    big, small = DeviceState.from_numpy(s.state), DeviceState.from_numpy(sub)
+    for _ in range(2):
+        engine.step(big, ng, s.dt, phys, abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)
+        engine.step(small, ng, s.dt, phys, abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)
+    torch.cuda.synchronize()
+    for f in FIELDS:
+        assert torch.equal(getattr(big, f)[:ng + 20000], getattr(small, f)), f
