@@ -63,6 +63,7 @@ def parse():
     p.add_argument("--solar-steps", type=int, default=1000)
     p.add_argument("--scale-err-steps", type=int, default=60)
     p.add_argument("--adjoint-steps", type=int, default=2000)
+    p.add_argument("--adjoint-plsml-steps", type=int, default=20)
     return p.parse_args()
 
 
@@ -401,6 +402,15 @@ def run_ours(args, world, rank, local):
                            "scale": scale_leg(local, fp32_peak)}
     if rank == 0 and args.adjoint_steps > 0:
         line["adjoint"] = adjoint_leg(local, n_steps=args.adjoint_steps)
+    if rank == 0 and args.adjoint_plsml_steps > 0:
+        # the image-loss system with the dusty ring's 4,096 planetesimals in the massive set
+        # (FP64 all-pairs, every grain feeling every planetesimal): fewer steps, since each FP64
+        # step costs about 85 ms forward; forward, recompute and reverse all cost per step
+        k = args.adjoint_plsml_steps
+        leg = adjoint_leg(local, n_steps=k, ckpt=max(1, k // 2), n_plsml=4096)
+        leg["steps_note"] = ("%d of the workload's 2,000 steps, checkpoints every %d: the forward, the "
+                             "recompute and the reverse all cost per step" % (k, max(1, k // 2)))
+        line["adjoint_planetesimals"] = leg
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(sysm, args.cpu_sample)
     if rank == 0:
@@ -856,18 +866,19 @@ def scale_leg(local, fp32_peak, steps=2, warmup=1):
                          "peak": fp32_peak, "unit": "TFLOP/s", "frac": flops / (dust_ms / 1e3) / 1e12 / fp32_peak}}
 
 
-def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
+def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100, n_plsml=0):
     """Adjoint/forward wall-time ratio on the image-loss workload: L2 loss between the
-    image of the dusty-ring system (262,144 grains, 512x512, 2,000 steps) and a target
-    made by the same code with planet 1 at 1.2x the mass and a + 2 AU; gradients with
-    respect to planet masses, a, e, i and every grain's initial state by
-    checkpoint-and-recompute every 100 steps.  Also a central finite-difference check of
+    image of the dusty-ring system (262,144 grains, 512x512, 2,000 steps; with n_plsml
+    gravitating planetesimals in the massive set) and a target made by the same code with
+    planet 1 at 1.2x the mass and a + 2 AU; gradients with respect to planet masses, a, e, i,
+    the planetesimals' states and masses and every grain's initial state by
+    checkpoint-and-recompute every ckpt steps.  Also a central finite-difference check of
     dL/dm of planet 1 (h = 1e-6 relative)."""
     import torch
     from diskdyn_gb300 import adjoint as adj
     from diskdyn_gb300.engine import Engine, make_phys, make_view
 
-    s = adj.adjoint_system(n_dust=n_dust, xsize=512, ysize=512, n_steps=n_steps)
+    s = adj.adjoint_system(n_dust=n_dust, xsize=512, ysize=512, n_steps=n_steps, n_plsml=n_plsml)
     eng = Engine(local)
     eng.set_size_table(**s.size_table)
     o = s.optics
@@ -880,6 +891,8 @@ def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
                          dtype=torch.float64, device=dev)
     phys, view = make_phys(**s.phys), make_view(**s.view)
     el = adj.planet_elements(s)
+    plsml = torch.tensor(np.stack([s.state[k][3:ng] for k in ("x", "y", "z", "vx", "vy", "vz", "m")], 1),
+                         dtype=torch.float64, device=dev).reshape(-1, 7)
 
     def elements(grad):
         t = {k: torch.tensor(np.asarray(v, dtype=np.float64), device=dev) for k, v in el.items()}
@@ -888,8 +901,9 @@ def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
                 t[k].requires_grad_(True)
         return t
 
-    def image(t, dust):
+    def image(t, dust, pl=plsml):
         M = adj.planet_state(t["Mstar"], t["m"], t["a"], t["e"], t["i"], t["w"], t["o"], t["nu"])
+        M = torch.cat([M, pl], dim=0)
         return adj.trajectory_image(eng, M, dust, N, ids, s.dt, n_steps, ckpt, phys, view, s.image_wj)
 
     with torch.no_grad():
@@ -907,9 +921,10 @@ def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
     t_fwd = time.perf_counter() - t0
     t = elements(True)
     d = dust0.clone().requires_grad_(True)
+    pg = plsml.clone().requires_grad_(n_plsml > 0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    L = ((image(t, d) - target) ** 2).sum()
+    L = ((image(t, d, pg) - target) ** 2).sum()
     L.backward()
     torch.cuda.synchronize()
     t_grad = time.perf_counter() - t0
@@ -924,12 +939,13 @@ def adjoint_leg(local, n_dust=262144, n_steps=2000, ckpt=100):
             vals.append(((image(tp, dust0) - target) ** 2).sum().item())
     fd = (vals[0] - vals[1]) / (2 * h)
     eng.close()
-    return {"workload": "image loss, 3 massive + %d grains, %dx%d, %d steps, checkpoints every %d"
-                        % (n_dust, 512, 512, n_steps, ckpt),
+    return {"workload": "image loss, %d massive + %d grains, %dx%d, %d steps, checkpoints every %d"
+                        % (ng, n_dust, 512, 512, n_steps, ckpt),
             "forward_s": t_fwd, "forward_plus_gradient_s": t_grad, "adjoint_over_forward": t_grad / t_fwd,
             "loss": L0, "dL_dm_planet1_adjoint": g_m, "dL_dm_planet1_fd": fd,
             "fd_rel_err": abs(g_m - fd) / abs(fd) if fd != 0 else None,
-            "grad_norm_a": t["a"].grad.norm().item(), "grad_norm_dust": d.grad.norm().item()}
+            "grad_norm_a": t["a"].grad.norm().item(), "grad_norm_dust": d.grad.norm().item(),
+            "grad_norm_planetesimals": pg.grad.norm().item() if n_plsml > 0 else None}
 
 
 def cpu_baseline(sysm, n_sample):

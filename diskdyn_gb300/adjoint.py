@@ -25,10 +25,10 @@ from .engine import DeviceState, _stream_handle, make_phys, make_view
 
 class _TrajectoryImage(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, massive, dust, eng, N, ids, dt, n_steps, ckpt, phys, view, wj):
+    def forward(ctx, massive, dust, eng, N, ids, dt, n_steps, ckpt, phys, view, wj, mass):
         ng, nd = massive.shape[0], dust.shape[0]
         dev = massive.device
-        zeros = torch.zeros(nd, dtype=torch.float64, device=dev)
+        zeros = torch.zeros(nd, dtype=torch.float64, device=dev) if mass is None else mass.to(torch.float64)
         st = DeviceState(
             x=torch.cat([massive[:, 0], dust[:, 0]]).contiguous(),
             y=torch.cat([massive[:, 1], dust[:, 1]]).contiguous(),
@@ -61,12 +61,14 @@ class _TrajectoryImage(torch.autograd.Function):
                   "ddx_adjoint_backward")
         g_massive = torch.cat([gs[:, :ng].T, gm[:, None]], dim=1)
         g_dust = gs[:, ng:].T
-        return g_massive, g_dust, None, None, None, None, None, None, None, None, None
+        return g_massive, g_dust, None, None, None, None, None, None, None, None, None, None
 
 
-def trajectory_image(eng, massive, dust, N, ids, dt, n_steps, ckpt, phys, view, wj):
-    """Differentiable image of the state after n_steps (see module docstring)."""
-    return _TrajectoryImage.apply(massive, dust, eng, N, ids, dt, n_steps, ckpt, phys, view, wj)
+def trajectory_image(eng, massive, dust, N, ids, dt, n_steps, ckpt, phys, view, wj, mass=None):
+    """Differentiable image of the state after n_steps (see module docstring).  mass: the
+    grains' masses (n_dust,), which the Lorentz force divides by (phys.FLQ = 1); without them
+    the grains count as massless and feel no Lorentz force."""
+    return _TrajectoryImage.apply(massive, dust, eng, N, ids, dt, n_steps, ckpt, phys, view, wj, mass)
 
 
 def coe2rv_t(M, m, a, e, i, w, o, nu, beta=0.0):
@@ -104,14 +106,15 @@ def planet_state(Mstar, pm, pa, pe, pi, pw, po, pnu):
     return torch.stack([X, Y, Z, VX, VY, VZ, m], dim=1)
 
 
-def adjoint_system(n_dust=262144, xsize=512, ysize=512, n_steps=2000, seed=synth.SEED):
+def adjoint_system(n_dust=262144, xsize=512, ysize=512, n_steps=2000, seed=synth.SEED, n_plsml=0):
     """The image-loss workload: the dusty-ring star (1.5 Msun, L = 8.7 Lsun) with its two
-    planets (1e-3 Msun at 20 AU, 3e-4 Msun at 60 AU) and n_dust grains of the ring with
-    radiation pressure, PR and stellar-wind drag; no gravitating planetesimals.  Optics:
+    planets (1e-3 Msun at 20 AU, 3e-4 Msun at 60 AU), n_plsml gravitating planetesimals of
+    the ring and n_dust grains of the ring with radiation pressure, PR and stellar-wind
+    drag.  Optics:
     HG tables on the grains' size bins, grey grains at T = 278.3 L^(1/4) (r/AU)^(-1/2) K;
     a 512 x 512 image, 300 AU across, at 30 deg inclination, at 1.25 um (scattered light)
     and 100 um (thermal)."""
-    s = synth.dusty_ring(n_dust=n_dust, n_plsml=0, seed=seed, n_steps=n_steps)
+    s = synth.dusty_ring(n_dust=n_dust, n_plsml=n_plsml, seed=seed, n_steps=n_steps)
     synth.ring_imaging(s, xsize, ysize)
     s.name = "adjoint_ring"
     return s

@@ -2,12 +2,14 @@
 // No counterpart in the reference.
 //
 // Model (the forward these kernels differentiate exactly):
-//  - massive set (n_grav <= DDX_ADJ_MAX_GRAV bodies, star at 0): the reference's RK4 with
-//    all-pairs gravity (src/gpu_functions.cu:71-625), integrated first for every step by
-//    one single-warp kernel that keeps the stage positions P_s(n) of every step;
+//  - massive set (star at 0): the reference's RK4 with all-pairs gravity
+//    (src/gpu_functions.cu:71-625), integrated first for every step, keeping the stage
+//    positions P_s(n) of every step: up to 32 bodies by one single-warp kernel for all
+//    steps, larger sets (the planetesimals of a dusty ring) by three launches per step, a
+//    warp per body;
 //  - dust tracers: the reference's RK4 (src/gpu_functions.cu:627-943) under the star term
-//    (gravity reduced by beta + beta_sw, PR + stellar-wind drag; no Lorentz force) and the
-//    gravity of the massive bodies at their stage positions.  Tracers are independent
+//    (gravity reduced by beta + beta_sw, PR + stellar-wind drag, the Lorentz force) and the
+//    gravity of every massive body at its stage positions.  Tracers are independent
 //    given P_s(n), so each thread integrates its tracer over all steps in one launch;
 //  - image: the flux of src/gpu_functions.cu:1049-1078 deposited with bilinear weights
 //    on the four pixel centres around the projected position, so the image, and the L2
@@ -24,7 +26,10 @@
 //     bodies' stage positions and masses are reduced per block in a fixed order (a
 //     transposed shared-memory tile per warp, then the warps, then block partials summed
 //     in block order), so the gradient is deterministic; a single-warp kernel then runs
-//     the reverse sweep of the massive set.
+//     the reverse sweep of the massive set.  With more than 32 bodies the sweep runs one
+//     launch per step: the block sums of the bodies' adjoints cover that step (a 32 x 32
+//     transpose per warp, then the warps in order), are reduced in block order, and the
+//     massive set's reverse runs stage by stage, a warp per body.
 // FP64 runs at ~1/75 of the FP32 rate here, so the kernels are bound by their count of
 // FP64 operations: the forward takes one division and one square root for the star and
 // one rsqrt per body per stage, and the reverse reuses them from the record.
@@ -36,7 +41,9 @@
 namespace ddx {
 namespace {
 
-constexpr int kMaxGrav = DDX_ADJ_MAX_GRAV;
+// Massive sets up to this size run the one-warp kernels (every step in one launch); larger
+// ones the launch-per-pass kernels of the "large massive sets" section.
+constexpr int kMaxGrav = 32;
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSegComp = 15;   // per tracer per step: x, y, z, vx, vy, vz, a1, a2, a3
@@ -51,19 +58,25 @@ struct AdjArgs {
     const Body* Ps;         // [n_steps][4][ng]
     const SizeBin* bins;
     const int* id;          // [nd]
+    const double* mass;     // [nd] tracer masses (the Lorentz force divides by them)
 };
 
 
 // Per-tracer constants of the star term: a = -Fg d - Fb1 (Fb2 d + r) with
 // Fg = g0/R^3, Fb1 = c1/R^2, Fb2 = (d.r)/R^2 (src/gpu_functions.cu:691-704).
+// Lorentz force (FLQ = 1, src/gpu_functions.cu:706-713): Fl = cL iR3 (ry - Wz dx, -(rx + Wz dy), 0)
+// with cL = q Bstar Rstar^3 / m of the tracer (0 without the force).
 struct StarConst {
-    double g0, c1, inv_m0;
+    double g0, c1, inv_m0, cL;
 };
-__device__ __forceinline__ StarConst star_const(const AdjArgs& A, double m0, float bet, float betsw) {
+__device__ __forceinline__ StarConst star_const(const AdjArgs& A, double m0, float bet, float betsw, float qe,
+                                                double m) {
     StarConst k;
     k.g0 = (1.0 - bet - betsw) * m0;
     k.c1 = (A.sa.SWQ == 1) ? m0 * (bet / kLightAU + betsw / A.sa.vswAU) : bet * m0 / kLightAU;
     k.inv_m0 = 1.0 / m0;
+    // a tracer without mass feels no Lorentz force here (the reference would divide by zero)
+    k.cL = A.sa.FLQ == 1 && m > 0.0 ? (double)qe * A.sa.Bstar * A.sa.Rstar * A.sa.Rstar * A.sa.Rstar / m : 0.0;
     return k;
 }
 
@@ -87,6 +100,10 @@ __device__ __forceinline__ bool tracer_accel(const AdjArgs& A, const StarConst& 
     ax = -Fg * dx - Fb1 * (Fb2 * dx + rx);
     ay = -Fg * dy - Fb1 * (Fb2 * dy + ry);
     az = -Fg * dz - Fb1 * (Fb2 * dz + rz);
+    if (K.cL != 0.0) {
+        ax += K.cL * iR3 * (ry - A.sa.Wz * dx);
+        ay -= K.cL * iR3 * (rx + A.sa.Wz * dy);
+    }
     for (int j = 1; j < A.ng; ++j) {
         const double ex = P[j].x - x, ey = P[j].y - y, ez = P[j].z - z;
         const double R2 = ex * ex + ey * ey + ez * ez;
@@ -258,10 +275,10 @@ dust_forward_kernel(AdjArgs A, double* y, double* N, int n0, int n1, int K, doub
     double x = y[0 * nd + i], yy = y[1 * nd + i], z = y[2 * nd + i];
     double vx = y[3 * nd + i], vy = y[4 * nd + i], vz = y[5 * nd + i];
     bool alive = N[i] != 0.0;
-    float bet = 0.f, betsw = 0.f;
+    float bet = 0.f, betsw = 0.f, qe = 0.f;
     const int id = A.id[i];
-    if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
-    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw);
+    if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; qe = A.bins[id].q; }
+    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw, qe, A.mass[i]);
     const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
     for (int n = n0; n < n1; ++n) {
         if (ck && n % K == 0) {
@@ -351,9 +368,10 @@ struct RowTile {
 // per source j, the tracer's adjoints of that source's stage position and mass into T.
 // rc (stride rs): the stage's reciprocal distances kept by the recompute.  Called by
 // every lane of the warp.
+template <class Tile>
 __device__ __forceinline__ void tracer_vjp(const AdjArgs& A, const StarConst& K, const Body* P, bool on,
                                            const double* pos, const double* r, const double* g, double* Lx,
-                                           double* Lr, const double* rc, size_t rs, RowTile& T) {
+                                           double* Lr, const double* rc, size_t rs, Tile& T) {
     {   // star (source 0)
         double s4[4] = {0, 0, 0, 0};
         if (on) {
@@ -368,13 +386,25 @@ __device__ __forceinline__ void tracer_vjp(const AdjArgs& A, const StarConst& K,
             const double gD = Fb2 * gd + gr;
             // a = -Fg d - Fb1 (Fb2 d + r): g^T da/dd = cg g + cd d + cr r ; g^T da/dr = cr d - Fb1 g
             const double cg = -Fg - Fb1 * Fb2;
-            const double cd = 3.0 * K.g0 * gd * iR5 + 2.0 * (K.c1 * gD + Fb1 * gd * dr) * (iRR * iRR);
+            double cd = 3.0 * K.g0 * gd * iR5 + 2.0 * (K.c1 * gD + Fb1 * gd * dr) * (iRR * iRR);
             const double cr = -Fb1 * gd * iRR;
             const double d[3] = {dx, dy, dz};
+            // Lorentz: g . dFl/dd = cL (-Wz iR3 (gx, gy, 0) - 3 iR5 Q d), Q = gx (ry - Wz dx) - gy (rx + Wz dy);
+            // g . dFl/dr = cL iR3 (-gy, gx, 0)
+            double lg[3] = {0.0, 0.0, 0.0}, lr[3] = {0.0, 0.0, 0.0};
+            if (K.cL != 0.0) {
+                const double Wz = A.sa.Wz;
+                const double Q = g[0] * (r[1] - Wz * dx) - g[1] * (r[0] + Wz * dy);
+                cd -= 3.0 * K.cL * iR5 * Q;
+                lg[0] = -K.cL * Wz * iR3 * g[0];
+                lg[1] = -K.cL * Wz * iR3 * g[1];
+                lr[0] = -K.cL * iR3 * g[1];
+                lr[1] = K.cL * iR3 * g[0];
+            }
             for (int c = 0; c < 3; ++c) {
-                const double ld = cg * g[c] + cd * d[c] + cr * r[c];
+                const double ld = cg * g[c] + cd * d[c] + cr * r[c] + lg[c];
                 Lx[c] += ld;
-                Lr[c] += cr * d[c] - Fb1 * g[c];
+                Lr[c] += cr * d[c] - Fb1 * g[c] + lr[c];
                 s4[c] = -ld;
             }
             s4[3] = (-Fg * gd - Fb1 * gD) * K.inv_m0;
@@ -415,13 +445,15 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
     const size_t nd = A.nd;
     const bool on = i < A.nd && active[i];
     double lx[3] = {0, 0, 0}, lv[3] = {0, 0, 0};
-    float bet = 0.f, betsw = 0.f;
+    float bet = 0.f, betsw = 0.f, qe = 0.f;
+    double mi = 1.0;
     if (on) {
         for (int c = 0; c < 3; ++c) { lx[c] = lam[c * nd + i]; lv[c] = lam[(3 + c) * nd + i]; }
         const int id = A.id[i];
-        if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; }
+        if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; qe = A.bins[id].q; }
+        mi = A.mass[i];
     }
-    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw);
+    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw, qe, mi);
     RowTile T{tbuf[warp], wpart[warp], 0, 0, lane};
     const int Kseg = n1 - n0;
     const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
@@ -499,6 +531,296 @@ dust_reverse_kernel(AdjArgs A, const double* __restrict__ seg, int n0, int n1, d
     }
     if (on)
         for (int c = 0; c < 3; ++c) { lam[c * nd + i] = lx[c]; lam[(3 + c) * nd + i] = lv[c]; }
+}
+
+// ---------------------------------------------------------------------------------------
+// Large massive sets (n_grav > kMaxGrav): the massive set runs one launch per pass (forward)
+// and per stage (reverse), a warp per body; the tracers' adjoints of the bodies' stage
+// positions and masses are summed per block for every step and reduced in block order.
+// ---------------------------------------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Acceleration of body j from every other body at one stage (records P[0..ng)), the
+// m / (RR sqrt(RR)) form of massive_acc, lanes strided over the sources with a fixed
+// butterfly sum.  All 32 lanes call it.
+__device__ __forceinline__ void massive_acc_warp(const Body* __restrict__ P, int ng, int j, double& ax, double& ay,
+                                                 double& az) {
+    const int lane = threadIdx.x & 31;
+    const Body pj = P[j];
+    ax = ay = az = 0.0;
+    for (int k = lane; k < ng; k += 32) {
+        if (k == j) continue;
+        const Body pk = P[k];
+        const double dx = pk.x - pj.x, dy = pk.y - pj.y, dz = pk.z - pj.z;
+        const double RR = dx * dx + dy * dy + dz * dz;
+        if (RR > 0.0) {
+            const double f = pk.m / (RR * sqrt(RR));
+            ax += f * dx; ay += f * dy; az += f * dz;
+        }
+    }
+    ax = warp_sum_d(ax); ay = warp_sum_d(ay); az = warp_sum_d(az);
+}
+
+// Step n of the massive forward, first launch: P1 = x, P2 = x + v dt/2 (a thread per body).
+__global__ void massive_fwd_init_kernel(int ng, double dt, const double* __restrict__ xv, Body* __restrict__ P) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ng) return;
+    const double h2 = dt * 0.5;
+    const double x = xv[j], y = xv[ng + j], z = xv[2 * ng + j], m = xv[6 * ng + j];
+    P[j] = make_body(x, y, z, m);
+    P[ng + j] = make_body(x + xv[3 * ng + j] * h2, y + xv[4 * ng + j] * h2, z + xv[5 * ng + j] * h2, m);
+}
+
+// Second launch: A1 at P1 and A2 at P2 (a warp per body), then P3 = x + (v + A1 dt/2) dt/2
+// and P4 = x + (v + A2 dt/2) dt; A1, A2 kept in macc[6][ng].
+__global__ void massive_fwd_pass1_kernel(int ng, double dt, const double* __restrict__ xv, Body* __restrict__ P,
+                                         double* __restrict__ macc) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= ng) return;   // warp-uniform
+    double a[6];
+    massive_acc_warp(P, ng, j, a[0], a[1], a[2]);
+    massive_acc_warp(P + ng, ng, j, a[3], a[4], a[5]);
+    if ((threadIdx.x & 31) != 0) return;
+    const double h2 = dt * 0.5;
+    double x[3], v[3];
+    for (int c = 0; c < 3; ++c) { x[c] = xv[c * ng + j]; v[c] = xv[(3 + c) * ng + j]; }
+    for (int c = 0; c < 6; ++c) macc[c * ng + j] = a[c];
+    const double m = xv[6 * ng + j];
+    double p3[3], p4[3];
+    for (int c = 0; c < 3; ++c) {
+        p3[c] = x[c] + (v[c] + a[c] * h2) * h2;
+        p4[c] = x[c] + (v[c] + a[3 + c] * h2) * dt;
+    }
+    P[2 * ng + j] = make_body(p3[0], p3[1], p3[2], m);
+    P[3 * ng + j] = make_body(p4[0], p4[1], p4[2], m);
+}
+
+// Third launch: A3 at P3 and A4 at P4, then the RK4 combination of the body's state.
+__global__ void massive_fwd_pass2_kernel(int ng, double dt, double* __restrict__ xv, const Body* __restrict__ P,
+                                         const double* __restrict__ macc) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= ng) return;
+    double a3[3], a4[3];
+    massive_acc_warp(P + 2 * ng, ng, j, a3[0], a3[1], a3[2]);
+    massive_acc_warp(P + 3 * ng, ng, j, a4[0], a4[1], a4[2]);
+    if ((threadIdx.x & 31) != 0) return;
+    const double h2 = dt * 0.5, d6 = dt / 6.0;
+    for (int c = 0; c < 3; ++c) {
+        const double x = xv[c * ng + j], v = xv[(3 + c) * ng + j];
+        const double a1 = macc[c * ng + j], a2 = macc[(3 + c) * ng + j];
+        const double r2 = v + a1 * h2, r3 = v + a2 * h2, r4 = v + a3[c] * dt;
+        xv[c * ng + j] = x + d6 * (v + 2.0 * r2 + 2.0 * r3 + r4);
+        xv[(3 + c) * ng + j] = v + d6 * (a1 + 2.0 * a2 + 2.0 * a3[c] + a4[c]);
+    }
+}
+
+// Body adjoints of one step, lamS[27][ng]: rows 0-2 Lx, 3-5 Lv, 6-8 Lr2, 9-11 Lr3, 12-14 Lr4,
+// 15 + 3 s + c the adjoint of stage s's acceleration.  Seeded from the adjoint of the state
+// after the step, lam[6][ng] (a thread per body).
+__global__ void massive_rev_init_kernel(int ng, double dt, const double* __restrict__ lam, double* __restrict__ lamS) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ng) return;
+    const double d6 = dt / 6.0;
+    for (int c = 0; c < 3; ++c) {
+        const double lx = lam[c * ng + j], lv = lam[(3 + c) * ng + j];
+        lamS[c * ng + j] = lx;
+        lamS[(3 + c) * ng + j] = lv + d6 * lx;
+        lamS[(6 + c) * ng + j] = 2.0 * d6 * lx;
+        lamS[(9 + c) * ng + j] = 2.0 * d6 * lx;
+        lamS[(12 + c) * ng + j] = d6 * lx;
+        lamS[(15 + c) * ng + j] = d6 * lv;
+        lamS[(18 + c) * ng + j] = 2.0 * d6 * lv;
+        lamS[(21 + c) * ng + j] = 2.0 * d6 * lv;
+        lamS[(24 + c) * ng + j] = d6 * lv;
+    }
+}
+
+// Reverse stage s (3..0) of one step for body j (a warp per body): the all-pairs VJP of the
+// stage's accelerations (massive_vjp) with the tracers' adjoints mu[s][j][4] added, then
+// the stage's share of the RK4 reverse; after stage 0, lam holds the adjoint of the state
+// before the step.  lam_m accumulates the mass adjoint.
+__global__ void massive_rev_stage_kernel(int ng, double dt, const Body* __restrict__ P, const double* __restrict__ mu,
+                                         int s, double* __restrict__ lamS, double* __restrict__ lam,
+                                         double* __restrict__ lam_m) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= ng) return;
+    const int lane = threadIdx.x & 31;
+    const double* G = lamS + (size_t)(15 + 3 * s) * ng;     // adjoints of this stage's accelerations
+    const Body pj = P[j];
+    const double gj[3] = {G[j], G[ng + j], G[2 * ng + j]};
+    double ox = 0, oy = 0, oz = 0, om = 0;
+    for (int k = lane; k < ng; k += 32) {
+        if (k == j) continue;
+        const Body pk = P[k];
+        const double dx = pj.x - pk.x, dy = pj.y - pk.y, dz = pj.z - pk.z;
+        const double RR = dx * dx + dy * dy + dz * dz;
+        if (!(RR > 0.0)) continue;
+        const double ri3 = 1.0 / (RR * sqrt(RR)), ri5 = ri3 / RR;
+        const double gk[3] = {G[k], G[ng + k], G[2 * ng + k]};
+        const double vx = pj.m * gk[0] - pk.m * gj[0];
+        const double vy = pj.m * gk[1] - pk.m * gj[1];
+        const double vz = pj.m * gk[2] - pk.m * gj[2];
+        const double dv = dx * vx + dy * vy + dz * vz;
+        ox += vx * ri3 - 3.0 * dv * dx * ri5;
+        oy += vy * ri3 - 3.0 * dv * dy * ri5;
+        oz += vz * ri3 - 3.0 * dv * dz * ri5;
+        om += (gk[0] * dx + gk[1] * dy + gk[2] * dz) * ri3;
+    }
+    ox = warp_sum_d(ox); oy = warp_sum_d(oy); oz = warp_sum_d(oz); om = warp_sum_d(om);
+    if (lane != 0) return;
+    const double* m4 = mu + ((size_t)s * ng + j) * 4;
+    const double LP[3] = {ox + m4[0], oy + m4[1], oz + m4[2]};
+    lam_m[j] += om + m4[3];
+    const double h2 = dt * 0.5;
+    auto at = [&](int row, int c) -> double& { return lamS[(size_t)(row + c) * ng + j]; };
+    for (int c = 0; c < 3; ++c) {
+        at(0, c) += LP[c];
+        if (s == 3) { at(9, c) += dt * LP[c]; at(3, c) += at(12, c); at(15 + 6, c) += dt * at(12, c); }
+        else if (s == 2) { at(6, c) += h2 * LP[c]; at(3, c) += at(9, c); at(15 + 3, c) += h2 * at(9, c); }
+        else if (s == 1) { at(3, c) += h2 * LP[c]; at(3, c) += at(6, c); at(15, c) += h2 * at(6, c); }
+        else { lam[c * ng + j] = at(0, c); lam[(3 + c) * ng + j] = at(3, c); }
+    }
+}
+
+// Block sums of the tracers' adjoints of the bodies' stage positions and masses: per warp the
+// RowTile transpose (8 sources of 4 values per round), then the warps' sums added in warp
+// order by the first 32 threads and written to out[4 * source + c].  Every thread of the
+// block calls put4 for every source.
+struct BlockRows {
+    double (*tb)[32];
+    double (*ws)[32];
+    double* out;
+    int rows, j0, lane, warp;
+
+    __device__ __forceinline__ void flush() {
+        if (rows == 0) return;
+        __syncwarp();
+        int p = 1;
+        while (2 * p * rows <= 32) p *= 2;
+        const int w = 32 / p, row = lane / p, part = lane % p;
+        double t = 0.0;
+        if (row < rows)
+            for (int k = 0; k < w; ++k) t += tb[row][(part * w + k + row) & 31];
+        for (int o = p / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (row < rows && part == 0) ws[warp][row] = t;
+        __syncthreads();
+        if ((int)threadIdx.x < rows) {
+            double u = 0.0;
+            for (int v = 0; v < kWarps; ++v) u += ws[v][threadIdx.x];
+            out[(size_t)j0 * 4 + threadIdx.x] = u;
+        }
+        __syncthreads();
+        j0 += rows / 4;
+        rows = 0;
+    }
+    __device__ __forceinline__ void put4(const double* v) {
+        if (rows == 32) flush();
+        for (int c = 0; c < 4; ++c) tb[rows + c][(lane + rows + c) & 31] = v[c];
+        rows += 4;
+    }
+};
+
+// Reverse sweep of one step n (record k of the segment) for every tracer, with the bodies'
+// adjoints of its four stages summed per block into part[block][s][j][4].  lam [6][nd]: the
+// tracers' adjoints after the step on entry, before it on exit.
+__global__ void __launch_bounds__(kThreads)
+dust_reverse_step_kernel(AdjArgs A, const double* __restrict__ seg, int k, int n, double* __restrict__ lam,
+                         const unsigned char* __restrict__ active, double* __restrict__ part) {
+    __shared__ double tbuf[kWarps][32][32];
+    __shared__ double ws[kWarps][32];
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t nd = A.nd;
+    const bool on = i < A.nd && active[i];
+    double lx[3] = {0, 0, 0}, lv[3] = {0, 0, 0};
+    float bet = 0.f, betsw = 0.f, qe = 0.f;
+    double mi = 1.0;
+    if (on) {
+        for (int c = 0; c < 3; ++c) { lx[c] = lam[c * nd + i]; lv[c] = lam[(3 + c) * nd + i]; }
+        const int id = A.id[i];
+        if (id >= 0 && id < A.sa.n_grid) { bet = A.bins[id].beta; betsw = A.bins[id].betasw; qe = A.bins[id].q; }
+        mi = A.mass[i];
+    }
+    const StarConst K0 = star_const(A, A.Ps[0].m, bet, betsw, qe, mi);
+    const double dt = A.dt, h2 = dt / 2.0, d6 = dt / 6.0;
+    const size_t rstage = (size_t)(2 + A.nir) * nd;
+    const double* S = seg + (size_t)k * A.ncomp * nd + (on ? i : 0);
+    const double* rc = S + kSegComp * nd;
+    double st[kSegComp];
+    for (int c = 0; c < kSegComp; ++c) st[c] = on ? S[c * nd] : 0.0;
+    const double* x = st;
+    const double* v = st + 3;
+    const double* a1 = st + 6;
+    const double* a2 = st + 9;
+    const double* a3 = st + 12;
+    double x2[3], r2[3], x3[3], r3[3], x4[3], r4[3];
+    for (int c = 0; c < 3; ++c) {
+        x2[c] = x[c] + v[c] * h2; r2[c] = v[c] + a1[c] * h2;
+        x3[c] = x[c] + r2[c] * h2; r3[c] = v[c] + a2[c] * h2;
+        x4[c] = x[c] + r3[c] * dt; r4[c] = v[c] + a3[c] * dt;
+    }
+    double Lx[3], Lv[3], Lr2[3], Lr3[3], Lr4[3], La1[3], La2[3], La3[3], La4[3];
+    for (int c = 0; c < 3; ++c) {
+        Lx[c] = lx[c];
+        Lv[c] = lv[c] + d6 * lx[c];
+        Lr2[c] = Lr3[c] = 2.0 * d6 * lx[c];
+        Lr4[c] = d6 * lx[c];
+        La1[c] = d6 * lv[c];
+        La2[c] = La3[c] = 2.0 * d6 * lv[c];
+        La4[c] = d6 * lv[c];
+    }
+    const Body* P = A.Ps + (size_t)n * 4 * A.ng;
+    double* pb = part + (size_t)blockIdx.x * 4 * A.ng * 4;
+    double Ls[3], Lq[3];
+    {   // stage 4
+        BlockRows T{tbuf[warp], ws, pb + (size_t)3 * A.ng * 4, 0, 0, lane, warp};
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, K0, P + 3 * A.ng, on, x4, r4, La4, Ls, Lq, rc + 3 * rstage, nd, T);
+        T.flush();
+        for (int c = 0; c < 3; ++c) {
+            Lr4[c] += Lq[c];
+            Lx[c] += Ls[c]; Lr3[c] += dt * Ls[c];
+            Lv[c] += Lr4[c]; La3[c] += dt * Lr4[c];
+        }
+    }
+    {   // stage 3
+        BlockRows T{tbuf[warp], ws, pb + (size_t)2 * A.ng * 4, 0, 0, lane, warp};
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, K0, P + 2 * A.ng, on, x3, r3, La3, Ls, Lq, rc + 2 * rstage, nd, T);
+        T.flush();
+        for (int c = 0; c < 3; ++c) {
+            Lr3[c] += Lq[c];
+            Lx[c] += Ls[c]; Lr2[c] += h2 * Ls[c];
+            Lv[c] += Lr3[c]; La2[c] += h2 * Lr3[c];
+        }
+    }
+    {   // stage 2
+        BlockRows T{tbuf[warp], ws, pb + (size_t)1 * A.ng * 4, 0, 0, lane, warp};
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, K0, P + A.ng, on, x2, r2, La2, Ls, Lq, rc + rstage, nd, T);
+        T.flush();
+        for (int c = 0; c < 3; ++c) {
+            Lr2[c] += Lq[c];
+            Lx[c] += Ls[c]; Lv[c] += h2 * Ls[c];
+            Lv[c] += Lr2[c]; La1[c] += h2 * Lr2[c];
+        }
+    }
+    {   // stage 1
+        BlockRows T{tbuf[warp], ws, pb, 0, 0, lane, warp};
+        Ls[0] = Ls[1] = Ls[2] = 0.0; Lq[0] = Lq[1] = Lq[2] = 0.0;
+        tracer_vjp(A, K0, P, on, x, v, La1, Ls, Lq, rc, nd, T);
+        T.flush();
+        for (int c = 0; c < 3; ++c) {
+            Lx[c] += Ls[c]; Lv[c] += Lq[c];
+        }
+    }
+    if (on)
+        for (int c = 0; c < 3; ++c) { lam[c * nd + i] = Lx[c]; lam[(3 + c) * nd + i] = Lv[c]; }
 }
 
 // mu[k][s][j][c] = sum over blocks of part[b][k][s][j][c], in block order.
@@ -677,7 +999,8 @@ __global__ void image_splat_adjoint_kernel(const double* __restrict__ y, const d
 }
 
 // Splits the SoA ddx_state into the adjoint's layouts.
-__global__ void gather_state_kernel(ddx_state s, int ng, int nd, double* xv_m, double* y, double* N, int* idv) {
+__global__ void gather_state_kernel(ddx_state s, int ng, int nd, double* xv_m, double* y, double* N, int* idv,
+                                    double* md) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ng) {
         xv_m[0 * ng + i] = s.x[i]; xv_m[1 * ng + i] = s.y[i]; xv_m[2 * ng + i] = s.z[i];
@@ -690,6 +1013,7 @@ __global__ void gather_state_kernel(ddx_state s, int ng, int nd, double* xv_m, d
         y[3 * (size_t)nd + i] = s.vx[t]; y[4 * (size_t)nd + i] = s.vy[t]; y[5 * (size_t)nd + i] = s.vz[t];
         N[i] = s.N[t];
         idv[i] = s.id[t];
+        md[i] = s.m[t];
     }
 }
 
@@ -720,6 +1044,8 @@ struct AdjointScratch {
     double *xv_m = nullptr, *y0 = nullptr, *y = nullptr, *N0 = nullptr, *N = nullptr, *ck = nullptr,
            *seg = nullptr, *lam = nullptr, *part = nullptr, *mu = nullptr, *lam_m = nullptr, *lam_mass = nullptr;
     int* idv = nullptr;
+    double* md = nullptr;                 // [nd] tracer masses
+    double *macc = nullptr, *lamS = nullptr;   // large massive sets: [6][ng] forward A1, A2; [27][ng] body adjoints
     unsigned char* active = nullptr;
     Body* Ps = nullptr;
     ViewConst* vc = nullptr;
@@ -731,6 +1057,7 @@ void adjoint_free(AdjointScratch*& a) {
     cudaFree(a->xv_m); cudaFree(a->y0); cudaFree(a->y); cudaFree(a->N0); cudaFree(a->N); cudaFree(a->ck);
     cudaFree(a->seg); cudaFree(a->lam); cudaFree(a->part); cudaFree(a->mu); cudaFree(a->lam_m);
     cudaFree(a->lam_mass); cudaFree(a->idv); cudaFree(a->active); cudaFree(a->Ps); cudaFree(a->vc);
+    cudaFree(a->md); cudaFree(a->macc); cudaFree(a->lamS);
     delete a;
     a = nullptr;
 }
@@ -751,6 +1078,7 @@ static AdjArgs adj_args(const AdjointScratch& a, const SizeBin* bins) {
     A.Ps = a.Ps;
     A.bins = bins;
     A.id = a.idv;
+    A.mass = a.md;
     return A;
 }
 
@@ -763,13 +1091,20 @@ int adjoint_forward(AdjointScratch*& a, const ddx_state& s, int ng, int nd, doub
     a->nck = n_steps / K + 1;
     a->nblk = (nd + kThreads - 1) / kThreads;
     const size_t nd6 = 6ull * nd;
+    // a large massive set keeps one step's block sums, a small one a whole segment's
+    const bool large = ng > kMaxGrav;
+    const size_t part_words = large ? (size_t)a->nblk * 4 * ng * 4 : (size_t)a->nblk * K * 4 * ng * 4;
+    const size_t mu_words = large ? (size_t)4 * ng * 4 : (size_t)K * 4 * ng * 4;
     bool fail = cudaMalloc(&a->xv_m, sizeof(double) * 7 * ng) || cudaMalloc(&a->y0, sizeof(double) * nd6) ||
                 cudaMalloc(&a->y, sizeof(double) * nd6) || cudaMalloc(&a->N0, sizeof(double) * nd) ||
                 cudaMalloc(&a->N, sizeof(double) * nd) || cudaMalloc(&a->ck, sizeof(double) * nd6 * a->nck) ||
                 cudaMalloc(&a->seg, sizeof(double) * (size_t)record_comps(ng) * nd * K) ||
                 cudaMalloc(&a->lam, sizeof(double) * nd6) ||
-                cudaMalloc(&a->part, sizeof(double) * (size_t)a->nblk * K * 4 * ng * 4) ||
-                cudaMalloc(&a->mu, sizeof(double) * (size_t)K * 4 * ng * 4) ||
+                cudaMalloc(&a->part, sizeof(double) * (part_words > 0 ? part_words : 1)) ||
+                cudaMalloc(&a->mu, sizeof(double) * mu_words) ||
+                cudaMalloc(&a->md, sizeof(double) * (nd > 0 ? nd : 1)) ||
+                (large && (cudaMalloc(&a->macc, sizeof(double) * 6 * ng) ||
+                           cudaMalloc(&a->lamS, sizeof(double) * 27 * ng))) ||
                 cudaMalloc(&a->lam_m, sizeof(double) * 6 * ng) || cudaMalloc(&a->lam_mass, sizeof(double) * ng) ||
                 cudaMalloc(&a->idv, sizeof(int) * nd) || cudaMalloc(&a->active, nd) ||
                 cudaMalloc(&a->Ps, sizeof(Body) * (size_t)n_steps * 4 * ng) || cudaMalloc(&a->vc, sizeof(ViewConst));
@@ -780,8 +1115,19 @@ int adjoint_forward(AdjointScratch*& a, const ddx_state& s, int ng, int nd, doub
     }
     const int thr = 256;
     const int blk = ((nd > ng ? nd : ng) + thr - 1) / thr;
-    gather_state_kernel<<<blk, thr, 0, st>>>(s, ng, nd, a->xv_m, a->y0, a->N0, a->idv);
-    massive_traj_kernel<<<1, 32, 0, st>>>(ng, n_steps, dt, a->xv_m, a->Ps);
+    gather_state_kernel<<<blk, thr, 0, st>>>(s, ng, nd, a->xv_m, a->y0, a->N0, a->idv, a->md);
+    if (!large) {
+        massive_traj_kernel<<<1, 32, 0, st>>>(ng, n_steps, dt, a->xv_m, a->Ps);
+    } else {
+        // three launches per step (a warp per body), the stage records of every step kept
+        const int tb = 256, wb = (ng * 32 + tb - 1) / tb;
+        for (int n = 0; n < n_steps; ++n) {
+            Body* P = a->Ps + (size_t)n * 4 * ng;
+            massive_fwd_init_kernel<<<(ng + tb - 1) / tb, tb, 0, st>>>(ng, dt, a->xv_m, P);
+            massive_fwd_pass1_kernel<<<wb, tb, 0, st>>>(ng, dt, a->xv_m, P, a->macc);
+            massive_fwd_pass2_kernel<<<wb, tb, 0, st>>>(ng, dt, a->xv_m, P, a->macc);
+        }
+    }
     cudaMemcpyAsync(a->y, a->y0, sizeof(double) * nd6, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
     const AdjArgs A = adj_args(*a, bins);
@@ -824,13 +1170,33 @@ int adjoint_backward(AdjointScratch* a, const double* G, double* grad_state, dou
                 cudaMemcpyAsync(a->N, a->N0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st);
                 dust_forward_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->y, a->N, n0, n1, K, nullptr, a->seg, n0);
             }
-            dust_reverse_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->seg, n0, n1, a->lam, a->active, a->part);
-            const int per = Kseg * 4 * ng * 4;
-            reduce_parts_kernel<<<(per + 255) / 256, 256, 0, st>>>(a->part, a->nblk, per, a->mu);
+            if (ng <= kMaxGrav) {
+                dust_reverse_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->seg, n0, n1, a->lam, a->active, a->part);
+                const int per = Kseg * 4 * ng * 4;
+                reduce_parts_kernel<<<(per + 255) / 256, 256, 0, st>>>(a->part, a->nblk, per, a->mu);
+            }
         } else {
-            cudaMemsetAsync(a->mu, 0, sizeof(double) * (size_t)Kseg * 4 * ng * 4, st);
+            cudaMemsetAsync(a->mu, 0, sizeof(double) * (size_t)(ng <= kMaxGrav ? Kseg : 1) * 4 * ng * 4, st);
         }
-        massive_reverse_kernel<<<1, 32, 0, st>>>(ng, a->dt, a->Ps, a->mu, n0, n1, a->lam_m, a->lam_mass);
+        if (ng <= kMaxGrav) {
+            massive_reverse_kernel<<<1, 32, 0, st>>>(ng, a->dt, a->Ps, a->mu, n0, n1, a->lam_m, a->lam_mass);
+            continue;
+        }
+        // large massive set: per step, the tracers' reverse with block sums of the bodies'
+        // adjoints, their reduction, then the massive set's reverse stage by stage
+        const int tb = 256, wb = (ng * 32 + tb - 1) / tb;
+        const int per = 4 * ng * 4;
+        for (int n = n1 - 1; n >= n0; --n) {
+            if (nd > 0) {
+                dust_reverse_step_kernel<<<a->nblk, kThreads, 0, st>>>(A, a->seg, n - n0, n, a->lam, a->active,
+                                                                       a->part);
+                reduce_parts_kernel<<<(per + 255) / 256, 256, 0, st>>>(a->part, a->nblk, per, a->mu);
+            }
+            massive_rev_init_kernel<<<(ng + tb - 1) / tb, tb, 0, st>>>(ng, a->dt, a->lam_m, a->lamS);
+            for (int sg = 3; sg >= 0; --sg)
+                massive_rev_stage_kernel<<<wb, tb, 0, st>>>(ng, a->dt, a->Ps + ((size_t)n * 4 + sg) * ng, a->mu, sg,
+                                                            a->lamS, a->lam_m, a->lam_mass);
+        }
     }
     const int thr = 256, blk = ((nd > ng ? nd : ng) + thr - 1) / thr;
     scatter_grad_kernel<<<blk, thr, 0, st>>>(ng, nd, a->lam_m, a->lam, grad_state);

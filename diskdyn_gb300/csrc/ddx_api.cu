@@ -569,7 +569,6 @@ int ddx_adjoint_forward(ddx_ctx* c, const ddx_state* s, int n_grav, int n_dust, 
                         int ckpt_every, const ddx_phys* phys, const ddx_view* view, const int* wj, int n_img,
                         double* image, void* stream) {
     if (!c || !state_ok(s) || !phys || !view || !wj || !image || n_steps < 1 || ckpt_every < 1) return DDX_ERR_ARG;
-    if (phys->FLQ != 0) return DDX_ERR_ARG;   // the adjoint does not cover the Lorentz force
     if (n_grav > DDX_ADJ_MAX_GRAV) return DDX_ERR_RANGE;
     if (n_img < 1 || n_img > kMaxImages || view->xsize < 1 || view->ysize < 1 || !(view->fov > 0.0)) return DDX_ERR_ARG;
     if (!c->bins || !c->optics_set) return DDX_ERR_STATE;

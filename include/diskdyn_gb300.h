@@ -305,9 +305,12 @@ int ddx_dust_grid(ddx_ctx *ctx, int n_wav, const double *w, const double *in,
 /* Discrete adjoint of the trajectory and image (no counterpart in the reference).
  *
  * ddx_adjoint_forward integrates the initial state `s` (read only) for n_steps fixed-dt
- * RK4 steps in FP64 -- the massive set (at most DDX_ADJ_MAX_GRAV bodies) and the dust
- * tracers under the physics of ddx_step except the Lorentz force (phys->FLQ must be 0) --
- * keeping a checkpoint of the tracer state every ckpt_every steps in the context.  It
+ * RK4 steps in FP64 -- the massive set (at most DDX_ADJ_MAX_GRAV bodies: star, planets and
+ * gravitating planetesimals, all-pairs) and the dust tracers under the physics of ddx_step
+ * (radiation pressure, PR and stellar-wind drag, the Lorentz force when phys->FLQ is 1, with
+ * the tracers' masses from s->m, a massless tracer feeling none; the gravity of every massive
+ * body) -- keeping the massive set's stage positions of every step and a checkpoint of the
+ * tracer state every ckpt_every steps in the context.  It
  * then writes image[n_img][xsize*ysize] (device): the flux of ddx_image deposited with
  * bilinear weights on the four pixel centres around each tracer's projected position
  * (pixel (x, y) centred at psca*(x + 1/2 - xsize/2)), which is continuous in the
@@ -318,7 +321,7 @@ int ddx_dust_grid(ddx_ctx *ctx, int n_wav, const double *w, const double *in,
  * vz; device) and dL/d(mass*4pi^2) of the massive bodies to grad_mass[n_grav] (device),
  * by checkpoint-and-recompute: every segment is recomputed from its checkpoint and swept
  * backwards through the RK4 stages.  One backward per forward. */
-#define DDX_ADJ_MAX_GRAV 32
+#define DDX_ADJ_MAX_GRAV 131072
 int ddx_adjoint_forward(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
                         int n_steps, int ckpt_every, const ddx_phys *phys, const ddx_view *view,
                         const int *wj, int n_img, double *image, void *stream);

@@ -1,8 +1,8 @@
 """ORACLE -- test infrastructure, not product code.
 
 FP64 reference for the discrete adjoint: the RK4 trajectory (massive all-pairs gravity,
-tracers under the star term with radiation pressure, PR and stellar-wind drag and the
-bodies' gravity -- src/gpu_functions.cu:71-943 without the Lorentz force) and the
+tracers under the star term with radiation pressure, PR and stellar-wind drag, the
+optional Lorentz force and the bodies' gravity -- src/gpu_functions.cu:71-943) and the
 bilinear-splat image of the flux (src/gpu_functions.cu:1049-1078), written with torch
 float64 operations on the CPU.  torch.autograd differentiates it, which gives an
 independent reference gradient for the hand-written adjoint kernels.  Small systems only.
@@ -22,7 +22,9 @@ PI = 3.14159265358979323846
 NR = 100
 
 
-def star_term(d, r, m0, bet, betsw, SWQ, vsw):
+def star_term(d, r, m0, bet, betsw, SWQ, vsw, lorentz=None):
+    """lorentz: None, or (cL, Wz) with cL = q Bstar Rstar^3 / m per tracer (nd, 1): the force
+    cL (ry - Wz dx, -(rx + Wz dy), 0) / R^3 of src/gpu_functions.cu:706-713."""
     RR = (d * d).sum(-1, keepdim=True)
     R3 = RR * torch.sqrt(RR)
     Fg = (1.0 - bet - betsw) * m0 / R3
@@ -31,7 +33,13 @@ def star_term(d, r, m0, bet, betsw, SWQ, vsw):
     else:
         Fb1 = bet * m0 / LIGHT_AU / RR
     Fb2 = (d * r).sum(-1, keepdim=True) / RR
-    return -Fg * d - Fb1 * (Fb2 * d + r)
+    a = -Fg * d - Fb1 * (Fb2 * d + r)
+    if lorentz is not None:
+        cL, Wz = lorentz
+        flx = cL / R3 * (r[:, 1:2] - Wz * d[:, 0:1])
+        fly = -cL / R3 * (r[:, 0:1] + Wz * d[:, 1:2])
+        a = a + torch.cat([flx, fly, torch.zeros_like(flx)], dim=1)
+    return a
 
 
 def massive_acc(P, m):
@@ -43,8 +51,8 @@ def massive_acc(P, m):
     return (f[:, :, None] * d).sum(1)
 
 
-def dust_acc(x, r, P, m, bet, betsw, SWQ, vsw):
-    a = star_term(x - P[0], r, m[0], bet, betsw, SWQ, vsw)
+def dust_acc(x, r, P, m, bet, betsw, SWQ, vsw, lorentz=None):
+    a = star_term(x - P[0], r, m[0], bet, betsw, SWQ, vsw, lorentz)
     for j in range(1, len(m)):
         d = P[j] - x
         RR = (d * d).sum(-1, keepdim=True)
@@ -52,8 +60,11 @@ def dust_acc(x, r, P, m, bet, betsw, SWQ, vsw):
     return a
 
 
-def trajectory(massive, dust, bet, betsw, dt, n_steps, SWQ, vsw):
-    """massive (ng, 7), dust (nd, 6) -> dust state after n_steps (nd, 6)."""
+def trajectory(massive, dust, bet, betsw, dt, n_steps, SWQ, vsw, lorentz=None):
+    """massive (ng, 7), dust (nd, 6) -> dust state after n_steps (nd, 6).  lorentz: see
+    star_term (cL per tracer, shape (nd,))."""
+    if lorentz is not None:
+        lorentz = (lorentz[0][:, None], lorentz[1])
     xm, vm, m = massive[:, 0:3], massive[:, 3:6], massive[:, 6]
     xd, vd = dust[:, 0:3], dust[:, 3:6]
     bet = bet[:, None]
@@ -71,13 +82,13 @@ def trajectory(massive, dust, bet, betsw, dt, n_steps, SWQ, vsw):
         R4 = vm + A3 * dt
         P4 = xm + R3 * dt
         A4 = massive_acc(P4, m)
-        a1 = dust_acc(xd, vd, P1, m, bet, betsw, SWQ, vsw)
+        a1 = dust_acc(xd, vd, P1, m, bet, betsw, SWQ, vsw, lorentz)
         r2 = vd + a1 * h2
-        a2 = dust_acc(xd + vd * h2, r2, P2, m, bet, betsw, SWQ, vsw)
+        a2 = dust_acc(xd + vd * h2, r2, P2, m, bet, betsw, SWQ, vsw, lorentz)
         r3 = vd + a2 * h2
-        a3 = dust_acc(xd + r2 * h2, r3, P3, m, bet, betsw, SWQ, vsw)
+        a3 = dust_acc(xd + r2 * h2, r3, P3, m, bet, betsw, SWQ, vsw, lorentz)
         r4 = vd + a3 * dt
-        a4 = dust_acc(xd + r3 * dt, r4, P4, m, bet, betsw, SWQ, vsw)
+        a4 = dust_acc(xd + r3 * dt, r4, P4, m, bet, betsw, SWQ, vsw, lorentz)
         xd = xd + d6 * (vd + 2.0 * (r2 + r3) + r4)
         vd = vd + d6 * (a1 + 2.0 * (a2 + a3) + a4)
         xm = xm + d6 * (vm + 2.0 * R2 + 2.0 * R3 + R4)

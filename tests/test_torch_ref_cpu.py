@@ -39,3 +39,38 @@ def test_torch_splat_flux_matches_c_oracle_image_flux():
     Fo, _ = oc.image(s.state, ng, s.optics, s.size_table["size"], s.view, s.image_wj)
     for k in range(len(s.image_wj)):
         assert abs(img[k].sum().item() / Fo[k].sum() - 1.0) < 1e-13
+
+
+def lorentz_system():
+    """The image-loss ring with 40 gravitating planetesimals, charged grains and a stellar
+    field (the Lorentz force on)."""
+    s = adj.adjoint_system(n_dust=96, xsize=64, ysize=64, n_steps=6, seed=31, n_plsml=40)
+    s.phys = dict(s.phys, FLQ=1, Bstar=5e-20, Wz=14.6)
+    s.size_table = dict(s.size_table, q=np.linspace(1e-3, 2e-3, len(s.size_table["q"])).astype(np.float32))
+    return s
+
+
+def lorentz_constants(s):
+    """cL = q Bstar Rstar^3 / m per tracer, the Lorentz force's coefficient."""
+    ng = s.n_grav
+    ids = s.state["id"][ng:]
+    q = s.size_table["q"].astype(np.float64)[ids]
+    return torch.tensor(q * s.phys["Bstar"] * s.phys["Rstar"] ** 3 / s.state["m"][ng:])
+
+
+def test_torch_trajectory_with_planetesimals_and_lorentz_matches_c_oracle():
+    s = lorentz_system()
+    ng = s.n_grav
+    ids = torch.tensor(s.state["id"][ng:], dtype=torch.int64)
+    beta = torch.tensor(s.size_table["beta"].astype(np.float64))[ids]
+    betasw = torch.tensor(s.size_table["betasw"].astype(np.float64))[ids]
+    massive = torch.tensor(np.stack([s.state[k][:ng] for k in ("x", "y", "z", "vx", "vy", "vz", "m")], 1))
+    dust = torch.tensor(np.stack([s.state[k][ng:] for k in ("x", "y", "z", "vx", "vy", "vz")], 1))
+    with torch.no_grad():
+        out = tr.trajectory(massive, dust, beta, betasw, s.dt, 6, s.phys["SWQ"], s.phys["vsw_AUyr"],
+                            lorentz=(lorentz_constants(s), s.phys["Wz"])).numpy()
+        plain = tr.trajectory(massive, dust, beta, betasw, s.dt, 6, s.phys["SWQ"], s.phys["vsw_AUyr"]).numpy()
+    ref = oc.step(s.state, ng, s.dt, s.size_table, s.phys, 6)
+    for c, k in enumerate(("x", "y", "z", "vx", "vy", "vz")):
+        np.testing.assert_allclose(out[:, c], ref[k][ng:], rtol=1e-12, atol=1e-12)
+    assert np.abs(plain[:, 3] - out[:, 3]).max() > 1e-9   # the force matters on this system
