@@ -612,58 +612,93 @@ __global__ void photo_prepare_kernel(OpticsDev o, const ViewConst* __restrict__ 
 // to 4), in the wavelengths' scaled domain (2^esh), as 16-byte vector atomics: one request
 // adds four wavelengths of a tracer, a quarter of the requests of one FP64 atomic per
 // wavelength, and FP32 atomics do not issue through the FP64 pipe.
+// Warp aggregation: the lanes of a warp whose tracers land on the same pixel are grouped
+// (__match_any_sync on the pixel index); the lowest lane of a group adds the group's fluxes
+// (shuffles, in lane order) and issues one atomic for all of them.  A warp whose tracers all
+// fall on different pixels skips the shuffles.  The gain grows with the tracers per pixel a
+// warp sees, i.e. with how the tracers are ordered in the state.
 // image_convert_kernel then writes the FP64 x-major images.
 __global__ void __launch_bounds__(256)
 image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ vcp, View32 v32, OpticsDev o,
                    ImageList il, PhotoConst pc, float* __restrict__ Fi, int K4,
                    unsigned long long* __restrict__ counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_dust) return;
-    const int t = n_grav + i;
-    const int id = s.id[t];
-    if (id < 0 || id >= o.n_grid) return;
-    const double x = s.x[t], y = s.y[t], z = s.z[t];
-    const float xf = d2f_trunc(x), yf = d2f_trunc(y), zf = d2f_trunc(z);
-    const float R = sqrtf(fmaf(xf, xf, fmaf(yf, yf, zf * zf)));
-    const float x1 = xf * v32.cr - yf * v32.sr;
-    const float y1 = xf * v32.sr + yf * v32.cr;
-    const float y2 = y1 * v32.ci + zf * v32.si;
-    const float u = (x1 * v32.cp - y2 * v32.sp + v32.hx) * v32.inv_psca;
-    const float w = (x1 * v32.sp + y2 * v32.cp + v32.hy) * v32.inv_psca;
-    const float g = 64.0f * kEps32 * (R * v32.inv_psca + fmaxf(fabsf(u), fabsf(w)) + 1.0f);
-    int xim, yim;
-    if (near_edge32(u, g) || near_edge32(w, g)) {
-        pixel_fp64(x, y, z, *vcp, xim, yim, counters);
-    } else {
-        xim = (int)floorf(u);
-        yim = (int)floorf(w);
-    }
-    if (xim < 0 || xim > v32.xsize - 1 || yim < 0 || yim > v32.ysize - 1) return;
-    if (!(R > v32.Rmin * (1.0f + 1e-5f))) {
-        if (R < v32.Rmin * (1.0f - 1e-5f)) return;
-        if (!outside_rmin_fp64(x, y, z, o.Rmin)) return;
-    }
+    const int lane = threadIdx.x & 31;
+    bool valid = false;
+    size_t pix = 0;
     Tracer32 tr;
-    tracer32_photometry(R, scatter_cos32(y1, zf, R, R * R, v32), id, d2f_trunc(s.N[t]), v32, o, tr);
-    const size_t pix = (size_t)v32.ysize * xim + yim;
-    const float2* lq2 = o.lQp32p + ((size_t)tr.id * (o.n_theta - 1) + tr.cm) * o.n_wav;
-    const float2* A = pc.A + (size_t)tr.id * pc.n_lam;
+    if (i < n_dust) {
+        const int t = n_grav + i;
+        const int id = s.id[t];
+        if (id >= 0 && id < o.n_grid) {
+            const double x = s.x[t], y = s.y[t], z = s.z[t];
+            const float xf = d2f_trunc(x), yf = d2f_trunc(y), zf = d2f_trunc(z);
+            const float R = sqrtf(fmaf(xf, xf, fmaf(yf, yf, zf * zf)));
+            const float x1 = xf * v32.cr - yf * v32.sr;
+            const float y1 = xf * v32.sr + yf * v32.cr;
+            const float y2 = y1 * v32.ci + zf * v32.si;
+            const float u = (x1 * v32.cp - y2 * v32.sp + v32.hx) * v32.inv_psca;
+            const float w = (x1 * v32.sp + y2 * v32.cp + v32.hy) * v32.inv_psca;
+            const float g = 64.0f * kEps32 * (R * v32.inv_psca + fmaxf(fabsf(u), fabsf(w)) + 1.0f);
+            int xim, yim;
+            if (near_edge32(u, g) || near_edge32(w, g)) {
+                pixel_fp64(x, y, z, *vcp, xim, yim, counters);
+            } else {
+                xim = (int)floorf(u);
+                yim = (int)floorf(w);
+            }
+            valid = !(xim < 0 || xim > v32.xsize - 1 || yim < 0 || yim > v32.ysize - 1);
+            if (valid && !(R > v32.Rmin * (1.0f + 1e-5f)))
+                valid = !(R < v32.Rmin * (1.0f - 1e-5f)) && outside_rmin_fp64(x, y, z, o.Rmin);
+            if (valid) {
+                tracer32_photometry(R, scatter_cos32(y1, zf, R, R * R, v32), id, d2f_trunc(s.N[t]), v32, o, tr);
+                pix = (size_t)v32.ysize * xim + yim;
+            }
+        }
+    }
+    // group the lanes by pixel (a lane without a pixel gets a key of its own)
+    const unsigned long long key = valid ? (unsigned long long)pix : ~0ull - (unsigned long long)lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const bool lead = valid && (__ffs(peers) - 1 == lane);
+    const int rounds = __reduce_max_sync(0xffffffffu, valid ? __popc(peers) - 1 : 0);
+    if (!valid && rounds == 0) return;   // no shuffles in this warp: nothing left for this lane
+    const float2* lq2 = valid ? o.lQp32p + ((size_t)tr.id * (o.n_theta - 1) + tr.cm) * o.n_wav : nullptr;
+    const float2* A = valid ? pc.A + (size_t)tr.id * pc.n_lam : nullptr;
     float* row = Fi + pix * K4;
     // eight wavelengths at a time, their table loads issued together before the arithmetic
     for (int g = 0; g < il.n; g += 8) {
-        float2 lv[8], av[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int k = g + u;
-            lv[u] = k < il.n ? lq2[il.wj[k]] : make_float2(0.f, 0.f);
-            av[u] = k < il.n ? A[k] : make_float2(0.f, 0.f);
-        }
         float f[8];
+        if (valid) {
+            float2 lv[8], av[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int k = g + u;
-            f[u] = k < il.n ? flux32_row(tr, lv[u], av[u], pc.C2[k]) : 0.0f;
+            for (int u = 0; u < 8; ++u) {
+                const int k = g + u;
+                lv[u] = k < il.n ? lq2[il.wj[k]] : make_float2(0.f, 0.f);
+                av[u] = k < il.n ? A[k] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int k = g + u;
+                f[u] = k < il.n ? flux32_row(tr, lv[u], av[u], pc.C2[k]) : 0.0f;
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) f[u] = 0.0f;
         }
+        if (rounds > 0) {
+            // the group's lowest lane adds its peers' fluxes, in lane order
+            unsigned rest = lead ? (peers & (peers - 1u)) : 0u;
+            for (int r = 0; r < rounds; ++r) {
+                const int src = rest ? __ffs(rest) - 1 : lane;
+                rest &= rest - 1u;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const float v = __shfl_sync(0xffffffffu, f[u], src);
+                    if (src != lane) f[u] += v;
+                }
+            }
+        }
+        if (!lead) continue;
 #pragma unroll
         for (int h = 0; h < 8; h += 4)
             if (g + h < il.n && (f[h] != 0.0f || f[h + 1] != 0.0f || f[h + 2] != 0.0f || f[h + 3] != 0.0f))
