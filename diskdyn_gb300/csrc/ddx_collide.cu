@@ -3,7 +3,8 @@
 // (xj-xi)^2 + (yj-yi)^2 + (zj-zi)^2 < h^2, every operation rounded on its own (no FMA
 // contraction), so the result is identical to a CPU brute force with the same expression.
 //
-//  1. keys    : cell = floor(x / cs) per axis with cs = 2h (1 + 1e-9), clamped to
+//  1. keys    : cell = floor(x / cs) per axis with cs = 2h (1 + 1e-9) (decided in FP32
+//               where that is certain, in FP64 near a cell edge), clamped to
 //               +-(2^19 - 2) (clamping only merges far cells), and the half of the cell the
 //               tracer lies in; the cell is hashed (the 32-bit finaliser of MurmurHash3 over
 //               a linear form lin of the three 20-bit coordinates) into T = 2^k >= 2n buckets,
@@ -26,7 +27,8 @@
 //               Most neighbour cells are empty, and their bucket is then empty or holds one
 //               or two tracers of other cells: the 8 bucket entries, loaded together, settle
 //               those without touching the tracers (a lin that differs means another cell),
-//               and only the rest are walked.  A test in FP32 with a proven margin rejects
+//               and only the rest are walked, shared out over the warp's lanes (a queue of
+//               (tracer, cell) items per warp).  A test in FP32 with a proven margin rejects
 //               the far candidates first; the FP64 test decides the rest (FP64 runs at 1/64
 //               of the FP32 rate here, and a warp pays for it whenever any of its lanes
 //               tests);
@@ -89,8 +91,10 @@ __device__ __forceinline__ unsigned long long neighbour_id(unsigned long long id
 // wide, the rounding of x / cs (below 1e-9 of a cell for |cell| < 2^19) cannot put a partner
 // within h outside these cells.  The conversion saturates for huge or infinite x (clamped)
 // and gives 0 for NaN, whose distance tests fail.
-__device__ __forceinline__ uint32_t axis_cell(double x, double inv2, uint32_t& upper) {
-    const long long k = __double2ll_rd(x * inv2);
+__device__ __forceinline__ float f32_trunc(double x);
+__device__ __forceinline__ long long half_cell(double x, double inv2, float inv2f);
+__device__ __forceinline__ uint32_t axis_cell(double x, double inv2, float inv2f, uint32_t& upper) {
+    const long long k = half_cell(x, inv2, inv2f);
     long long c = k >> 1;
     upper = (uint32_t)(k & 1);
     if (c < -kCellLim) c = -kCellLim;
@@ -119,7 +123,24 @@ __device__ __forceinline__ float f32_trunc(double x) {
     return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | ((uint32_t)(b >> 29) & 0x7FFFFFu));
 }
 
-__global__ void keys_kernel(ddx_state s, int i0, int n, double inv2, uint32_t mask, uint32_t sentinel,
+// floor(x * inv2) with the product rounded to FP64, as __double2ll_rd(x * inv2) gives it, from
+// FP32 arithmetic where that is certain.  pf = trunc32(x) * RN32(inv2), rounded, is within
+// (2^-23 + 2^-24 + 2^-24 + 2^-53)|x inv2| < 2^-21.9 |pf| of the FP64 product, so when the
+// interval pf +- m, m = 2^-21 |pf| + 2^-100 (the absolute term covers float underflow and the
+// sign of a tiny product), rounded (each end moves by at most half an ulp of pf, 2^-24 |pf|),
+// lies inside one integer step, its floor is the FP64 product's.  Near an integer, beyond
+// +-2^21 (where the cell clamps anyway), and for inf, NaN or an infinite inv2f the FP64 form
+// decides.  On the dusty ring (about 1,300 half-cells from the star) about one axis in 800 is
+// near an integer, so the FP64 pipe, 1/64 of the FP32 rate on this part, is almost idle.
+__device__ __forceinline__ long long half_cell(double x, double inv2, float inv2f) {
+    const float pf = __fmul_rn(f32_trunc(x), inv2f);
+    const float m = __fmaf_rn(fabsf(pf), 0x1p-21f, 0x1p-100f);
+    const int lo = __float2int_rd(__fsub_rn(pf, m)), hi = __float2int_rd(__fadd_rn(pf, m));
+    if (lo == hi && fabsf(pf) < 0x1p21f) return lo;
+    return __double2ll_rd(x * inv2);
+}
+
+__global__ void keys_kernel(ddx_state s, int i0, int n, double inv2, float inv2f, uint32_t mask, uint32_t sentinel,
                             uint32_t* __restrict__ bsize, uint32_t* __restrict__ bucket, uint32_t* __restrict__ rank,
                             unsigned long long* __restrict__ cellid, uint32_t* __restrict__ count) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -132,9 +153,9 @@ __global__ void keys_kernel(ddx_state s, int i0, int n, double inv2, uint32_t ma
         return;
     }
     uint32_t hx, hy, hz;
-    const uint32_t ux = axis_cell(s.x[idx], inv2, hx);
-    const uint32_t uy = axis_cell(s.y[idx], inv2, hy);
-    const uint32_t uz = axis_cell(s.z[idx], inv2, hz);
+    const uint32_t ux = axis_cell(s.x[idx], inv2, inv2f, hx);
+    const uint32_t uy = axis_cell(s.y[idx], inv2, inv2f, hy);
+    const uint32_t uz = axis_cell(s.z[idx], inv2, inv2f, hz);
     const uint32_t b = bucket_of(cell_lin(ux, uy, uz), mask);
     cellid[p] = pack_u(ux, uy, uz) | ((unsigned long long)(hx << 2 | hy << 1 | hz) << 60);
     bucket[p] = b;
@@ -186,30 +207,29 @@ __device__ __forceinline__ void keep_smallest(int2* seg, uint32_t& filled, uint3
     seg[b] = make_int2(i, j);
 }
 
-// hf: h as a float, rounded up.
-template <bool WRITE>
-__global__ void pairs_kernel(const CellRec* __restrict__ rec, const uint32_t* __restrict__ vals,
+// The write pass: every tracer with partners writes them, ordered by j, to its segment of
+// the list (offs: the scan of the counts), cut at cap.  The partners kept by the count pass
+// are copied; a tracer with more than kSlots walks its octant again.  hf: h as a float,
+// rounded up.
+__global__ void write_kernel(const CellRec* __restrict__ rec, const uint32_t* __restrict__ vals,
                              const uint4* __restrict__ table, const uint32_t* __restrict__ n_live, int i0,
-                             double h2, float hf, uint32_t mask, uint32_t* __restrict__ count,
-                             int* __restrict__ slots, const uint32_t* __restrict__ offs, int2* __restrict__ pairs,
-                             long long cap) {
+                             double h2, float hf, uint32_t mask, const uint32_t* __restrict__ count,
+                             const int* __restrict__ slots, const uint32_t* __restrict__ offs,
+                             int2* __restrict__ pairs, long long cap) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;   // bucket order
     if (q >= *n_live) return;
     const uint32_t p = vals[q];
     const int i = i0 + (int)p;
-    int2* seg = nullptr;
-    uint32_t k = 0, filled = 0;
-    if (WRITE) {
-        const uint32_t cnt = count[p];
-        const long long base = offs[p];
-        if (cnt == 0 || base >= cap) return;
-        k = (long long)cnt < cap - base ? cnt : (uint32_t)(cap - base);
-        seg = pairs + base;
-        if (cnt <= kSlots) {
-            // the count pass kept all of this tracer's partners: no second walk
-            for (uint32_t u = 0; u < cnt; ++u) keep_smallest(seg, filled, k, i, slots[(size_t)p * kSlots + u]);
-            return;
-        }
+    const uint32_t cnt = count[p];
+    const long long base = offs[p];
+    if (cnt == 0 || base >= cap) return;
+    const uint32_t k = (long long)cnt < cap - base ? cnt : (uint32_t)(cap - base);
+    int2* seg = pairs + base;
+    uint32_t filled = 0;
+    if (cnt <= kSlots) {
+        // the count pass kept all of this tracer's partners: no second walk
+        for (uint32_t u = 0; u < cnt; ++u) keep_smallest(seg, filled, k, i, slots[(size_t)p * kSlots + u]);
+        return;
     }
     const CellRec me = rec[q];
     const double xi = me.x, yi = me.y, zi = me.z;
@@ -232,7 +252,6 @@ __global__ void pairs_kernel(const CellRec* __restrict__ rec, const uint32_t* __
     const bool filter = M + hf < 1e15f && hf > 1e-12f;   // false for NaN
     const float reach = hf + (M + hf) * 0x1p-18f;
     const float thr = reach * reach * (1.0f + 0x1p-16f);
-    uint32_t c = 0;
     // entries of bucket bk that lie in cell nid: j > i within h
     auto walk = [&](unsigned long long nid, uint4 bk) {
         for (uint32_t r = bk.x; r < bk.x + bk.y; ++r) {
@@ -249,12 +268,7 @@ __global__ void pairs_kernel(const CellRec* __restrict__ rec, const uint32_t* __
             const double ey = __dsub_rn(o.y, yi);
             const double ez = __dsub_rn(o.z, zi);
             const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez));
-            if (d2 < h2) {
-                const int j = i0 + (int)pj;
-                if (WRITE) keep_smallest(seg, filled, k, i, j);
-                if (!WRITE && c < kSlots) slots[(size_t)p * kSlots + c] = j;
-                ++c;
-            }
+            if (d2 < h2) keep_smallest(seg, filled, k, i, i0 + (int)pj);
         }
     };
     if (hx - lx == 1 && hy - ly == 1 && hz - lz == 1) {
@@ -285,7 +299,159 @@ __global__ void pairs_kernel(const CellRec* __restrict__ rec, const uint32_t* __
                 for (int dz = lz; dz <= hz; ++dz)
                     walk(neighbour_id(id0, dx, dy, dz), table[bucket_of(neighbour_lin(lin0, dx, dy, dz), mask)]);
     }
-    if (!WRITE) count[p] = c;
+}
+
+// The count pass with the walks shared out over the warp.  Each tracer settles its octant's 8
+// bucket entries as in write_kernel; the buckets left to walk go into a per-warp queue of
+// (lane, cell) items, and the warp then walks 32 items at a time, each lane on one item with
+// the owner's position and cell taken by shuffles, so the walks of one tracer no longer hold
+// the other 31 lanes (about 0.45 walks per tracer on the dusty ring, up to eight on one lane).
+// Partners are counted per owner in shared memory, and the first kSlots found are kept in the
+// order the items run (the write pass sorts them).  A tracer on a clamped axis (more than 8
+// cells) walks on its own lane.
+constexpr int kCountThreads = 256;
+
+__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(kCountThreads, 4) count_kernel(const CellRec* __restrict__ rec,
+                                                              const uint32_t* __restrict__ vals,
+                                                              const uint4* __restrict__ table,
+                                                              const uint32_t* __restrict__ n_live, int i0, double h2,
+                                                              float hf, uint32_t mask, uint32_t* __restrict__ count,
+                                                              int* __restrict__ slots) {
+    __shared__ uint8_t queue[kCountThreads / 32][256];
+    __shared__ uint32_t found[kCountThreads];
+    const uint32_t FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t q0 = blockIdx.x * blockDim.x + warp * 32;   // the warp's first slot
+    const uint32_t q = q0 + lane;
+    const uint32_t nl = *n_live;
+    if (q0 >= nl) return;   // the whole warp: nothing to do
+    const bool live = q < nl;
+    uint32_t p = 0, linl = 0, need = 0, own_cnt = 0;
+    unsigned long long idl = 0;
+    double xi = 0.0, yi = 0.0, zi = 0.0;
+    float fxi = 0.f, fyi = 0.f, fzi = 0.f, thr = 0.f;
+    found[threadIdx.x] = 0;
+    if (live) {
+        p = vals[q];
+        const CellRec me = rec[q];
+        xi = me.x;
+        yi = me.y;
+        zi = me.z;
+        const unsigned long long id0 = me.cell & kIdMask;
+        const uint32_t ux = (uint32_t)(id0 >> 40) & 0xFFFFFu, uy = (uint32_t)(id0 >> 20) & 0xFFFFFu,
+                       uz = (uint32_t)id0 & 0xFFFFFu;
+        int lx, hx, ly, hy, lz, hz;
+        axis_walk(ux, (uint32_t)(me.cell >> 62) & 1u, lx, hx);
+        axis_walk(uy, (uint32_t)(me.cell >> 61) & 1u, ly, hy);
+        axis_walk(uz, (uint32_t)(me.cell >> 60) & 1u, lz, hz);
+        const uint32_t lin0 = cell_lin(ux, uy, uz);
+        // FP32 rejection threshold as in write_kernel; +inf where the filter does not apply,
+        // so that every candidate takes the FP64 test there
+        fxi = f32_trunc(xi);
+        fyi = f32_trunc(yi);
+        fzi = f32_trunc(zi);
+        const float M = fmaxf(fabsf(fxi), fmaxf(fabsf(fyi), fabsf(fzi)));
+        const float reach = hf + (M + hf) * 0x1p-18f;
+        thr = (M + hf < 1e15f && hf > 1e-12f) ? reach * reach * (1.0f + 0x1p-16f) : INFINITY;
+        if (hx - lx == 1 && hy - ly == 1 && hz - lz == 1) {
+            idl = neighbour_id(id0, lx, ly, lz);
+            linl = neighbour_lin(lin0, lx, ly, lz);
+            const int own = (lx ? 4 : 0) | (ly ? 2 : 0) | (lz ? 1 : 0);
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const uint32_t nlin = neighbour_lin(linl, t >> 2, (t >> 1) & 1, t & 1);
+                const uint4 e = table[bucket_of(nlin, mask)];
+                const bool self0 = t == own && e.x == q, self1 = t == own && e.x + 1 == q;
+                const bool hit =
+                    (e.y >= 1 && e.z == nlin && !self0) || (e.y >= 2 && e.w == nlin && !self1) || e.y >= 3;
+                if (hit) need |= 1u << t;
+            }
+        } else {
+            // a clamped axis: up to 27 cells, walked here
+            for (int dx = lx; dx <= hx; ++dx)
+                for (int dy = ly; dy <= hy; ++dy)
+                    for (int dz = lz; dz <= hz; ++dz) {
+                        const unsigned long long nid = neighbour_id(id0, dx, dy, dz);
+                        const uint4 bk = table[bucket_of(neighbour_lin(lin0, dx, dy, dz), mask)];
+                        for (uint32_t r = bk.x; r < bk.x + bk.y; ++r) {
+                            if (r == q) continue;
+                            const CellRec o = rec[r];
+                            if ((o.cell & kIdMask) != nid) continue;
+                            const float ex = f32_trunc(o.x) - fxi, ey = f32_trunc(o.y) - fyi,
+                                        ez = f32_trunc(o.z) - fzi;
+                            if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > thr) continue;
+                            const uint32_t pj = vals[r];
+                            if (pj <= p) continue;
+                            const double dx_ = __dsub_rn(o.x, xi), dy_ = __dsub_rn(o.y, yi), dz_ = __dsub_rn(o.z, zi);
+                            const double d2 =
+                                __dadd_rn(__dadd_rn(__dmul_rn(dx_, dx_), __dmul_rn(dy_, dy_)), __dmul_rn(dz_, dz_));
+                            if (d2 < h2) {
+                                if (own_cnt < kSlots) slots[(size_t)p * kSlots + own_cnt] = i0 + (int)pj;
+                                ++own_cnt;
+                            }
+                        }
+                    }
+        }
+    }
+    // the warp's queue of (lane, cell) items
+    const uint32_t nit = __popc(need);
+    const uint32_t inc = warp_incl_sum(nit);
+    const uint32_t total = __shfl_sync(FULL, inc, 31);
+    {
+        uint32_t pos = inc - nit, m = need;
+        while (m) {
+            const int t = __ffs(m) - 1;
+            m &= m - 1;
+            queue[warp][pos++] = (uint8_t)(lane << 3 | t);
+        }
+    }
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t g = base + lane;
+        const uint32_t item = g < total ? queue[warp][g] : (uint32_t)(lane << 3);
+        const int o = (int)(item >> 3), t = (int)(item & 7);
+        const double oxi = __shfl_sync(FULL, xi, o), oyi = __shfl_sync(FULL, yi, o), ozi = __shfl_sync(FULL, zi, o);
+        const float ofx = __shfl_sync(FULL, fxi, o), ofy = __shfl_sync(FULL, fyi, o), ofz = __shfl_sync(FULL, fzi, o);
+        const float othr = __shfl_sync(FULL, thr, o);
+        const uint32_t op = __shfl_sync(FULL, p, o), olinl = __shfl_sync(FULL, linl, o);
+        const unsigned long long oidl = __shfl_sync(FULL, idl, o);
+        if (g >= total) continue;
+        const int dx = t >> 2, dy = (t >> 1) & 1, dz = t & 1;
+        const unsigned long long nid = neighbour_id(oidl, dx, dy, dz);
+        const uint4 bk = table[bucket_of(neighbour_lin(olinl, dx, dy, dz), mask)];
+        const uint32_t oq = q0 + (uint32_t)o;
+        for (uint32_t r = bk.x; r < bk.x + bk.y; ++r) {
+            if (r == oq) continue;
+            const CellRec c = rec[r];
+            if ((c.cell & kIdMask) != nid) continue;
+            const float ex = f32_trunc(c.x) - ofx, ey = f32_trunc(c.y) - ofy, ez = f32_trunc(c.z) - ofz;
+            if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > othr) continue;
+            const uint32_t pj = vals[r];
+            if (pj <= op) continue;
+            const double dx_ = __dsub_rn(c.x, oxi), dy_ = __dsub_rn(c.y, oyi), dz_ = __dsub_rn(c.z, ozi);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx_, dx_), __dmul_rn(dy_, dy_)), __dmul_rn(dz_, dz_));
+            if (d2 < h2) {
+                const uint32_t k = atomicAdd(&found[warp * 32 + o], 1u);
+                if (k < kSlots) slots[(size_t)op * kSlots + k] = i0 + (int)pj;
+            }
+        }
+    }
+    __syncwarp();
+    if (live) {
+        // partners of a clamped-axis tracer were counted on its own lane (own_cnt), and it has
+        // no queue items, so the two counts never share slots
+        count[p] = found[threadIdx.x] + own_cnt;
+    }
 }
 
 }  // namespace
@@ -351,18 +517,17 @@ int collide_run(CollideScratch*& cs, const ddx_state& s, int i0, int i1, double 
     uint32_t* n_live = cs->total;
     uint32_t* n_found = cs->total + 1;
     cudaMemsetAsync(cs->bsize, 0, 4ull * T, st);
-    keys_kernel<<<blk, thr, 0, st>>>(s, i0, n, inv2, mask, sentinel, cs->bsize, cs->bucket, cs->rank, cs->cellid,
+    keys_kernel<<<blk, thr, 0, st>>>(s, i0, n, inv2, (float)inv2, mask, sentinel, cs->bsize, cs->bucket, cs->rank, cs->cellid,
                                      cs->count);
-    uint32_t* tw = reinterpret_cast<uint32_t*>(cs->table);   // entries {start, size, first cell}
-    if (exclusive_scan_strided(cs->bsize, 1, tw, 4, (int)T, cs->temp, n_live, st, tw + 1) != cudaSuccess)
-        return DDX_ERR_CUDA;
+    // entries {start, size, lin of the first two cells (written by the scatter)}
+    if (exclusive_scan_table(cs->bsize, cs->table, (int)T, cs->temp, n_live, st) != cudaSuccess) return DDX_ERR_CUDA;
     scatter_kernel<<<blk, thr, 0, st>>>(s, i0, n, sentinel, cs->bucket, cs->rank, cs->cellid, cs->table, cs->rec,
                                         cs->vals);
-    pairs_kernel<false><<<blk, thr, 0, st>>>(cs->rec, cs->vals, cs->table, n_live, i0, h2, hf, mask, cs->count,
-                                             cs->slots, nullptr, nullptr, 0);
+    count_kernel<<<(n + kCountThreads - 1) / kCountThreads, kCountThreads, 0, st>>>(
+        cs->rec, cs->vals, cs->table, n_live, i0, h2, hf, mask, cs->count, cs->slots);
     if (exclusive_scan(cs->count, cs->offs, n, cs->temp, n_found, st) != cudaSuccess) return DDX_ERR_CUDA;
     if (pairs && cap > 0)
-        pairs_kernel<true><<<blk, thr, 0, st>>>(cs->rec, cs->vals, cs->table, n_live, i0, h2, hf, mask, cs->count,
+        write_kernel<<<blk, thr, 0, st>>>(cs->rec, cs->vals, cs->table, n_live, i0, h2, hf, mask, cs->count,
                                                 cs->slots, cs->offs, pairs, cap);
     if (cudaGetLastError() != cudaSuccess) return DDX_ERR_CUDA;
     uint32_t tot = 0;

@@ -5,17 +5,17 @@
 
 namespace ddx {
 
-// 32-bit words of temporary storage exclusive_scan needs for n items.
+// 32-bit words of temporary storage the scans need for n items.
 size_t scan_temp_words(int n);
 
-// out[i] = sum of in[0..i-1]; *total (device, optional) = sum of all.  in == out allowed.
+// out[i] = sum of in[0..i-1]; *total (device, optional) = sum of all.  in and out must not
+// overlap.
 cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, int n, uint32_t* temp, uint32_t* total,
                            cudaStream_t st);
 
-// The same over strided arrays: element k is in[k * is] and out[k * os]; with copy, also
-// copy[k * os] = in[k * is] (out and copy may be two fields of an array of structs, which then
-// holds {start, size} pairs).
-cudaError_t exclusive_scan_strided(const uint32_t* in, int is, uint32_t* out, int os, int n, uint32_t* temp,
-                                   uint32_t* total, cudaStream_t st, uint32_t* copy);
+// The same, written as 16-byte entries table[i] = {start, size = in[i], 0, 0} (a bucket
+// table: the last two words are free for the caller).
+cudaError_t exclusive_scan_table(const uint32_t* in, uint4* table, int n, uint32_t* temp, uint32_t* total,
+                                 cudaStream_t st);
 
 }  // namespace ddx
