@@ -716,348 +716,6 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
     s.vx[t] = vx; s.vy[t] = vy; s.vz[t] = vz;
 }
 
-// ---- two tracers per thread ----------------------------------------------------------
-// The same step with each thread carrying two tracers adjacent in the visiting order: every
-// pair record read from shared memory serves both, which halves the shared-memory loads per
-// interaction and gives each thread two independent rsqrt/FMA chains.  Each tracer makes
-// its own far/near choice per span (so results are those of the one-tracer kernel to the
-// bit); a span where the two choose differently runs each tracer's own form.  Two blocks of
-// 256 threads per SM (up to 128 registers).
-constexpr int kThreads2 = 256;
-
-// One tracer over one span of kPairSpan pair records, in the far form (high parts alone) or
-// the near form (hi/lo separation, largest reciprocal distance kept in mx).
-template <bool FAR>
-__device__ __forceinline__ void span1(const BodyPair* R, f2 XH, f2 YH, f2 ZH, f2 XL, f2 YL, f2 ZL, f2& px, f2& py,
-                                      f2& pz, float& mx) {
-#pragma unroll 4
-    for (int u = 0; u < kPairSpan; ++u) {
-        const BodyPair* r = R + u;
-        const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);
-        const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);
-        f2 dX, dY, dZ;
-        if (FAR) {
-            dX = sub2(q0.x, XH); dY = sub2(q0.y, YH); dZ = sub2(q1.x, ZH);
-        } else {
-            const ulonglong2 q2 = *reinterpret_cast<const ulonglong2*>(r->lx);
-            const f2 lz = *reinterpret_cast<const f2*>(r->lz);
-            dX = add2(sub2(q0.x, XH), sub2(q2.x, XL));
-            dY = add2(sub2(q0.y, YH), sub2(q2.y, YL));
-            dZ = add2(sub2(q1.x, ZH), sub2(lz, ZL));
-        }
-        const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
-        float r0, r1;
-        f2_split(RR, r0, r1);
-        const float i0 = rsqrt_approx(r0), i1 = rsqrt_approx(r1);
-        if (!FAR) mx = fmax3(mx, i0, i1);
-        const f2 ri = f2_join(i0, i1);
-        const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
-        px = fma2(f, dX, px); py = fma2(f, dY, py); pz = fma2(f, dZ, pz);
-    }
-}
-
-// One span of kPairSpan pair records for both tracers of a thread, both in the same form.
-template <bool FAR>
-__device__ __forceinline__ void span2(const BodyPair* R, const f2 (&XH)[2], const f2 (&XL)[2], const f2 (&YH)[2],
-                                      const f2 (&YL)[2], const f2 (&ZH)[2], const f2 (&ZL)[2], f2 (&px)[2],
-                                      f2 (&py)[2], f2 (&pz)[2], float (&mx)[2]) {
-#pragma unroll
-    for (int u = 0; u < kPairSpan; ++u) {
-        const BodyPair* r = R + u;
-        const ulonglong2 q0 = *reinterpret_cast<const ulonglong2*>(r->hx);  // hx, hy
-        const ulonglong2 q1 = *reinterpret_cast<const ulonglong2*>(r->hz);  // hz, m
-        ulonglong2 q2;
-        f2 lz = 0;
-        if (!FAR) {
-            q2 = *reinterpret_cast<const ulonglong2*>(r->lx);                // lx, ly
-            lz = *reinterpret_cast<const f2*>(r->lz);
-        }
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            f2 dX, dY, dZ;
-            if (FAR) {
-                dX = sub2(q0.x, XH[q]); dY = sub2(q0.y, YH[q]); dZ = sub2(q1.x, ZH[q]);
-            } else {
-                dX = add2(sub2(q0.x, XH[q]), sub2(q2.x, XL[q]));
-                dY = add2(sub2(q0.y, YH[q]), sub2(q2.y, YL[q]));
-                dZ = add2(sub2(q1.x, ZH[q]), sub2(lz, ZL[q]));
-            }
-            const f2 RR = fma2(dX, dX, fma2(dY, dY, mul2(dZ, dZ)));
-            float r0, r1;
-            f2_split(RR, r0, r1);
-            const float i0 = rsqrt_approx(r0), i1 = rsqrt_approx(r1);
-            if (!FAR) mx[q] = fmax3(mx[q], i0, i1);
-            const f2 ri = f2_join(i0, i1);
-            const f2 f = mul2(mul2(q1.y, ri), mul2(ri, ri));
-            px[q] = fma2(f, dX, px[q]); py[q] = fma2(f, dY, py[q]); pz[q] = fma2(f, dZ, pz[q]);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kThreads2, 2)
-dust_rk4_mixed2_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins,
-                       const int* __restrict__ perm, bool boxes, const int* __restrict__ src) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) unsigned long long mbar[2];
-    __shared__ float bred[kThreads2 / 32][7];
-    __shared__ float bbox[7];
-    __shared__ uint32_t allfar[kFlagSpans / 32], allnear[kFlagSpans / 32];
-    BodyPair* const tiles = reinterpret_cast<BodyPair*>(smem);
-    const int tid = threadIdx.x;
-    const int ng = a.n_grav;
-    int ti[2];
-    bool alive[2];
-    double x[2], y[2], z[2], vx[2], vy[2], vz[2], m[2];
-    float bet[2], betsw[2], qe[2];
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int slot = 2 * (blockIdx.x * kThreads2 + tid) + q;   // position in the visiting order
-        const int i = perm && slot < a.n_dust ? perm[slot] : slot;
-        ti[q] = i;
-        alive[q] = false;
-        x[q] = y[q] = z[q] = vx[q] = vy[q] = vz[q] = 0.0;
-        m[q] = 1.0;
-        bet[q] = betsw[q] = qe[q] = 0.f;
-        if (i < a.n_dust) {
-            const int t = ng + i;
-            alive[q] = s.N[t] != 0.0;
-            if (alive[q]) {
-                x[q] = s.x[t]; y[q] = s.y[t]; z[q] = s.z[t];
-                vx[q] = s.vx[t]; vy[q] = s.vy[t]; vz[q] = s.vz[t];
-                m[q] = s.m[t];
-                const int id = s.id[t];
-                if (id >= 0 && id < a.n_grid) {
-                    const SizeBin b = bins[id];
-                    bet[q] = b.beta; betsw[q] = b.betasw; qe[q] = b.q;
-                }
-            }
-        }
-    }
-
-    const int npairs = pair_count(ng - a.n_exact);
-    const int ntiles = (npairs + kTilePairs - 1) / kTilePairs;
-    const int G = 4 * ntiles;
-    const uint32_t mb[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
-    if (tid == 0) {
-        mbar_init(mb[0], 1);
-        mbar_init(mb[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    int in_flight[2] = {-1, -1};
-    auto issue = [&](int g) {
-        if (g == a.lose_tile) return;
-        const int stg = g / ntiles, first = (g - stg * ntiles) * kTilePairs;
-        const unsigned bytes = (unsigned)(min(kTilePairs, npairs - first) * sizeof(BodyPair));
-        mbar_expect_tx(mb[g & 1], bytes);
-        bulk_load(smem_u32(tiles + (g & 1) * kTilePairs), ms.PP + (size_t)stg * ms.pcap + first, bytes,
-                  mb[g & 1]);
-        in_flight[g & 1] = g;
-    };
-    if (tid == 0 && G > 0) issue(0);
-
-    const double dt = a.dt, dt2 = a.dt / 2.0, dt6 = a.dt / 6.0;
-    double rpx[2], rpy[2], rpz[2], kpx[2], kpy[2], kpz[2], Ax[2], Ay[2], Az[2], Bx[2], By[2], Bz[2];
-    int removed[2] = {0, 0}, removed_stage[2] = {-1, -1};
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        rpx[q] = vx[q]; rpy[q] = vy[q]; rpz[q] = vz[q];
-        kpx[q] = kpy[q] = kpz[q] = 0.0;
-        Ax[q] = Ay[q] = Az[q] = Bx[q] = By[q] = Bz[q] = 0.0;
-    }
-    int lost = 0;
-    int g = 0;
-
-#pragma unroll 1
-    for (int st = 0; st < 4; ++st) {
-        const double w = (st == 1 || st == 2) ? 2.0 : 1.0;
-        double kx[2], ky[2], kz[2];
-        f2 XH[2], XL[2], YH[2], YL[2], ZH[2], ZL[2];
-        float xh[2], yh[2], zh[2], own[2], inv_near[2], xr[2], yr[2], zr[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            double xt = x[q], yt = y[q], zt = z[q], rx = vx[q], ry = vy[q], rz = vz[q];
-            if (st > 0) {
-                const double c = st == 3 ? dt : dt2;
-                xt = x[q] + rpx[q] * c; yt = y[q] + rpy[q] * c; zt = z[q] + rpz[q] * c;
-                rx = vx[q] + kpx[q] * c; ry = vy[q] + kpy[q] * c; rz = vz[q] + kpz[q] * c;
-            }
-            Ax[q] += w * rx; Ay[q] += w * ry; Az[q] += w * rz;
-            rpx[q] = rx; rpy[q] = ry; rpz[q] = rz;
-            kx[q] = ky[q] = kz[q] = 0.0;
-            if (alive[q]) {
-                const Body ps = ms.P[st * ms.cap + 0];
-                if (!star_term(xt - ps.x, yt - ps.y, zt - ps.z, rx, ry, rz, ps.m, bet[q], betsw[q], qe[q], m[q], a,
-                               kx[q], ky[q], kz[q])) {
-                    alive[q] = false; removed[q] = 1; removed_stage[q] = st;
-                }
-            }
-            for (int j = 1; alive[q] && j < a.n_exact; ++j) {
-                const Body p = ms.P[st * ms.cap + j];
-                const double ex = p.x - xt, ey = p.y - yt, ez = p.z - zt;
-                const double RR = ex * ex + ey * ey + ez * ez;
-                if (RR == 0.0) { alive[q] = false; removed[q] = 2; removed_stage[q] = st; break; }
-                const double ri = rsqrt(RR);
-                const double f = p.m * (ri * ri * ri);
-                kx[q] = fma(f, ex, kx[q]); ky[q] = fma(f, ey, ky[q]); kz[q] = fma(f, ez, kz[q]);
-            }
-            float xl, yl, zl;
-            split_hilo(xt, xh[q], xl); split_hilo(yt, yh[q], yl); split_hilo(zt, zh[q], zl);
-            xr[q] = rest3(xt, xh[q], xl); yr[q] = rest3(yt, yh[q], yl); zr[q] = rest3(zt, zh[q], zl);
-            XH[q] = f2_dup(xh[q]); XL[q] = f2_dup(xl); YH[q] = f2_dup(yh[q]); YL[q] = f2_dup(yl);
-            ZH[q] = f2_dup(zh[q]); ZL[q] = f2_dup(zl);
-            own[q] = fmaxf(fabsf(xh[q]), fmaxf(fabsf(yh[q]), fabsf(zh[q])));
-            inv_near[q] = near_inv(a.near_eta, own[q]);
-        }
-        const Body* const Pn = ms.P + (size_t)st * ms.cap + a.n_exact;
-        const int nspans = npairs / kPairSpan;
-        const bool flags = boxes && nspans <= kFlagSpans;
-        if (flags) {
-#pragma unroll
-            for (int qb = 0; qb < 7; ++qb) {
-                const bool mxq = (qb & 1) || qb == 6;
-                float wv = mxq ? -INFINITY : INFINITY;
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const float v[7] = {xh[q], xh[q], yh[q], yh[q], zh[q], zh[q], own[q]};
-                    if (alive[q]) wv = mxq ? fmaxf(wv, v[qb]) : fminf(wv, v[qb]);
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float u = __shfl_xor_sync(0xffffffffu, wv, o);
-                    wv = mxq ? fmaxf(wv, u) : fminf(wv, u);
-                }
-                if ((tid & 31) == 0) bred[tid >> 5][qb] = wv;
-            }
-            __syncthreads();
-            if (tid < 7) {
-                const bool mxq = (tid & 1) || tid == 6;
-                float wv = bred[0][tid];
-                for (int k = 1; k < kThreads2 / 32; ++k) wv = mxq ? fmaxf(wv, bred[k][tid]) : fminf(wv, bred[k][tid]);
-                bbox[tid] = tid == 6 ? fmaxf(wv, 0.f) : wv;
-            }
-            __syncthreads();
-            float b[7];
-#pragma unroll
-            for (int qb = 0; qb < 7; ++qb) b[qb] = bbox[qb];
-            const BodyPair* PPs = ms.PP + (size_t)st * ms.pcap;
-            for (int j0 = 0; j0 < nspans; j0 += kThreads2) {
-                const int j = j0 + tid;
-                bool f = false, nr = false;
-                if (j < nspans) {
-                    float2 bx, by, bz;
-                    float xm, dn, df;
-                    span_box(PPs + (size_t)j * kPairSpan, bx, by, bz, xm);
-                    block_far(bx, by, bz, xm, b, f, nr, dn, df);
-                }
-                const uint32_t wf = __ballot_sync(0xffffffffu, f), wn = __ballot_sync(0xffffffffu, nr);
-                if ((tid & 31) == 0 && j < nspans) { allfar[j >> 5] = wf; allnear[j >> 5] = wn; }
-            }
-            __syncthreads();
-        }
-        f2 Sx[2] = {0, 0}, Sy[2] = {0, 0}, Sz[2] = {0, 0}, Cx[2] = {0, 0}, Cy[2] = {0, 0}, Cz[2] = {0, 0};
-        for (int tt = 0; tt < ntiles; ++tt, ++g) {
-            lost = __syncthreads_or(lost);
-            if (lost) break;
-            if (tid == 0 && g + 1 < G) issue(g + 1);
-            if (!mbar_wait(mb[g & 1], (g >> 1) & 1, a.wait_ns)) { lost = 1; continue; }
-            if (tid == 0) in_flight[g & 1] = -1;
-            if (!alive[0] && !alive[1]) continue;
-            const BodyPair* T = tiles + (g & 1) * kTilePairs;
-            const int cnt = min(kTilePairs, npairs - tt * kTilePairs);
-            const uint32_t all = cnt / kPairSpan == 32 ? 0xFFFFFFFFu : (1u << (cnt / kPairSpan)) - 1u;
-            uint32_t fm[2] = {0u, 0u};
-            if (boxes) {
-                uint32_t open = all, af = 0u;
-                if (flags) {
-                    const int j0 = tt * (kTilePairs / kPairSpan);
-                    af = span_bits(allfar, j0, cnt / kPairSpan);
-                    open = all & ~(af | span_bits(allnear, j0, cnt / kPairSpan));
-                }
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    fm[q] = af;
-                    uint32_t o = open;
-                    while (o) {
-                        const int j = __ffs(o) - 1;
-                        o &= o - 1;
-                        float2 bx, by, bz;
-                        float xm;
-                        span_box(T + j * kPairSpan, bx, by, bz, xm);
-                        if (lane_far(bx, by, bz, xm, xh[q], yh[q], zh[q], own[q])) fm[q] |= 1u << j;
-                    }
-                }
-            }
-            // a removed tracer takes the cheapest form; its sums are not used
-            if (!alive[0]) fm[0] = all;
-            if (!alive[1]) fm[1] = all;
-            for (int k = 0; k < cnt; k += kPairSpan) {
-                f2 px[2] = {0, 0}, py[2] = {0, 0}, pz[2] = {0, 0};
-                float mx[2] = {0.f, 0.f};
-                const int sb = k / kPairSpan;
-                const bool f0 = (fm[0] >> sb) & 1u, f1 = (fm[1] >> sb) & 1u;
-                if (f0 == f1) {
-                    if (f0) span2<true>(T + k, XH, XL, YH, YL, ZH, ZL, px, py, pz, mx);
-                    else span2<false>(T + k, XH, XL, YH, YL, ZH, ZL, px, py, pz, mx);
-                } else {
-                    // the two choose differently (rare with the tracers in cell order): each
-                    // tracer runs its own form over the span
-#pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const bool fq = (fm[q] >> sb) & 1u;
-                        if (fq) span1<true>(T + k, XH[q], YH[q], ZH[q], XL[q], YL[q], ZL[q], px[q], py[q], pz[q], mx[q]);
-                        else span1<false>(T + k, XH[q], YH[q], ZH[q], XL[q], YL[q], ZL[q], px[q], py[q], pz[q], mx[q]);
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    if (mx[q] > inv_near[q])   // rare: a source of this span within tracer q's near radius
-                        near_span(T + k, 2 * (tt * kTilePairs + k), XH[q], XL[q], YH[q], YL[q], ZH[q], ZL[q], xr[q],
-                                  yr[q], zr[q], inv_near[q], Pn, src, px[q], py[q], pz[q], kx[q], ky[q], kz[q]);
-                    kahan2(Sx[q], Cx[q], px[q]); kahan2(Sy[q], Cy[q], py[q]); kahan2(Sz[q], Cz[q], pz[q]);
-                }
-            }
-        }
-        if (ntiles > 0) lost = __syncthreads_or(lost);
-        if (lost) break;
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            if (alive[q]) {
-                const double tx = f2_total(Sx[q], Cx[q]), ty = f2_total(Sy[q], Cy[q]), tz = f2_total(Sz[q], Cz[q]);
-                if (!(isfinite(tx) && isfinite(ty) && isfinite(tz))) {
-                    alive[q] = false; removed[q] = 2; removed_stage[q] = st;
-                }
-                kx[q] += tx; ky[q] += ty; kz[q] += tz;
-            }
-            Bx[q] += w * kx[q]; By[q] += w * ky[q]; Bz[q] += w * kz[q];
-            kpx[q] = kx[q]; kpy[q] = ky[q]; kpz[q] = kz[q];
-        }
-    }
-    lost = __syncthreads_or(lost);
-    if (lost) {
-        if (tid == 0) {
-            atomicOr(ms.status, kStatusTimeout);
-            for (int b = 0; b < 2; ++b)
-                if (in_flight[b] >= 0) mbar_wait(mb[b], (in_flight[b] >> 1) & 1, a.wait_ns);
-        }
-        return;
-    }
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int i = ti[q];
-        if (i >= a.n_dust) continue;
-        const int t = ng + i;
-        if (removed[q]) {
-            if (removed[q] == 1 && removed_stage[q] == 3 && a.mode == DDX_MODE_REFERENCE) s.N[i] = 0;
-            else s.N[t] = 0;
-            continue;
-        }
-        if (!alive[q]) continue;
-        s.x[t] = x[q] + dt6 * Ax[q]; s.y[t] = y[q] + dt6 * Ay[q]; s.z[t] = z[q] + dt6 * Az[q];
-        s.vx[t] = vx[q] + dt6 * Bx[q]; s.vy[t] = vy[q] + dt6 * By[q]; s.vz[t] = vz[q] + dt6 * Bz[q];
-    }
-}
-
 }  // namespace
 
 cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const MassiveScratch& ms,
@@ -1066,7 +724,6 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
     const bool comp = precision == DDX_PREC_COMPENSATED;
     const size_t smem = 2 * (size_t)kTilePairs * sizeof(BodyPair);
     static bool attr_set[128] = {};   // the attributes are set once per device
-    static int sms[128] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
@@ -1076,9 +733,6 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(dust_rk4_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(dust_rk4_mixed2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
@@ -1099,11 +753,7 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
     // the source of each pair slot, for the FP64 pulls of near sources: the sources sit in
     // cell order when the step ordered them (massive_prepare), else slot q holds source q
     const int* src = ms.slot && spatial_order_on(a) ? ms.src : nullptr;
-    // two tracers per thread once the grains fill two of its blocks on every SM
-    const int blocks2 = (a.n_dust + 2 * kThreads2 - 1) / (2 * kThreads2);
     if (comp) dust_rk4_mixed_kernel<true><<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes, src);
-    else if (blocks2 >= 2 * sms[dev])
-        dust_rk4_mixed2_kernel<<<blocks2, kThreads2, smem, st>>>(s, a, ms, bins, perm, boxes, src);
     else dust_rk4_mixed_kernel<false><<<blocks, threads, smem, st>>>(s, a, ms, bins, perm, boxes, src);
     return cudaGetLastError();
 }

@@ -128,11 +128,11 @@ def test_ordered_step_with_removed_non_finite_and_distant_tracers(engine, n_dust
 
 
 @pytest.mark.parametrize("n_plsml", [1100, 9000])
-def test_two_tracers_per_thread_identical_to_one(engine, n_plsml):
-    """From two blocks of 512 grains per SM on, the mixed step carries two tracers per thread
-    (adjacent in the visiting order).  A tracer's result depends only on its own state and
-    the massive set, so the first 20,000 grains of a 400,000-grain system step to the same
-    bits as those 20,000 grains alone, which take one tracer per thread."""
+def test_grains_step_alike_alone_and_among_many(engine, n_plsml):
+    """A tracer's result depends only on its own state and the massive set, not on the other
+    grains (which set the spatial visiting order, the blocks' span choices and the block
+    size): the first 20,000 grains of a 400,000-grain system step to the same bits as those
+    20,000 grains alone."""
     s = synth.dusty_ring(n_dust=400_000, n_plsml=n_plsml, seed=23, n_steps=2)
     ng = s.n_grav
     sub = {k: np.asarray(v)[:ng + 20000].copy() for k, v in s.state.items()}
