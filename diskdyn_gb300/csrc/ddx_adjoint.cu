@@ -923,6 +923,14 @@ __device__ __forceinline__ void flux_grad(double n, int id, int wj, const Tracer
     dFdc = scale * Ks * dPdc;
 }
 
+// Whether the bilinear footprint of a tracer (the four pixel centres around (u, w)) can touch
+// the frame: u in (-1, xsize) and w in (-1, ysize).  Outside it every weight on a frame
+// pixel is zero, and the pixel indices of a tracer far away (a grain thrown out to 1e15 AU
+// by a strong Lorentz force) would overflow int.  False for NaN.
+__device__ __forceinline__ bool in_reach(const TracerFlux& g, const ViewConst& v) {
+    return g.u > -1.0 && g.u < (double)v.xsize && g.w > -1.0 && g.w < (double)v.ysize;
+}
+
 __global__ void image_splat_kernel(const double* __restrict__ y, const double* __restrict__ N,
                                    const int* __restrict__ idv, int nd, const ViewConst* __restrict__ vcp,
                                    OpticsDev o, ImageList il, double* __restrict__ img) {
@@ -936,7 +944,7 @@ __global__ void image_splat_kernel(const double* __restrict__ y, const double* _
     if (id < 0 || id >= o.n_grid || n == 0.0) return;
     TracerFlux g;
     tracer_geometry(y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i], id, v, o, g);
-    if (!(g.R > o.Rmin)) return;
+    if (!(g.R > o.Rmin) || !in_reach(g, v)) return;
     const int i0 = (int)floor(g.u), j0 = (int)floor(g.w);
     const double fu = g.u - i0, fw = g.w - j0;
     const size_t npix = (size_t)v.xsize * v.ysize;
@@ -969,7 +977,7 @@ __global__ void image_splat_adjoint_kernel(const double* __restrict__ y, const d
     if (id < 0 || id >= o.n_grid || n == 0.0) return;
     TracerFlux g;
     tracer_geometry(y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i], id, v, o, g);
-    if (!(g.R > o.Rmin)) return;
+    if (!(g.R > o.Rmin) || !in_reach(g, v)) return;
     active[i] = 1;
     const double pos[3] = {y[i], y[(size_t)nd + i], y[2 * (size_t)nd + i]};
     const int i0 = (int)floor(g.u), j0 = (int)floor(g.w);

@@ -104,6 +104,15 @@ __device__ __forceinline__ void fast_pixel_coord(double x, double y, double z, c
     w = Y / v.psca;
 }
 
+// Whether a tracer is certainly off the frame: its fast pixel coordinates lie more than the
+// guard band g plus 2 pixels outside it (the reference sequence then lies outside too), or
+// beyond 2^30 pixels (where the reference's own int conversion of the floor overflows), or
+// are NaN.  Such a tracer adds nothing, and no int conversion of its coordinates is made.
+__device__ __forceinline__ bool far_off_frame(double u, double w, double g, const ViewConst& v) {
+    const double m = g + 2.0;
+    return !(u > -m && u < v.xsize + m && w > -m && w < v.ysize + m && fabs(u) < 0x1p30 && fabs(w) < 0x1p30);
+}
+
 // Scattering-angle cosine of a tracer at rotated position (x1, y1, z) for an observer at
 // distance dist along (0, -sin i, cos i), clamped like the reference
 // (src/gpu_functions.cu:1017-1023).
@@ -186,6 +195,7 @@ image_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ 
     int xim, yim;
     double cossc;
     const double g = guard_width(R, fmax(fabs(u), fabs(w)), v);
+    if (far_off_frame(u, w, g, v)) return;
     const bool exact = near_edge(u, g) || near_edge(w, g);
     if (exact) {
         exact_pixel(x, y, z, v, xim, yim, cossc);
@@ -232,6 +242,7 @@ __global__ void pixel_kernel(ddx_state s, int n_grav, int n_dust, const ViewCons
     fast_pixel_coord(x, y, z, v, u, w);
     int xim, yim;
     const double g = guard_width(R, fmax(fabs(u), fabs(w)), v);
+    if (far_off_frame(u, w, g, v)) return;
     if (near_edge(u, g) || near_edge(w, g)) {
         double cossc;
         exact_pixel(x, y, z, v, xim, yim, cossc);
@@ -474,6 +485,10 @@ __device__ __noinline__ void pixel_fp64(double x, double y, double z, const View
     double ud, wd;
     fast_pixel_coord(x, y, z, v, ud, wd);
     const double gd = guard_width(Rd, fmax(fabs(ud), fabs(wd)), v);
+    if (far_off_frame(ud, wd, gd, v)) {
+        xim = yim = -1;
+        return;
+    }
     if (near_edge(ud, gd) || near_edge(wd, gd)) {
         double cs;
         exact_pixel(x, y, z, v, xim, yim, cs);

@@ -169,11 +169,13 @@ def test_adjoint_with_planetesimals_and_lorentz_matches_torch_autograd():
     """A massive set of the star, two planets and 256 gravitating planetesimals (the
     launch-per-pass path), charged grains under the Lorentz force: the gradients of the loss
     in the planets' elements, in every planetesimal's state and mass and in every grain's
-    state agree with torch autograd of the same FP64 model on the CPU."""
+    state agree with torch autograd of the same FP64 model on the CPU.  The charges give the
+    smallest grains (m ~ 3e-43) a Lorentz acceleration of about a tenth of the star's pull at
+    100 AU (cL = q Bstar Rstar^3 / m ~ 0.15)."""
     n_steps, ckpt = 10, 4
     s = adj.adjoint_system(n_dust=128, xsize=64, ysize=64, n_steps=n_steps, seed=77, n_plsml=256)
     s.phys = dict(s.phys, FLQ=1, Bstar=5e-20, Wz=14.6)
-    s.size_table = dict(s.size_table, q=np.linspace(1e-3, 2e-3, len(s.size_table["q"])).astype(np.float32))
+    s.size_table = dict(s.size_table, q=np.linspace(1e-18, 2e-18, len(s.size_table["q"])).astype(np.float32))
     eng = Engine(0)
     eng.set_size_table(**s.size_table)
     o = s.optics
@@ -220,4 +222,45 @@ def test_adjoint_with_planetesimals_and_lorentz_matches_torch_autograd():
     for k in ("m", "a", "e", "i"):
         np.testing.assert_allclose(tg[k].grad.cpu().numpy(), tc[k].grad.numpy(), rtol=1e-7,
                                    atol=1e-9 * np.abs(tc[k].grad.numpy()).max(), err_msg=k)
+    eng.close()
+
+
+def test_tracers_far_off_the_frame_add_nothing_and_carry_no_gradient():
+    """Grains thrown far out (1e7 to 1e22 AU, beyond int pixel range) and a NaN grain: the
+    differentiable image equals the image without them, their gradient is zero, and the
+    binned ddx_image ignores them too."""
+    n_steps = 2
+    s, eng = setup(n_dust=256, n_steps=n_steps)
+    ng = s.n_grav
+    far = [1e7, -3e9, 2e12, -5e15, 7e18, -1e22]
+    for k, r in enumerate(far):
+        s.state["x"][ng + k] = r
+        s.state["y"][ng + k] = -0.7 * r
+    s.state["z"][ng + len(far)] = np.nan
+    n_bad = len(far) + 1
+    t = elements(s, "cuda")
+    d = dust_from(s, "cuda").requires_grad_(True)
+    L, img = gpu_loss(s, eng, t, d, 0.0, n_steps, 1)
+    L.backward()
+    assert torch.isfinite(img).all()
+    assert (d.grad[:n_bad] == 0).all() and torch.isfinite(d.grad).all()
+    # the same image with those grains removed (N = 0)
+    N_off = torch.tensor(s.state["N"][ng:], dtype=torch.float64, device="cuda")
+    N_off[:n_bad] = 0.0
+    ids = torch.tensor(s.state["id"][ng:], dtype=torch.int32, device="cuda")
+    with torch.no_grad():
+        img_off = adj.trajectory_image(eng, massive_from(t), d.detach(), N_off, ids, s.dt, n_steps, 1,
+                                       make_phys(**s.phys), make_view(**s.view), s.image_wj)
+    np.testing.assert_allclose(img.detach().cpu().numpy(), img_off.cpu().numpy(), rtol=1e-12,
+                               atol=1e-14 * img_off.abs().max().item())
+    # the binned image of the initial state skips them as well
+    from diskdyn_gb300.engine import DeviceState
+    Ns = dict(s.state)
+    Ns["N"] = s.state["N"].copy()
+    Ns["N"][ng:ng + n_bad] = 0.0
+    for prec, rtol in ((abi.DDX_PREC_FP64, 1e-12), (abi.DDX_PREC_MIXED, 1e-6)):
+        binned = eng.image(DeviceState.from_numpy(s.state), ng, make_view(**s.view), s.image_wj, precision=prec)
+        binned_off = eng.image(DeviceState.from_numpy(Ns), ng, make_view(**s.view), s.image_wj, precision=prec)
+        np.testing.assert_allclose(binned.cpu().numpy(), binned_off.cpu().numpy(), rtol=rtol,
+                                   atol=rtol * binned_off.abs().max().item())
     eng.close()
