@@ -450,13 +450,14 @@ View32 make_view32(const ddx_view& v, const OpticsDev& o) {
 }
 
 // FP64 -> FP32 by truncating the significand (error < 1 ulp of the float); values below
-// the FP32 normal range become zero.
+// the FP32 normal range become zero, values above it infinite, and NaN stays NaN (so that a
+// NaN tracer fails every range test downstream).
 __device__ __forceinline__ float d2f_trunc(double v) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
     const int e = (int)((b >> 52) & 0x7ff) - 1023;
     const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
     if (e < -126) return __uint_as_float(sign);
-    if (e > 127) return __uint_as_float(sign | 0x7f800000u);
+    if (e > 127) return __uint_as_float((b << 12) != 0ull && e == 1024 ? 0x7fc00000u : (sign | 0x7f800000u));
     return __uint_as_float(sign | ((unsigned int)(e + 127) << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
 }
 
@@ -523,7 +524,7 @@ __device__ __forceinline__ float scatter_cos32(float y1, float z, float R, float
     const float q = y1 * v.si - z * v.ci;
     const float ad = A * v.inv_d;
     float c = (ad + q) / (R * sqrtf(fmaf(ad, v.inv_d, fmaf(2.0f * q, v.inv_d, 1.0f))));
-    if (c < -1.0f) c = -1.0f;
+    if (!(c >= -1.0f)) c = -1.0f;   // NaN too (a tracer beyond the float range): the table index stays in range
     if (c >= v.cmax) c = v.cmax;
     return c;
 }
@@ -627,11 +628,11 @@ __global__ void photo_prepare_kernel(OpticsDev o, const ViewConst* __restrict__ 
 // to 4), in the wavelengths' scaled domain (2^esh), as 16-byte vector atomics: one request
 // adds four wavelengths of a tracer, a quarter of the requests of one FP64 atomic per
 // wavelength, and FP32 atomics do not issue through the FP64 pipe.
-// Warp aggregation: the lanes of a warp whose tracers land on the same pixel are grouped
-// (__match_any_sync on the pixel index); the lowest lane of a group adds the group's fluxes
-// (shuffles, in lane order) and issues one atomic for all of them.  A warp whose tracers all
-// fall on different pixels skips the shuffles.  The gain grows with the tracers per pixel a
-// warp sees, i.e. with how the tracers are ordered in the state.
+// Warp aggregation: adjacent lanes whose tracers land on the same pixel form a run; a
+// segmented tree sum (five shuffle steps) gives each run's first lane the run's fluxes, and
+// that lane issues one atomic for all of them.  A warp without such runs skips the shuffles.
+// The gain grows with the tracers per pixel that sit next to each other in the state (all
+// of them when the tracers are stored in pixel order).
 // image_convert_kernel then writes the FP64 x-major images.
 __global__ void __launch_bounds__(256)
 image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restrict__ vcp, View32 v32, OpticsDev o,
@@ -655,8 +656,13 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
             const float u = (x1 * v32.cp - y2 * v32.sp + v32.hx) * v32.inv_psca;
             const float w = (x1 * v32.sp + y2 * v32.cp + v32.hy) * v32.inv_psca;
             const float g = 64.0f * kEps32 * (R * v32.inv_psca + fmaxf(fabsf(u), fabsf(w)) + 1.0f);
-            int xim, yim;
-            if (near_edge32(u, g) || near_edge32(w, g)) {
+            // more than g + 2 pixels off the frame (or NaN): off the frame in FP64 and in the
+            // reference's sequence too, and no int conversion of the coordinates is made
+            const float mg = g + 2.0f;
+            const bool reach = u > -mg && u < (float)v32.xsize + mg && w > -mg && w < (float)v32.ysize + mg;
+            int xim = -1, yim = -1;
+            if (!reach) {
+            } else if (near_edge32(u, g) || near_edge32(w, g)) {
                 pixel_fp64(x, y, z, *vcp, xim, yim, counters);
             } else {
                 xim = (int)floorf(u);
@@ -671,12 +677,27 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
             }
         }
     }
-    // group the lanes by pixel (a lane without a pixel gets a key of its own)
+    // Runs of adjacent lanes on one pixel (a lane without a pixel gets a key of its own):
+    // the first lane of each run is its head.  A warp whose lanes all differ from their
+    // neighbours (tracers in no particular order) learns so from one shuffle and one ballot
+    // and goes straight to the atomics.
+    const unsigned FULL = 0xffffffffu;
     const unsigned long long key = valid ? (unsigned long long)pix : ~0ull - (unsigned long long)lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const bool lead = valid && (__ffs(peers) - 1 == lane);
-    const int rounds = __reduce_max_sync(0xffffffffu, valid ? __popc(peers) - 1 : 0);
-    if (!valid && rounds == 0) return;   // no shuffles in this warp: nothing left for this lane
+    const unsigned long long prev = __shfl_up_sync(FULL, key, 1);
+    const bool head = lane == 0 || prev != key;
+    const unsigned heads = __ballot_sync(FULL, head);
+    const bool runs = heads != FULL;
+    if (!valid && !runs) return;   // no shuffles in this warp: nothing left for this lane
+    // the segmented tree sum's steps: bit k set when lane + 2^k is in this lane's run
+    unsigned take = 0u;
+    if (runs) {
+        const unsigned seg = __popc(heads & (FULL >> (31 - lane)));   // runs begun at or below this lane
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const unsigned so = __shfl_down_sync(FULL, seg, 1 << k);
+            if (lane + (1 << k) < 32 && so == seg) take |= 1u << k;
+        }
+    }
     const float2* lq2 = valid ? o.lQp32p + ((size_t)tr.id * (o.n_theta - 1) + tr.cm) * o.n_wav : nullptr;
     const float2* A = valid ? pc.A + (size_t)tr.id * pc.n_lam : nullptr;
     float* row = Fi + pix * K4;
@@ -700,20 +721,20 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
 #pragma unroll
             for (int u = 0; u < 8; ++u) f[u] = 0.0f;
         }
-        if (rounds > 0) {
-            // the group's lowest lane adds its peers' fluxes, in lane order
-            unsigned rest = lead ? (peers & (peers - 1u)) : 0u;
-            for (int r = 0; r < rounds; ++r) {
-                const int src = rest ? __ffs(rest) - 1 : lane;
-                rest &= rest - 1u;
+        if (runs) {
+            // after step k each lane holds the sum of its run over lanes [lane, lane + 2^(k+1));
+            // the run being contiguous, its head ends with the whole run
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    const float v = __shfl_sync(0xffffffffu, f[u], src);
-                    if (src != lane) f[u] += v;
+                    if (g + u >= il.n) break;   // warp-uniform: no shuffles for the padding slots
+                    const float v = __shfl_down_sync(FULL, f[u], 1 << k);
+                    if ((take >> k) & 1u) f[u] += v;
                 }
             }
         }
-        if (!lead) continue;
+        if (!valid || !head) continue;
 #pragma unroll
         for (int h = 0; h < 8; h += 4)
             if (g + h < il.n && (f[h] != 0.0f || f[h + 1] != 0.0f || f[h + 2] != 0.0f || f[h + 3] != 0.0f))
