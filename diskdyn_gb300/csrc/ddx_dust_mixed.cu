@@ -66,7 +66,7 @@ namespace ddx {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTilePairs = 384;                 // pair records per tile (24 KiB)
+constexpr int kTilePairs = 256;                 // pair records per tile (16 KiB)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -393,12 +393,14 @@ __device__ __forceinline__ uint32_t span_bits(const uint32_t* w, int j0, int n) 
     return (uint32_t)(v >> r) & (n == 32 ? 0xFFFFFFFFu : (1u << n) - 1u);
 }
 
-// Four blocks per SM (64 registers, two 24 KiB tiles each): the FP64 values the compiler
+// Four blocks per SM (64 registers, two 16 KiB tiles each): the FP64 values the compiler
 // keeps in local memory are touched only between stages, and the kernel is held by the
 // latency of the broadcast shared-memory reads and of rsqrt.approx, which more warps hide.
 // Measured on the dusty ring (dust kernel): 3 blocks (80 registers, 32 KiB tiles) 8.50 ms,
 // 4 blocks 8.34 ms, 5 blocks (48 registers, 20 KiB tiles) 8.41 ms; two blocks without
-// spills were slower than three.
+// spills were slower than three.  With the near-source test in (8.64 ms at 24 KiB tiles),
+// smaller tiles leave more of the SM's 256 KiB to L1, where the spilled values live:
+// 8.55 ms at 12 KiB, 8.47 ms at 16 KiB, 8.53 ms at 20 KiB.
 // COMP: the compensated variant, two blocks per SM (its float-float pair needs more
 // registers than 64).
 template <bool COMP>
