@@ -61,7 +61,7 @@ def parse():
     p.add_argument("--workload", choices=["dusty_ring", "imaging", "scale", "solar", "setup", "cadence", "accuracy"],
                    default="dusty_ring")
     p.add_argument("--solar-steps", type=int, default=1000)
-    p.add_argument("--scale-err-steps", type=int, default=60)
+    p.add_argument("--scale-err-steps", type=int, default=500)
     p.add_argument("--adjoint-steps", type=int, default=2000)
     p.add_argument("--adjoint-plsml-steps", type=int, default=20)
     return p.parse_args()
@@ -602,8 +602,8 @@ def run_accuracy(args, world, rank, local):
         sweep.append({"eta": eta, "near_radius_at_130AU": eta * 130.0, "ms_per_step": ms,
                       "body_steps_per_s": (ng + full.n_dust) / (ms / 1e3), "error_vs_fp64": errs(m, ref, sng)})
     comp_sweep = []
-    for ceta, neta in ((0.25, 4e-3), (0.5, 4e-3), (0.5, 1.6e-2), (0.5, 3.2e-2), (1.0, 1.6e-2),
-                       (float("inf"), 1.6e-2)):
+    for ceta, neta in ((0.25, 4e-3), (0.25, 1.6e-2), (0.35, 1.6e-2), (0.5, 4e-3), (0.5, 1.6e-2), (0.5, 3.2e-2),
+                       (1.0, 1.6e-2), (float("inf"), 1.6e-2)):
         eng.set_size_table(**full.size_table)
         eng.set_compensated_radius(ceta)
         eng.set_near_radius(neta)
