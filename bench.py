@@ -1198,6 +1198,23 @@ def run_imaging(args, world, rank, local):
         tp.append(e[0].elapsed_time(e[1]))
     out["mixed"]["image_ms_tracers_in_pixel_order"] = statistics.mean(tp)
     out["mixed"]["pixel_order_image_rel_diff_max"] = float(((F - Fm).abs()[F64 != 0] / Fm[F64 != 0].abs()).max().item())
+    # and in a random order (seeded), where adjacent lanes almost never share a pixel
+    perm = torch.randperm(n, generator=torch.Generator(device="cuda").manual_seed(11), device="cuda")
+    for f in ("x", "y", "z", "vx", "vy", "vz", "m", "N", "id"):
+        a = getattr(st, f)
+        a[s.n_grav:] = a[s.n_grav:][perm]
+    for _ in range(args.warmup):
+        eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=abi.DDX_PREC_MIXED)
+    tr = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        e[0].record(stream)
+        eng.image(st, s.n_grav, view, s.image_wj, out=F, precision=abi.DDX_PREC_MIXED)
+        e[1].record(stream)
+        torch.cuda.synchronize()
+        tr.append(e[0].elapsed_time(e[1]))
+    out["mixed"]["image_ms_tracers_in_random_order"] = statistics.mean(tr)
     lit = F64 != 0
     out["mixed_vs_fp64"] = {
         "lit_pixels_identical": bool(torch.equal(lit, Fm != 0)),
