@@ -401,10 +401,10 @@ __device__ __forceinline__ uint32_t span_bits(const uint32_t* w, int j0, int n) 
 // spills were slower than three.  With the near-source test in (8.64 ms at 24 KiB tiles),
 // smaller tiles leave more of the SM's 256 KiB to L1, where the spilled values live:
 // 8.55 ms at 12 KiB, 8.47 ms at 16 KiB, 8.53 ms at 20 KiB.
-// COMP: the compensated variant, two blocks per SM (its float-float pair needs more
-// registers than 64).
+// COMP: the compensated variant, three blocks per SM (80 registers; its float-float pair
+// needs more than 64): 22.75 ms on the dusty ring against 23.0 ms with two blocks of 128.
 template <bool COMP>
-__global__ void __launch_bounds__(kThreads, COMP ? 2 : 4)
+__global__ void __launch_bounds__(kThreads, COMP ? 3 : 4)
 dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin* __restrict__ bins,
                       const int* __restrict__ perm, bool boxes, const int* __restrict__ src) {
     constexpr int NB = COMP ? 8 : 7;              // box values: 3 x (min, max), largest own[, smallest own]

@@ -6,6 +6,9 @@
   the mixed step orders its sources and tracers in space and takes far spans) with a
   4,096-grain shard: mixed precision against the oracle over 5 steps, and the FP64 step
   in the reference's arithmetic against the reference's own kernels over 3 steps.
+- Scale: all 16,777,216 grains with 65,536 gravitating planetesimals, two mixed steps; the
+  grains are test particles, so a 16,384-grain shard of them must step as it does in the
+  FP64 step of the same massive set with that shard alone.
 - Imaging: all 4,194,304 tracers at 1024 x 1024 and 10 wavelengths.  The FP64 image
   against the reference's own flux kernel (1e-11 per pixel, the same lit pixels: every
   tracer adds a positive flux, so a tracer binned to another pixel would change two
@@ -81,6 +84,34 @@ def test_ring_full_massive_set_fp64_matches_reference_kernels(engine, refk, ring
     assert rel_err(g, r, slice(0, s.n_grav)).max() < 1e-12
     live = r["N"][s.n_grav:] != 0
     assert rel_err(g, r, slice(s.n_grav, None))[live].max() < 1e-10
+
+
+def test_scale_full_size_mixed_matches_fp64_on_a_shard(engine):
+    n_shard = 16384
+    full = synth.dusty_ring(n_dust=16777216, n_plsml=65536, seed=synth.SEED + 4243, n_steps=500)
+    ng = full.n_grav
+    shard = synth.System(full.name, ng, {k: np.asarray(v)[:ng + n_shard].copy() for k, v in full.state.items()},
+                         full.dt, 2, full.phys, full.size_table)
+    engine.set_size_table(**full.size_table)
+    st = DeviceState.from_numpy(full.state)
+    full.state = None
+    engine.evolve(st, ng, full.dt, 2, make_phys(**full.phys), abi.DDX_PREC_MIXED, abi.DDX_MODE_FIXED)
+    torch.cuda.synchronize()
+    m = {k: getattr(st, k)[:ng + n_shard].cpu().numpy() for k in ("x", "y", "z", "N")}
+    alive = int((st.N[ng:] != 0).sum().item())
+    finite = bool(torch.isfinite(st.x[ng:]).all().item())
+    del st
+    torch.cuda.empty_cache()
+    f = run_gpu(engine, shard, 2, abi.DDX_PREC_FP64)
+    np.testing.assert_array_equal(m["N"] != 0, f["N"] != 0)
+    live = f["N"][ng:] != 0
+    ed = rel_err(m, f, slice(ng, None))[live]
+    em = rel_err(m, f, slice(0, ng))
+    print(f"scale mixed vs FP64 shard, 2 steps: dust median {np.median(ed):.3e} max {ed.max():.3e}; "
+          f"massive max {em.max():.3e}; {alive} of 16777216 grains alive")
+    assert finite and alive > 16_000_000
+    assert np.median(ed) < 1e-13 and ed.max() < 1e-11
+    assert em.max() < 1e-11
 
 
 @pytest.fixture(scope="module")
