@@ -425,6 +425,7 @@ constexpr float kEps32 = 5.9604645e-8f;   // 2^-24
 struct View32 {
     float cr, sr, ci, si, cp, sp;
     float inv_psca, hx, hy;               // 1/psca, 0.5 psca xsize, 0.5 psca ysize
+    double inv_psca64;                    // 1/psca in FP64 (the guard-band path)
     float inv_d;                          // 1/dist
     float htheta, cmax;                   // (ntheta-1)/2, 1 - 2/ntheta
     float Rmin, Rmax, fR, inv_fR;
@@ -438,6 +439,7 @@ View32 make_view32(const ddx_view& v, const OpticsDev& o) {
     w.ci = (float)cos(v.inc); w.si = (float)sin(v.inc);
     w.cp = (float)cos(v.PA); w.sp = (float)sin(v.PA);
     w.inv_psca = (float)(1.0 / psca);
+    w.inv_psca64 = 1.0 / psca;
     w.hx = (float)(0.5 * psca * v.xsize);
     w.hy = (float)(0.5 * psca * v.ysize);
     w.inv_d = (float)(1.0 / v.dist);
@@ -478,14 +480,28 @@ __device__ __forceinline__ bool near_edge32(float u, float g) {
 }
 
 // The FP64 decisions of the mixed image, out of line so that none of their FP64 work is
-// hoisted into the common FP32 path.
-__device__ __noinline__ void pixel_fp64(double x, double y, double z, const ViewConst& v, int& xim, int& yim,
-                                        unsigned long long* counters) {
+// hoisted into the common FP32 path.  R32: the tracer's FP32 radius from truncated
+// coordinates (at most 2^-22 below the FP64 one), so R32 (1 + 1e-6) bounds the radius from
+// above for the guard band without an FP64 square root.  The coordinates are scaled by the
+// reciprocal pixel size instead of divided (one more rounding, 3e-16 of the coordinate, far
+// inside the 1e-12 band), which keeps this path at about 25 FP64 operations (about 55 with
+// the square root and the three divisions).
+__device__ __forceinline__ void fast_pixel_coord_mul(double x, double y, double z, const ViewConst& v,
+                                                     double inv_psca, double& u, double& w) {
+    const double x1 = x * v.cr - y * v.sr;
+    const double y1 = x * v.sr + y * v.cr;
+    const double y2 = y1 * v.ci + z * v.si;
+    u = (x1 * v.cp - y2 * v.sp + 0.5 * v.psca * v.xsize) * inv_psca;
+    w = (x1 * v.sp + y2 * v.cp + 0.5 * v.psca * v.ysize) * inv_psca;
+}
+__device__ __noinline__ void pixel_fp64(double x, double y, double z, float R32, double inv_psca, const ViewConst& v,
+                                        int& xim, int& yim, unsigned long long* counters) {
     atomicAdd(&counters[1], 1ull);
-    const double Rd = sqrt(x * x + y * y + z * z);
+    const double Rd = (double)R32 * (1.0 + 1e-6);
     double ud, wd;
-    fast_pixel_coord(x, y, z, v, ud, wd);
-    const double gd = guard_width(Rd, fmax(fabs(ud), fabs(wd)), v);
+    fast_pixel_coord_mul(x, y, z, v, inv_psca, ud, wd);
+    // guard_width with R/psca as R * inv_psca: a bound either way (no FP64 division)
+    const double gd = 1e-12 * (Rd * inv_psca + fmax(fabs(ud), fabs(wd)) + 1.0);
     if (far_off_frame(ud, wd, gd, v)) {
         xim = yim = -1;
         return;
@@ -663,7 +679,7 @@ image_mixed_kernel(ddx_state s, int n_grav, int n_dust, const ViewConst* __restr
             int xim = -1, yim = -1;
             if (!reach) {
             } else if (near_edge32(u, g) || near_edge32(w, g)) {
-                pixel_fp64(x, y, z, *vcp, xim, yim, counters);
+                pixel_fp64(x, y, z, R, v32.inv_psca64, *vcp, xim, yim, counters);
             } else {
                 xim = (int)floorf(u);
                 yim = (int)floorf(w);
