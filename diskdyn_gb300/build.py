@@ -82,5 +82,27 @@ def build(verbose: bool = False) -> Path:
     return LIB
 
 
+DRIVER_SRC = PKG / "driver" / "ddyn_gb300.cpp"
+DRIVER = PKG / "ddyn_gb300"
+
+
+def build_driver(verbose: bool = False) -> Path:
+    """The ddyn_gb300 program (a whole run from a parameter file through the C ABI), linked
+    against libddx.so next to it."""
+    lib = build(verbose)
+    hs = [DRIVER_SRC] + list((ROOT / "include").glob("*.h"))
+    if DRIVER.exists() and DRIVER.stat().st_mtime >= max(lib.stat().st_mtime, *(h.stat().st_mtime for h in hs)):
+        return DRIVER
+    tmp = DRIVER.with_suffix(".tmp")
+    cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-ffp-contract=off", "-I", str(ROOT / "include"),
+           str(DRIVER_SRC), "-o", str(tmp), "-L", str(PKG), "-lddx", "-lcudart", "-Xlinker", "-rpath=$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build of ddyn_gb300 failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 if __name__ == "__main__":
     print(build(verbose=True))
+    print(build_driver(verbose=True))
