@@ -8,13 +8,14 @@
 // across spans.
 //
 // Far spans.  The low parts matter only for sources near the tracer: for a source at
-// distance r >= X/2 (X the largest |coordinate| of the two), the high parts alone give the
-// separation within e = (2 sqrt(3) 2^-23 + 2^-24) r = 4.7e-7 r, and the source's pull
+// distance r >= X/4 (X the largest |coordinate| of the two), the high parts alone give the
+// separation within e = (2 sqrt(3) 2^-22 + 2^-24) r = 8.9e-7 r, and the source's pull
 // within 4e (direction and r^-3), a few times the 5.6e-7 that rsqrt.approx and FP32
 // rounding leave in every pull; over 1,000 steps of the dusty ring the position errors
-// against FP64 did not move.  So a tracer takes a span with the high-part separation (3 of
-// the 9 separation operations) when the span's box (high parts of its 32 sources) lies at
-// least X/2 from the tracer's own point, X over the box and the point.  The choice depends
+// against FP64 did not move (from X/2 to X/4 neither).  So a tracer takes a span with the
+// high-part separation (3 of the 9 separation operations) when the span's box (high parts
+// of its 32 sources) lies at least X/4 from the tracer's own point, X over the box and the
+// point.  The choice depends
 // on the tracer and the sources alone, so a tracer's result does not depend on the others
 // or on their order.  The tracers are visited in cell order and the sources sit in their
 // pair records in cell order (ddx_order.cu), so the lanes of a warp lie close together and
@@ -248,7 +249,7 @@ __global__ void span_box_kernel(BodyPair* __restrict__ PP, int pcap, int n_src, 
 // span box (bx, by, bz: min and max per axis; xm: its largest |coordinate|, NaN when a
 // coordinate is NaN): far when the box lies at least X = kFar max(xm, own) away.  Rounded
 // operations only (no contraction), so the block tests below imply its outcome.
-constexpr float kFar = 0.5f;   // far from X/2 on (a power of two: the scaling is exact)
+constexpr float kFar = 0.25f;  // far from X/4 on (a power of two: the scaling is exact)
 
 __device__ __forceinline__ bool lane_far(float2 bx, float2 by, float2 bz, float xm, float xh, float yh, float zh,
                                          float own) {
