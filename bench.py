@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--scale-err-steps", type=int, default=500)
     p.add_argument("--adjoint-steps", type=int, default=2000)
     p.add_argument("--adjoint-plsml-steps", type=int, default=20)
+    p.add_argument("--adjoint-n-dust", type=int, default=262144, help="grains of the image-loss workload")
     return p.parse_args()
 
 
@@ -401,13 +402,13 @@ def run_ours(args, world, rank, local):
         line["configs"] = {"solar": solar_leg(local, fp64_peak), "imaging": imaging_leg(local),
                            "scale": scale_leg(local, fp32_peak)}
     if rank == 0 and args.adjoint_steps > 0:
-        line["adjoint"] = adjoint_leg(local, n_steps=args.adjoint_steps)
+        line["adjoint"] = adjoint_leg(local, n_dust=args.adjoint_n_dust, n_steps=args.adjoint_steps)
     if rank == 0 and args.adjoint_plsml_steps > 0:
         # the image-loss system with the dusty ring's 4,096 planetesimals in the massive set
         # (FP64 all-pairs, every grain feeling every planetesimal): fewer steps, since each FP64
         # step costs about 85 ms forward; forward, recompute and reverse all cost per step
         k = args.adjoint_plsml_steps
-        leg = adjoint_leg(local, n_steps=k, ckpt=max(1, k // 2), n_plsml=4096)
+        leg = adjoint_leg(local, n_dust=args.adjoint_n_dust, n_steps=k, ckpt=max(1, k // 2), n_plsml=4096)
         leg["steps_note"] = ("%d of the workload's 2,000 steps, checkpoints every %d: the forward, the "
                              "recompute and the reverse all cost per step" % (k, max(1, k // 2)))
         line["adjoint_planetesimals"] = leg
