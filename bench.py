@@ -406,7 +406,7 @@ def run_ours(args, world, rank, local):
     if rank == 0 and args.adjoint_plsml_steps > 0:
         # the image-loss system with the dusty ring's 4,096 planetesimals in the massive set
         # (FP64 all-pairs, every grain feeling every planetesimal): fewer steps, since each FP64
-        # step costs about 85 ms forward; forward, recompute and reverse all cost per step
+        # step costs about 150 ms forward; forward, recompute and reverse all cost per step
         k = args.adjoint_plsml_steps
         leg = adjoint_leg(local, n_dust=args.adjoint_n_dust, n_steps=k, ckpt=max(1, k // 2), n_plsml=4096)
         leg["steps_note"] = ("%d of the workload's 2,000 steps, checkpoints every %d: the forward, the "
