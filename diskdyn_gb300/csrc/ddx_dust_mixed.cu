@@ -44,8 +44,9 @@
 // FP64 stage positions instead (the FP64 step's arithmetic).  The loop over a span of 32
 // sources keeps the largest FP32 reciprocal distance (one three-input max per pair
 // record); a span whose largest exceeds 1 / (near_eta own) is summed again without its
-// near sources, which are added in FP64.  Far spans never hold a near source (near_eta is
-// at most a quarter, far spans start at a half).
+// near sources, which are added in FP64.  Far spans hold no source nearer than the near
+// radius (near_eta is at most a quarter, and far spans start a quarter of the largest
+// coordinate away).
 //
 // Compensated variant (DDX_PREC_COMPENSATED).  The near radius does not bound the largest
 // errors: in this chaotic system a grain amplifies the FP32 rounding of every planetesimal

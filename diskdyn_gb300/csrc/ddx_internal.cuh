@@ -56,8 +56,8 @@ __host__ __device__ inline float default_near_eta(int precision) {
 // Default radius of the float-float spans of DDX_PREC_COMPENSATED, relative to the tracer's
 // largest |coordinate|.
 constexpr float kDefaultCompEta = 0.5f;
-// Largest accepted near radius: far spans (dust kernel) start at half the largest coordinate,
-// so a near source can never sit in a far span.
+// Largest accepted near radius: far spans (dust kernel) start a quarter of the largest
+// coordinate away, so a far span holds no source nearer than the near radius.
 constexpr float kMaxNearEta = 0.25f;
 
 // 1 / (near_eta * own): a source is near when its FP32 reciprocal distance exceeds this
@@ -118,7 +118,7 @@ constexpr int kOrderBits = 6;                                   // cell index bi
 constexpr uint32_t kOrderBins = 1u << (3 * kOrderBits);         // cells; one more for removed bodies
 cudaError_t order_alloc(OrderScratch& o, int cap, bool stable);
 void order_free(OrderScratch& o);
-// Orders bodies [first, first + n) of s by the Morton code of their cell on a grid over
+// Orders bodies [first, first + n) of s by the Hilbert index of their cell on a grid over
 // their bounding box (64^3 cells; 32^3 and equal codes in index order when o is stable):
 // perm[position] = body - first and, when inv is given, inv[body - first] = position.  With
 // dead_last, bodies with N == 0 come last.  Stream-ordered.

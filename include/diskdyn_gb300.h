@@ -130,8 +130,9 @@ int ddx_set_optics(ddx_ctx *ctx, int n_grid, int n_wav, int n_theta, const doubl
  *     massive_RK4(dt); small_RK4(dt); massive_final(dt);   (src/grid.cu:387-389)
  * The size table must be set.  `precision` is DDX_PREC_*, `mode` is DDX_MODE_*.
  * DDX_PREC_MIXED with 1,024 planetesimals or more visits the tracers and reads the FP32
- * planetesimals in a spatial order (Morton cells) and takes planetesimals farther from a
- * tracer than half the largest |coordinate| of the two with the FP32 high parts alone.
+ * planetesimals in a spatial order (Hilbert cells) and takes spans of 32 planetesimals that
+ * lie at least a quarter of the largest |coordinate| of the two away from a tracer with the
+ * FP32 high parts alone.
  * Each tracer's result depends on its own data and the massive set only (not on the
  * other tracers or their order), and the result is the same from run to run. */
 int ddx_step(ddx_ctx *ctx, const ddx_state *s, int n_grav, int n_dust, double dt,
