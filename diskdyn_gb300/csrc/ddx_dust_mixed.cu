@@ -773,7 +773,8 @@ cudaError_t launch_dust_mixed(const ddx_state& s, const StepArgs& a, const Massi
     bool boxes = false;
     const int n_src = a.n_grav - a.n_exact;
     if (ms.slot && ms.dust_order.cap >= a.n_dust && spatial_order_on(a)) {
-        cudaError_t e = order_bodies(s, a.n_grav, a.n_dust, true, ms.dust_order, ms.dust_order.perm, nullptr, st);
+        cudaError_t e =
+            order_bodies(s, a.n_grav, a.n_dust, true, ms.dust_order, ms.dust_order.perm, nullptr, !comp, st);
         if (e != cudaSuccess) return e;
         const int nspans = pair_count(n_src) / kPairSpan;
         span_box_kernel<<<(4 * nspans * 32 + 127) / 128, 128, 0, st>>>(ms.PP, ms.pcap, n_src, nspans);

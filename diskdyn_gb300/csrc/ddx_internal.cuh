@@ -118,12 +118,13 @@ constexpr int kOrderBits = 6;                                   // cell index bi
 constexpr uint32_t kOrderBins = 1u << (3 * kOrderBits);         // cells; one more for removed bodies
 cudaError_t order_alloc(OrderScratch& o, int cap, bool stable);
 void order_free(OrderScratch& o);
-// Orders bodies [first, first + n) of s by the Hilbert index of their cell on a grid over
-// their bounding box (64^3 cells; 32^3 and equal codes in index order when o is stable):
-// perm[position] = body - first and, when inv is given, inv[body - first] = position.  With
-// dead_last, bodies with N == 0 come last.  Stream-ordered.
+// Orders bodies [first, first + n) of s by the code of their cell on a grid over their
+// bounding box (64^3 cells; 32^3 and equal codes in index order when o is stable): the
+// Hilbert index on cubic cells when hilbert, else the Morton code on cells stretched to the
+// box per axis.  perm[position] = body - first and, when inv is given, inv[body - first] =
+// position.  With dead_last, bodies with N == 0 come last.  Stream-ordered.
 cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, const OrderScratch& o, int* perm,
-                         int* inv, cudaStream_t st);
+                         int* inv, bool hilbert, cudaStream_t st);
 
 // The mixed step orders its tracers and FP32 sources in space (far spans, ddx_order.cu)
 // from this many sources on.  With fewer, the dust kernel is short and the orders and span

@@ -3,12 +3,20 @@
 // span of pair records and the tracers of a warp each lie in a small region, and a tracer
 // far from a span can take the separation from the high parts alone.
 //
-// The order: the bodies' bounding box (in FP32), cubic cells over it (the box's largest
-// extent cut into 2^bits on every axis, so a thin disk is not cut into slabs), and the
-// Hilbert index of the cell (cells next to each other on the curve are next to each other in
-// space), sorted in one of two ways.  Against Morton codes on cells stretched to the box per
-// axis, the spans of 32 dusty-ring planetesimals shrank from a median radius of 37 AU to 12
-// AU, more of them became far spans, and the dust kernel went from 8.02 to 7.75 ms:
+// The order: the bodies' bounding box (in FP32), a cell per body on a 2^bits grid over it,
+// and a code per cell that puts cells close on the curve close in space, in one of two forms:
+//  - the Hilbert index on cubic cells (the box's largest extent cut into 2^bits on every
+//    axis, so a thin disk is not cut into slabs), for DDX_PREC_MIXED.  Against the Morton
+//    form the spans of 32 dusty-ring planetesimals shrank from a median radius of 37 AU to
+//    12 AU, 89 % of the tracer-span pairs were far instead of 81 %, and the dust kernel went
+//    from 8.02 to 7.75 ms (cubic Morton cells alone: 7.79 ms);
+//  - the Morton code (x, y, z bits interleaved) on cells stretched to the box per axis, for
+//    DDX_PREC_COMPENSATED.  Its longer spans take more sources into the float-float form per
+//    span test: over 1,000 steps of four 16,384-grain shards its worst grains were 6.0e-10,
+//    2.0e-9, 5.0e-10 and 4.7e-10 from FP64 at 24.8 ms a step, where the Hilbert order gave
+//    1.5e-9, 1.9e-9, 6.3e-10 and 8.9e-10 at 21.8 ms, and needed the float-float radius doubled
+//    (30.6 ms) to come to 8.6e-10, 1.8e-9, 8.6e-10 and 8.6e-10.
+// The codes are sorted in one of two ways:
 //  - counting sort (the tracers: 6 bits per axis): an atomic increment gives each body its
 //    rank in its cell, an exclusive scan of the cell counts the cells' first positions, and
 //    perm[start + rank] = body.  The order inside a cell follows the atomics, which is
@@ -119,27 +127,38 @@ __device__ __forceinline__ uint32_t hilbert_index(uint32_t c0, uint32_t c1, uint
     return key;
 }
 
-// Hilbert index of the cell of v on a (1 << bits)^3 grid of cubic cells over the box [lo, hi]
-// (the largest extent sets the cell size on every axis).
-__device__ __forceinline__ uint32_t cell_code(const float* v, const float* lo, const float* hi, int bits) {
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {   // bit b of v to bit 3b
+    uint32_t r = 0;
+#pragma unroll
+    for (int b = 0; b < kOrderBits; ++b) r |= ((v >> b) & 1u) << (3 * b);
+    return r;
+}
+
+// Code of the cell of v on a (1 << bits)^3 grid over the box [lo, hi]: hilbert, the Hilbert
+// index on cubic cells (the largest extent sets the cell size on every axis); else the
+// Morton code on cells stretched to the box per axis.
+__device__ __forceinline__ uint32_t cell_code(const float* v, const float* lo, const float* hi, int bits,
+                                              bool hilbert) {
     const int cells = 1 << bits;
     const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-    const float scale = ext > 0.0f ? (float)cells / ext : 0.0f;
     uint32_t c[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
+        const float e = hilbert ? ext : hi[a] - lo[a];
+        const float scale = e > 0.0f ? (float)cells / e : 0.0f;
         // NaN, or a span too wide for FP32, gives cell 0 or the last: any cell is valid
         const float u = fminf(fmaxf((v[a] - lo[a]) * scale, 0.0f), (float)(cells - 1));
         c[a] = (uint32_t)(u == u ? (int)u : 0);
     }
-    return hilbert_index(c[0], c[1], c[2], bits);
+    return hilbert ? hilbert_index(c[0], c[1], c[2], bits) : spread3(c[0]) << 2 | spread3(c[1]) << 1 | spread3(c[2]);
 }
 
 // The whole stable order of up to kSmallOrder bodies in one block.
 constexpr int kSmallOrder = 8192;        // index < 2^13 below the 15-bit code + removed bit
 constexpr int kSmallThreads = 1024;
 __global__ void __launch_bounds__(kSmallThreads)
-order_small_kernel(ddx_state s, int first, int n, bool dead_last, int* __restrict__ perm, int* __restrict__ inv) {
+order_small_kernel(ddx_state s, int first, int n, bool dead_last, bool hilbert, int* __restrict__ perm,
+                   int* __restrict__ inv) {
     __shared__ uint32_t keys[kSmallOrder];
     __shared__ float red[kSmallThreads / 32][6];
     __shared__ float box[6];
@@ -177,7 +196,7 @@ order_small_kernel(ddx_state s, int first, int n, bool dead_last, int* __restric
             if (!(dead_last && removed(s, first + k))) {
                 const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]),
                                     d2f_toward0(s.z[first + k])};
-                code = cell_code(v, box, box + 3, kBits);
+                code = cell_code(v, box, box + 3, kBits, hilbert);
             }
             key = code << 13 | (uint32_t)k;
         }
@@ -201,10 +220,11 @@ order_small_kernel(ddx_state s, int first, int n, bool dead_last, int* __restric
     }
 }
 
-// Hilbert index of each body's cell (bits per axis; removed bodies get 1 << 3 bits when
+// Code of each body's cell (bits per axis; removed bodies get 1 << 3 bits when
 // dead_last).  count given: rank[k] = the body's rank in its cell by an atomic increment;
 // else rank[k] = k (the values of the stable sort).
-__global__ void order_keys_kernel(ddx_state s, int first, int n, bool dead_last, int bits, const int* __restrict__ box,
+__global__ void order_keys_kernel(ddx_state s, int first, int n, bool dead_last, int bits, bool hilbert,
+                                  const int* __restrict__ box,
                                   uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
                                   uint32_t* __restrict__ count) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -214,7 +234,7 @@ __global__ void order_keys_kernel(ddx_state s, int first, int n, bool dead_last,
         const float v[3] = {d2f_toward0(s.x[first + k]), d2f_toward0(s.y[first + k]), d2f_toward0(s.z[first + k])};
         const float lo[3] = {float_of(box[0]), float_of(box[1]), float_of(box[2])};
         const float hi[3] = {float_of(box[3]), float_of(box[4]), float_of(box[5])};
-        bin = cell_code(v, lo, hi, bits);
+        bin = cell_code(v, lo, hi, bits, hilbert);
     }
     key[k] = bin;
     rank[k] = count ? atomicAdd(&count[bin], 1u) : (uint32_t)k;
@@ -353,11 +373,11 @@ void order_free(OrderScratch& o) {
 }
 
 cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, const OrderScratch& o, int* perm,
-                         int* inv, cudaStream_t st) {
+                         int* inv, bool hilbert, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (n > o.cap) return cudaErrorInvalidValue;
     if (o.stable && n <= kSmallOrder) {
-        order_small_kernel<<<1, kSmallThreads, 0, st>>>(s, first, n, dead_last, perm, inv);
+        order_small_kernel<<<1, kSmallThreads, 0, st>>>(s, first, n, dead_last, hilbert, perm, inv);
         return cudaGetLastError();
     }
     const int blk = (n + kThreads - 1) / kThreads;
@@ -365,14 +385,16 @@ cudaError_t order_bodies(const ddx_state& s, int first, int n, bool dead_last, c
     order_box_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, o.box);
     if (o.stable) {
         constexpr int kBits = kOrderBits - 1;   // 32^3 cells: two 8-bit digit passes
-        order_keys_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, kBits, o.box, o.key, o.rank, nullptr);
+        order_keys_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, kBits, hilbert, o.box, o.key, o.rank,
+                                                    nullptr);
         uint32_t *ko = nullptr, *vo = nullptr;
         cudaError_t e = radix_sort_stable(o.key, o.rank, n, 3 * kBits + 1, o.temp, &ko, &vo, st);
         if (e != cudaSuccess) return e;
         order_from_sorted_kernel<<<blk, kThreads, 0, st>>>(n, vo, perm, inv);
         return cudaGetLastError();
     }
-    order_keys_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, kOrderBits, o.box, o.key, o.rank, o.count);
+    order_keys_kernel<<<blk, kThreads, 0, st>>>(s, first, n, dead_last, kOrderBits, hilbert, o.box, o.key, o.rank,
+                                                o.count);
     cudaError_t e = exclusive_scan(o.count, o.start, (int)kOrderBins + 1, o.temp, nullptr, st);
     if (e != cudaSuccess) return e;
     order_scatter_kernel<<<blk, kThreads, 0, st>>>(n, o.key, o.rank, o.start, perm, inv);

@@ -642,7 +642,8 @@ cudaError_t launch_massive_prepare(const ddx_state& s, const StepArgs& a, Massiv
     // the FP32 sources' pair slots in cell order, from their positions at the start of the step
     if (precision != DDX_PREC_FP64 && ms.slot && spatial_order_on(a)) {
         const cudaError_t e =
-            order_bodies(s, a.n_exact, a.n_grav - a.n_exact, false, ms.src_order, nullptr, ms.slot, st);
+            order_bodies(s, a.n_exact, a.n_grav - a.n_exact, false, ms.src_order, nullptr, ms.slot,
+                         precision == DDX_PREC_MIXED, st);
         if (e != cudaSuccess) return e;
     }
     const int threads = 128;
