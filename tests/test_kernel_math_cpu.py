@@ -8,6 +8,9 @@
    adjacent lanes on one pixel are summed by a segmented tree of five shuffle-down steps;
    each run's first lane must end with the run's sum, so every tracer's flux reaches its
    pixel exactly once.
+3. The spatial order's Hilbert index (csrc/ddx_order.cu, hilbert_index): on a grid of
+   2^bits cells per axis it must number every cell once, and consecutive indices must be
+   face neighbours, so that a run of bodies in index order stays in a compact region.
 """
 import numpy as np
 
@@ -91,3 +94,46 @@ def test_segmented_warp_sum_gives_each_run_to_its_first_lane():
                 r += 1
             assert abs(v[l] - f[l:r + 1].sum()) < 1e-12
         assert abs(v[valid & head].sum() - f.sum()) < 1e-9
+
+
+def hilbert_index(c, bits):
+    """hilbert_index of csrc/ddx_order.cu, step for step: Skilling's transform of the axes to
+    the transposed index, the Gray code, then the bits interleaved (axis 0 first)."""
+    X = list(c)
+    M = 1 << (bits - 1)
+    Q = M
+    while Q > 1:
+        P = Q - 1
+        for i in range(3):
+            if X[i] & Q:
+                X[0] ^= P
+            else:
+                t = (X[0] ^ X[i]) & P
+                X[0] ^= t
+                X[i] ^= t
+        Q >>= 1
+    X[1] ^= X[0]
+    X[2] ^= X[1]
+    t, Q = 0, M
+    while Q > 1:
+        if X[2] & Q:
+            t ^= Q - 1
+        Q >>= 1
+    X = [x ^ t for x in X]
+    key = 0
+    for b in range(bits - 1, -1, -1):
+        for i in range(3):
+            key = key << 1 | ((X[i] >> b) & 1)
+    return key
+
+
+def test_hilbert_index_numbers_every_cell_once_in_face_neighbour_steps():
+    for bits in (1, 2, 3, 5):   # 5: the planetesimals' grid (the tracers' 6 bits follow the same steps)
+        n = 1 << bits
+        cells = [(x, y, z) for x in range(n) for y in range(n) for z in range(n)]
+        keys = [hilbert_index(c, bits) for c in cells]
+        assert sorted(keys) == list(range(n ** 3))
+        walk = [c for _, c in sorted(zip(keys, cells))]
+        assert walk[0] == (0, 0, 0)
+        steps = np.abs(np.diff(np.array(walk), axis=0)).sum(axis=1)
+        assert (steps == 1).all()
