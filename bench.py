@@ -35,11 +35,12 @@ WORKLOAD = "dusty_ring"
 # star term (gravity reduced by beta + PR/stellar-wind drag), per tracer per stage.
 FLOP_PAIR = 20
 FLOP_STAR = 45
-# Mixed dust kernel, bytes per grain and launch: DRAM traffic measured by ncu (20.73 MB read
-# + 9.74 MB written for 262,144 grains with 16 KiB tiles: `ncu --set full -k
-# regex:"dust_rk4_mixed_kernel"` on `bench.py --n-dust 262144`), and the algorithmic bytes
-# (the state read, 68 B, and the positions, velocities and grain number written, 56 B).
-DUST_TRAFFIC_PER_GRAIN = (20.73e6 + 9.74e6) / 262144
+# Mixed dust kernel, bytes per grain and launch: DRAM traffic measured by ncu (20.65 MB read
+# + 6.20 MB written for 262,144 grains: `ncu --set full -k regex:"dust_rk4_mixed_kernel"` on
+# `bench.py --n-dust 262144`; writes still in L2 when the kernel ends are not counted), and
+# the algorithmic bytes (the state read, 68 B, and the positions, velocities and grain
+# number written, 56 B).
+DUST_TRAFFIC_PER_GRAIN = (20.65e6 + 6.20e6) / 262144
 ALG_BYTES_PER_GRAIN = 68 + 56
 
 
