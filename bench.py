@@ -1057,6 +1057,9 @@ def run_reference(args, world, rank, local):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                              "sample": f"each step: {ng} massive bodies + {n_sample} grains of the workload"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["sample_note"] = ("every counted body, massive or grain, takes n_grav - 1 = %d pair interactions per "
+                           "stage in the sample and in the full workload alike, so the sample's rate stands for the "
+                           "full workload's" % (ng - 1))
     try:
         import oracle.refk as rk
         if rk.available():
