@@ -34,3 +34,26 @@ def test_driver_rejects_bad_arguments_and_files(tmp_path):
     r = subprocess.run([str(exe), str(bad), "--table", "x", "--spec", "y", "--dry-run"], capture_output=True,
                        text=True, timeout=60)
     assert r.returncode != 0 and "rejected" in r.stderr
+
+
+def test_driver_dry_run_reads_the_reference_systems():
+    """The reference's own test systems (tests/*.param of its checkout), each read by the
+    program with a synthetic Mie table and spectrum in the reference's formats: the counts
+    it prints are those of the same files read through the Python API."""
+    from oracle.ref import paths
+    paths.require(paths.TESTS, "the reference's test systems")
+    exe = build.build_driver()
+    table, spec = GOLD / "optics" / "t1_table.dat", GOLD / "optics" / "s1_spec.dat"
+    t = formats.read_optical(table)
+    systems = sorted(paths.TESTS.glob("*.param"))
+    assert len(systems) >= 13
+    for param in systems:
+        r = subprocess.run([str(exe), str(param), "--table", str(table), "--spec", str(spec), "--dry-run"],
+                           capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, (param.name, r.stderr)
+        p = formats.read_param_struct(param)
+        formats.param_grid(p, t["dmin"], t["dmax"])
+        run = formats.setup_count(p, t["dmin"], t["dmax"])
+        want = (f"system: {p.n_planets + run.n_mass} massive ({p.n_planets} star and planets), {run.n_dust} "
+                f"grain tracers, {p.n_grid} size bins, {t['w'].size} wavelengths")
+        assert r.stdout.strip() == want, param.name
