@@ -382,8 +382,8 @@ __device__ __forceinline__ void near_span_ff(const BodyPair* R, const f2* ML, in
     }
 }
 
-// Kahan sums across spans.  The compensated variant keeps both lanes (float-float span sums:
-// high parts through the Kahan sum, low parts into its compensation).  The FP32 forms add
+// Kahan sums across the FP32 spans.  The compensated variant keeps both lanes (its
+// float-float spans go to the FP64 acceleration instead, ff_total).  The FP32 forms add
 // the span's two lanes (one rounding, against the 16 of each lane's plain sum) and carry one
 // FP32 sum per axis: six registers fewer in the loop, which the dusty-ring dust kernel took
 // from 8.18 to 8.00 ms.
@@ -391,7 +391,6 @@ template <bool F2> struct SpanAcc;
 template <> struct SpanAcc<true> {
     f2 S = 0, C = 0;
     __device__ __forceinline__ void add(f2 v) { kahan2(S, C, v); }
-    __device__ __forceinline__ void sub_lo(f2 l) { C = sub2(C, l); }
     __device__ __forceinline__ double total() const { return f2_total(S, C); }
 };
 template <> struct SpanAcc<false> {
@@ -404,9 +403,23 @@ template <> struct SpanAcc<false> {
         C = __fsub_rn(__fsub_rn(t, S), y);
         S = t;
     }
-    __device__ __forceinline__ void sub_lo(f2) {}
     __device__ __forceinline__ double total() const { return (double)S - (double)C; }
 };
+
+// A float-float span sum (both lanes' high parts H and low parts L) in FP64: the lanes' high
+// parts added exactly (TwoSum), the error and the low parts in FP32, then two FP64 adds.  The
+// compensated variant adds its float-float spans to the stage's FP64 acceleration this way
+// rather than through the FP32 Kahan sum, whose error grows as the number of spans times
+// 2^-48 of the magnitudes summed: on the dusty ring the 99th percentile of the 1,000-step
+// errors halved (1.0e-11 to 5.1e-12), for 0.2 ms of the 24.8 ms step.
+__device__ __forceinline__ double ff_total(f2 H, f2 L) {
+    float a, b, la, lb;
+    f2_split(H, a, b);
+    f2_split(L, la, lb);
+    const float s = __fadd_rn(a, b), v = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v));
+    return (double)s + (double)__fadd_rn(__fadd_rn(la, lb), e);
+}
 
 // Spans with one bit per block test (all far, all near) in shared memory, per stage; beyond
 // this many spans every tracer tests every span itself.
@@ -650,8 +663,7 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
             for (int k = 0; k < cnt; k += kPairSpan) {
                 f2 px = 0, py = 0, pz = 0;
                 if (COMP && ((cm >> (k / kPairSpan)) & 1u)) {
-                    // float-float span sums, folded into the compensated running sums: the
-                    // high parts through kahan2, the low parts straight into its compensation
+                    // float-float span sums, added to the stage's FP64 acceleration
                     f2 SH[3] = {0, 0, 0}, SL[3] = {0, 0, 0};
                     const f2* ML = reinterpret_cast<const f2*>(ms.PM + (size_t)st * ms.pcap + tt * kTilePairs + k);
                     float mx = 0.f;
@@ -664,8 +676,7 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
                     if (mx > inv_near)   // a source within the near radius: its pull in FP64
                         near_span_ff(T + k, ML, 2 * (tt * kTilePairs + k), XH, XL, YH, YL, ZH, ZL, xr, yr, zr,
                                      inv_near, Pn, src, SH, SL, kx, ky, kz);
-                    ax.add(SH[0]); ay.add(SH[1]); az.add(SH[2]);
-                    ax.sub_lo(SL[0]); ay.sub_lo(SL[1]); az.sub_lo(SL[2]);
+                    kx += ff_total(SH[0], SL[0]); ky += ff_total(SH[1], SL[1]); kz += ff_total(SH[2], SL[2]);
                     continue;
                 }
                 if ((fm >> (k / kPairSpan)) & 1u) {
@@ -715,7 +726,9 @@ dust_rk4_mixed_kernel(ddx_state s, StepArgs a, MassiveScratch ms, const SizeBin*
         if (alive) {
             const double px = ax.total(), py = ay.total(), pz = az.total();
             // An exact coincidence makes RR = 0, the rsqrt infinite and the sum NaN.
-            if (!(isfinite(px) && isfinite(py) && isfinite(pz))) {
+            // (the compensated variant has added its float-float spans to k already)
+            if (!(isfinite(px) && isfinite(py) && isfinite(pz) &&
+                  (!COMP || (isfinite(kx) && isfinite(ky) && isfinite(kz))))) {
                 alive = false; removed = 2; removed_stage = st;
             }
             kx += px; ky += py; kz += pz;
