@@ -8,7 +8,7 @@ the FP64 step's position.  The plain mixed step stays near 3e-11 at the median b
 1e-8 and more off for a few grains: this chaotic system amplifies the FP32 rounding of the
 pulls by three to four orders of magnitude, and float-float removes most of it.  The worst
 grain of a shard still varies from draw to draw (on one of four shards measured it ends
-2.0e-9 away); the test holds the bench's shard to the target and every shard's 99th
+2.3e-9 away); the test holds the bench's shard to the target and every shard's 99th
 percentile far below it.
 """
 import ctypes as C
